@@ -1,0 +1,85 @@
+// Fused training march: workspace layout shared by march.cu, mlp.cu and
+// train.cu.
+#pragma once
+#include "pvdb_internal.cuh"
+#include "ray_ops.cuh"
+
+namespace pvdb {
+
+// Per-launch constants of the march (device copy of pvdb_march_params plus
+// derived values).
+struct MarchP {
+  float mn[3], mx[3];
+  float ext[3];   // xyz_max - xyz_min (float, as torch computes it)
+  float wsm1[3];  // world_size - 1 (as float)
+  float near_, far_, stepdist, shift, interval, thr, t_stop, bg;
+  const uint8_t* mask;
+  int mshape[3];
+  float mscale[3], mshift[3];
+  int cap;
+};
+
+// Device pointers of the workspace, passed by value to kernels.
+struct MarchW {
+  // per ray
+  float* ray_sd;  // [R*6] sample origin (rays_o + rays_d*t_min) and unit direction
+  float* T_last;
+  uint32_t* n_kept;
+  uint32_t* n_color;
+  uint32_t* kept_off;
+  uint32_t* color_off;
+  // per (ray, kept slot): index r*cap + i
+  float* k_alpha;
+  float* k_w;
+  int32_t* k_step;  // sample index along the ray; bit 31 set for colour samples
+  int32_t* k_row;   // colour row of the sample, -1 otherwise
+  // per colour row
+  float* r_k0;
+  float* r_w;
+  float* r_alpha;
+  int32_t* r_ray;
+  int32_t* r_step;
+  // per kept sample (global kept index), backward
+  float* b_pos;
+  float* b_gsig;
+  int32_t* b_row;
+  // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
+  uint32_t* totals;
+};
+
+}  // namespace pvdb
+
+struct pvdb_march_s {
+  int max_rays = 0;
+  int cap = 0;
+  int64_t slots = 0;  // max_rays * cap
+  int k0_channels = 0;
+  pvdb::MarchW w{};
+  pvdb::ReduceScratch red;   // contributions (8 per kept sample)
+  pvdb::ReduceScratch red2;  // second reduction when k0 has its own topology
+  uint32_t* scan_partial = nullptr;
+  size_t scan_partial_cap = 0;
+  // state of the last forward
+  pvdb::MarchP p{};
+  int n_rays = 0;
+  bool has_fwd = false;
+  bool prof = false;  // record stage-profiler marks (set by the train step)
+  pvdb_grid_s* density = nullptr;
+  pvdb_grid_s* k0 = nullptr;
+  // rgbnet scratch (mlp.cu)
+  float* hpe = nullptr;          // [max_rays, width] per-ray layer-0 PE part + bias
+  size_t hpe_cap = 0;
+  float* wpart = nullptr;        // per-CTA partial weight gradients
+  size_t wpart_cap = 0;
+  void* mlp_packed = nullptr;    // packed BF16 weights for the tensor-core path
+  size_t mlp_packed_cap = 0;
+  // train-step scratch (train.cu)
+  float* t_rgb = nullptr;        // [M_max,3]
+  float* t_grad_rgb = nullptr;   // [M_max,3]
+  float* t_grad_w = nullptr;     // [M_max]
+  float* t_grad_k0 = nullptr;    // [M_max, C]
+  float* t_grad_last = nullptr;  // [max_rays]
+  float* t_loss_part = nullptr;  // [max_rays]
+  float* t_rgb_marched = nullptr;  // [max_rays,3]
+  size_t t_cap_rows = 0;
+};

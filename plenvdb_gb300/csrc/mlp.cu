@@ -1,0 +1,531 @@
+// rgbnet: Linear(C0+Dpe -> 128) ReLU Linear(128 -> 128) ReLU Linear(128 -> 3),
+// then sigmoid (dvgo.py:91-107, :354-362), evaluated on the colour rows of a
+// march workspace. Layer 0 is split into the per-row k0 part and a per-ray
+// part W0[:,C0:]·PE(viewdir) + b0 computed once per ray (the reference
+// renderer hoists it the same way, renderer.cu:100-101).
+//
+// FP32 SIMT kernels: persistent CTAs over 64-row tiles; every thread owns a
+// 4-row x 8-column block (columns strided by 16 so the padded weight rows are
+// read without bank conflicts). The backward recomputes the activations of its
+// tile, and accumulates the weight gradients of all tiles it visits in
+// registers; per-CTA partials are summed in CTA order by k_wgrad_reduce, so the
+// weight gradients are deterministic for a given grid size.
+#include <algorithm>
+
+#include "march.cuh"
+
+namespace pvdb {
+
+constexpr int kW = 128;       // hidden width
+constexpr int kTile = 64;     // rows per tile
+constexpr int kMaxC0 = 16;    // k0 channels
+constexpr int kMaxPe = 32;    // PE dims
+constexpr int kW1S = kW + 1;  // padded row stride of W1 in shared memory
+constexpr int kAS = kTile + 4;  // row stride of transposed activation tiles
+constexpr int kMlpThreads = 256;
+
+struct MlpArgs {
+  const float* w0; const float* b0;
+  const float* w1; const float* b1;
+  const float* w2; const float* b2;
+  int c0, dpe, din;  // din = c0 + dpe
+};
+
+// Flat parameter layout shared with the train step and the Python side:
+// [w0 (128 x din), b0 (128), w1 (128 x 128), b1 (128), w2 (3 x 128), b2 (3)].
+__host__ __device__ inline int64_t mlp_param_count(int din) { return int64_t(kW) * din + kW + kW * kW + kW + 3 * kW + 3; }
+
+// PE of a unit view direction: [d, sin(d*2^i) (i-major per axis), cos(...)]
+// (dvgo.py:354-355).
+__device__ __forceinline__ void view_pe(const float d[3], int npe, float* out) {
+  out[0] = d[0]; out[1] = d[1]; out[2] = d[2];
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i < npe; ++i) {
+      const float x = d[a] * float(1 << i);
+      out[3 + a * npe + i] = sinf(x);
+      out[3 + 3 * npe + a * npe + i] = cosf(x);
+    }
+}
+
+// Per ray: pe[r][0:dpe] and hpe[r][n] = b0[n] + sum_q w0[n][c0+q] * pe[r][q].
+__global__ void k_pe_hpe(const float* __restrict__ viewdirs, int R, int npe, MlpArgs a,
+                         float* pe_out, float* hpe) {
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (t >= int64_t(R) * kW) return;
+  const int r = int(t / kW), n = int(t % kW);
+  const float d[3] = {viewdirs[r * 3], viewdirs[r * 3 + 1], viewdirs[r * 3 + 2]};
+  float pe[kMaxPe];
+  view_pe(d, npe, pe);
+  float s = 0.f;
+  for (int q = 0; q < a.dpe; ++q) s = fmaf(a.w0[n * a.din + a.c0 + q], pe[q], s);
+  hpe[t] = a.b0[n] + s;
+  if (n < a.dpe) pe_out[int64_t(r) * kMaxPe + n] = pe[n];
+}
+
+struct MlpSmem {
+  float w1[kW * kW1S];
+  float w0k[kW * (kMaxC0 + 1)];
+  float w2[3 * kW];
+  float b1[kW];
+  float b2[4];
+  float x[kTile * kMaxC0];  // k0 rows of the tile
+  float h0t[kW * kAS];      // relu(layer 0), transposed [n][row]
+};
+
+__device__ void mlp_load_weights(MlpSmem& S, const MlpArgs& a) {
+  for (int i = threadIdx.x; i < kW * kW; i += blockDim.x) S.w1[(i / kW) * kW1S + (i % kW)] = a.w1[i];
+  for (int i = threadIdx.x; i < kW * a.c0; i += blockDim.x)
+    S.w0k[(i / a.c0) * (kMaxC0 + 1) + (i % a.c0)] = a.w0[(i / a.c0) * a.din + (i % a.c0)];
+  for (int i = threadIdx.x; i < 3 * kW; i += blockDim.x) S.w2[i] = a.w2[i];
+  for (int i = threadIdx.x; i < kW; i += blockDim.x) S.b1[i] = a.b1[i];
+  if (threadIdx.x < 3) S.b2[threadIdx.x] = a.b2[threadIdx.x];
+}
+
+// Layer 0 and layer 1 of one tile; returns relu(layer 1) in h1[4][8] for rows
+// ty*4+i and columns tx+16*j. Leaves relu(layer 0) in S.h0t.
+__device__ __forceinline__ void mlp_tile_forward(MlpSmem& S, const MlpArgs& a,
+                                                 const float* __restrict__ k0,
+                                                 const int32_t* __restrict__ ray,
+                                                 const float* __restrict__ hpe, int64_t row0,
+                                                 int64_t M, float h1[4][8]) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int i = threadIdx.x; i < kTile * a.c0; i += blockDim.x) {
+    const int rr = i / a.c0, q = i % a.c0;
+    const int64_t m = row0 + rr;
+    S.x[rr * kMaxC0 + q] = m < M ? k0[m * a.c0 + q] : 0.f;
+  }
+  __syncthreads();
+  // layer 0
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int rr = ty * 4 + i;
+    const int64_t m = row0 + rr;
+    const int r = m < M ? ray[m] : -1;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = tx + 16 * j;
+      float z = r >= 0 ? hpe[int64_t(r) * kW + n] : 0.f;
+      for (int q = 0; q < a.c0; ++q) z = fmaf(S.w0k[n * (kMaxC0 + 1) + q], S.x[rr * kMaxC0 + q], z);
+      S.h0t[n * kAS + rr] = fmaxf(z, 0.f);
+    }
+  }
+  __syncthreads();
+  // layer 1
+  float acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < kW; ++k) {
+    const float4 av = *reinterpret_cast<const float4*>(&S.h0t[k * kAS + ty * 4]);
+    const float aa[4] = {av.x, av.y, av.z, av.w};
+    float bb[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) bb[j] = S.w1[(tx + 16 * j) * kW1S + k];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) h1[i][j] = fmaxf(acc[i][j] + S.b1[tx + 16 * j], 0.f);
+}
+
+// Layer 2 logits for rows ty*4+i: partial dot products over this thread's
+// columns, reduced over the 16 threads of the row group (xor within 16 lanes).
+__device__ __forceinline__ void mlp_logits(const MlpSmem& S, const float h1[4][8], float lg[4][3]) {
+  const int tx = threadIdx.x & 15;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float s = 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) s = fmaf(S.w2[c * kW + tx + 16 * j], h1[i][j], s);
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      lg[i][c] = s + S.b2[c];
+    }
+}
+
+__global__ void __launch_bounds__(kMlpThreads, 1)
+    k_mlp_fwd_f32(MlpArgs a, const float* __restrict__ k0, const int32_t* __restrict__ ray,
+                  const float* __restrict__ hpe, const uint32_t* __restrict__ totals,
+                  float* rgb, int out_logits) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem_raw);
+  const int64_t M = totals[1];
+  const int64_t ntiles = (M + kTile - 1) / kTile;
+  if (blockIdx.x >= ntiles) return;
+  mlp_load_weights(S, a);
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t row0 = t * kTile;
+    float h1[4][8];
+    mlp_tile_forward(S, a, k0, ray, hpe, row0, M, h1);
+    float lg[4][3];
+    mlp_logits(S, h1, lg);
+    if (tx == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t m = row0 + ty * 4 + i;
+        if (m < M)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            rgb[m * 3 + c] = out_logits ? lg[i][c] : 1.f / (1.f + expf(-lg[i][c]));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+struct MlpBwdSmem {
+  MlpSmem f;
+  float dl[kTile * 4];       // d logits [row][c]
+  float dz1t[kW * kAS];      // d(layer-1 pre-activation), transposed [n][row]
+  float dz0t[kW * kAS];      // d(layer-0 pre-activation), transposed [n][row]
+  float pe[kTile * kMaxPe];  // PE rows of the tile
+};
+
+// Per-CTA partial gradient layout (same as the flat parameter layout).
+__global__ void __launch_bounds__(kMlpThreads, 1)
+    k_mlp_bwd_f32(MlpArgs a, const float* __restrict__ k0, const int32_t* __restrict__ ray,
+                  const float* __restrict__ hpe, const float* __restrict__ pe_buf,
+                  const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
+                  const float* __restrict__ grad_rgb, float* grad_k0, float* wpart) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MlpBwdSmem& B = *reinterpret_cast<MlpBwdSmem*>(smem_raw);
+  MlpSmem& S = B.f;
+  const int64_t M = totals[1];
+  const int64_t ntiles = (M + kTile - 1) / kTile;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t P = mlp_param_count(a.din);
+  float* part = wpart + int64_t(blockIdx.x) * P;
+  float* pw0 = part;
+  float* pb0 = pw0 + kW * a.din;
+  float* pw1 = pb0 + kW;
+  float* pb1 = pw1 + kW * kW;
+  float* pw2 = pb1 + kW;
+  float* pb2 = pw2 + 3 * kW;
+  // accumulators: dW1 block (n = ty+16i, k = tx+16j), dW0 row n = tid>>1 half q,
+  // db0/db1 for n = tid>>1 (even threads), dW2/db2 entries tid, tid+256
+  float aw1[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) aw1[i][j] = 0.f;
+  const int n0 = tid >> 1, qh = tid & 1;
+  const int qbeg = qh ? (a.din + 1) / 2 : 0, qend = qh ? a.din : (a.din + 1) / 2;
+  float aw0[24];
+#pragma unroll
+  for (int q = 0; q < 24; ++q) aw0[q] = 0.f;
+  float ab0 = 0.f, ab1 = 0.f;
+  float aw2[2] = {0.f, 0.f};
+  float ab2 = 0.f;
+  if (blockIdx.x < ntiles) {
+    mlp_load_weights(S, a);
+    __syncthreads();
+  }
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t row0 = t * kTile;
+    // PE rows
+    for (int i = tid; i < kTile * a.dpe; i += blockDim.x) {
+      const int rr = i / a.dpe, q = i % a.dpe;
+      const int64_t m = row0 + rr;
+      B.pe[rr * kMaxPe + q] = m < M ? pe_buf[int64_t(ray[m]) * kMaxPe + q] : 0.f;
+    }
+    float h1[4][8];
+    mlp_tile_forward(S, a, k0, ray, hpe, row0, M, h1);
+    // d logits: sigmoid backward
+    if (tid < kTile * 3) {
+      const int rr = tid / 3, c = tid % 3;
+      const int64_t m = row0 + rr;
+      float d = 0.f;
+      if (m < M) {
+        const float y = rgb[m * 3 + c];
+        d = grad_rgb[m * 3 + c] * (1.f - y) * y;
+      }
+      B.dl[rr * 4 + c] = d;
+    }
+    __syncthreads();
+    // dz1 = (dl . W2) * relu'(h1); also dW2 needs h1: write h1 into dz0t scratch
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rr = ty * 4 + i;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int n = tx + 16 * j;
+        float g = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) g = fmaf(B.dl[rr * 4 + c], S.w2[c * kW + n], g);
+        B.dz1t[n * kAS + rr] = h1[i][j] > 0.f ? g : 0.f;
+        B.dz0t[n * kAS + rr] = h1[i][j];
+      }
+    }
+    __syncthreads();
+    // dW2, db2 (entries e = c*128+n for c<3) and db2
+    for (int e = tid, s = 0; e < 3 * kW; e += blockDim.x, ++s) {
+      const int c = e / kW, n = e % kW;
+      float acc = 0.f;
+      for (int rr = 0; rr < kTile; ++rr) acc = fmaf(B.dl[rr * 4 + c], B.dz0t[n * kAS + rr], acc);
+      aw2[s] += acc;
+    }
+    if (tid < 3) {
+      float acc = 0.f;
+      for (int rr = 0; rr < kTile; ++rr) acc += B.dl[rr * 4 + tid];
+      ab2 += acc;
+    }
+    // dW1[n][k] += sum_row dz1[row][n] * h0[row][k]   (n = ty+16i, k = tx+16j)
+    for (int rr = 0; rr < kTile; ++rr) {
+      float av[8], bv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) av[i] = B.dz1t[(ty + 16 * i) * kAS + rr];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) bv[j] = S.h0t[(tx + 16 * j) * kAS + rr];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) aw1[i][j] = fmaf(av[i], bv[j], aw1[i][j]);
+    }
+    if (!qh) {
+      float acc = 0.f;
+      for (int rr = 0; rr < kTile; ++rr) acc += B.dz1t[n0 * kAS + rr];
+      ab1 += acc;
+    }
+    __syncthreads();  // dz0t scratch (h1) no longer needed
+    // dh0[row][k] = sum_n dz1[row][n] * W1[n][k]; dz0 = dh0 * relu'(h0)
+    {
+      float acc[4][8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+      for (int n = 0; n < kW; ++n) {
+        const float4 av = *reinterpret_cast<const float4*>(&B.dz1t[n * kAS + ty * 4]);
+        const float aa[4] = {av.x, av.y, av.z, av.w};
+        float bb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) bb[j] = S.w1[n * kW1S + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int k = tx + 16 * j, rr = ty * 4 + i;
+          B.dz0t[k * kAS + rr] = S.h0t[k * kAS + rr] > 0.f ? acc[i][j] : 0.f;
+        }
+    }
+    __syncthreads();
+    // dW0[n][q] += sum_row dz0[row][n] * x[row][q]  (x = [k0, pe]); db0
+    for (int rr = 0; rr < kTile; ++rr) {
+      const float g = B.dz0t[n0 * kAS + rr];
+#pragma unroll
+      for (int q = 0; q < 24; ++q) {
+        const int qq = qbeg + q;
+        if (qq < qend) {
+          const float xv = qq < a.c0 ? S.x[rr * kMaxC0 + qq] : B.pe[rr * kMaxPe + qq - a.c0];
+          aw0[q] = fmaf(g, xv, aw0[q]);
+        }
+      }
+      if (!qh) ab0 += g;
+    }
+    // grad_k0[row][q] = sum_n dz0[row][n] * W0[n][q]
+    for (int e = tid; e < kTile * a.c0; e += blockDim.x) {
+      const int rr = e / a.c0, q = e % a.c0;
+      const int64_t m = row0 + rr;
+      float acc = 0.f;
+      for (int n = 0; n < kW; ++n) acc = fmaf(B.dz0t[n * kAS + rr], S.w0k[n * (kMaxC0 + 1) + q], acc);
+      if (m < M) grad_k0[m * a.c0 + q] = acc;
+    }
+    __syncthreads();
+  }
+  // write this CTA's partials (zeros if it had no tile)
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) pw1[(ty + 16 * i) * kW + tx + 16 * j] = aw1[i][j];
+  for (int q = 0; q < 24; ++q)
+    if (qbeg + q < qend) pw0[n0 * a.din + qbeg + q] = aw0[q];
+  if (!qh) {
+    pb0[n0] = ab0;
+    pb1[n0] = ab1;
+  }
+  for (int e = tid, s = 0; e < 3 * kW; e += blockDim.x, ++s) pw2[e] = aw2[s];
+  if (tid < 3) pb2[tid] = ab2;
+}
+
+__global__ void k_wgrad_reduce(const float* __restrict__ wpart, int nparts, int64_t P, float* out) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= P) return;
+  float s = 0.f;
+  for (int c = 0; c < nparts; ++c) s += wpart[int64_t(c) * P + i];
+  out[i] = s;
+}
+
+__global__ void k_scatter_grads(const float* __restrict__ flat, int din, float* w0, float* b0,
+                                float* w1, float* b1, float* w2, float* b2) {
+  const int64_t P = mlp_param_count(din);
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= P) return;
+  int64_t o = i;
+  const int64_t s0 = int64_t(kW) * din, s1 = kW, s2 = int64_t(kW) * kW, s3 = kW, s4 = 3 * kW;
+  if (o < s0) { if (w0) w0[o] = flat[i]; return; }
+  o -= s0;
+  if (o < s1) { if (b0) b0[o] = flat[i]; return; }
+  o -= s1;
+  if (o < s2) { if (w1) w1[o] = flat[i]; return; }
+  o -= s2;
+  if (o < s3) { if (b1) b1[o] = flat[i]; return; }
+  o -= s3;
+  if (o < s4) { if (w2) w2[o] = flat[i]; return; }
+  o -= s4;
+  if (b2) b2[o] = flat[i];
+}
+
+// ------------------------------------------------------------------ host
+static int mlp_grid() { return num_sms(); }
+
+static int mlp_reserve(pvdb_march_s* m, int din) {
+  int rc = dev_reserve((void**)&m->hpe, &m->hpe_cap,
+                       size_t(m->max_rays) * (kW + kMaxPe) * 4);
+  if (rc) return rc;
+  const size_t P = size_t(mlp_param_count(din));
+  return dev_reserve((void**)&m->wpart, &m->wpart_cap, (size_t(mlp_grid()) + 1) * P * 4);
+}
+
+int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, float* rgb,
+                     cudaStream_t st) {
+  const int R = m->n_rays;
+  if (R <= 0) return PVDB_OK;
+  int rc = mlp_reserve(m, a.din);
+  if (rc) return rc;
+  float* hpe = m->hpe;
+  float* pe = m->hpe + size_t(m->max_rays) * kW;
+  k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  static bool attr = false;
+  if (!attr) {
+    PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(sizeof(MlpSmem))));
+    PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(sizeof(MlpBwdSmem))));
+    attr = true;
+  }
+  k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
+      a, m->w.r_k0, m->w.r_ray, hpe, m->w.totals, rgb, 0);
+  PVDB_CHECK_LAUNCH("k_mlp_fwd_f32");
+  return PVDB_OK;
+}
+
+// Rows from any producer (the merged renderer): k0rows [M, c0], ray [M] ->
+// viewdirs [R,3]; M = totals[1]. hpe_buf holds R*(128+32) floats.
+int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
+                     const float* viewdirs, int R, const uint32_t* totals, float* out,
+                     int out_logits, float* hpe_buf, cudaStream_t st) {
+  if (R <= 0) return PVDB_OK;
+  float* hpe = hpe_buf;
+  float* pe = hpe_buf + size_t(R) * kW;
+  k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(sizeof(MlpSmem))));
+  k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
+                                                                  out, out_logits);
+  PVDB_CHECK_LAUNCH("k_mlp_fwd_f32(rows)");
+  return PVDB_OK;
+}
+
+// hpe/pe of the current forward must still be in the workspace.
+int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* rgb, const float* grad_rgb,
+                      float* grad_k0, float* grad_flat, cudaStream_t st) {
+  const int R = m->n_rays;
+  const int64_t P = mlp_param_count(a.din);
+  if (R <= 0) {
+    PVDB_CHECK_CUDA(cudaMemsetAsync(grad_flat, 0, P * 4, st));
+    return PVDB_OK;
+  }
+  int rc = mlp_reserve(m, a.din);
+  if (rc) return rc;
+  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(sizeof(MlpBwdSmem))));
+  const int G = mlp_grid();
+  k_mlp_bwd_f32<<<G, kMlpThreads, sizeof(MlpBwdSmem), st>>>(
+      a, m->w.r_k0, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
+      grad_rgb, grad_k0, m->wpart);
+  PVDB_CHECK_LAUNCH("k_mlp_bwd_f32");
+  k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+  PVDB_CHECK_LAUNCH("k_wgrad_reduce");
+  return PVDB_OK;
+}
+
+int mlp_args_from(const pvdb_mlp_weights* w, MlpArgs& a) {
+  PVDB_REQUIRE(w && w->w0 && w->b0 && w->w1 && w->b1 && w->w2 && w->b2, "null MLP weight");
+  PVDB_REQUIRE(w->width == kW, "rgbnet width must be 128");
+  PVDB_REQUIRE(w->c0 > 0 && w->c0 <= kMaxC0, "k0 channels must be in 1..16");
+  PVDB_REQUIRE(w->pe >= 0 && w->pe <= 4, "viewbase_pe must be in 0..4");
+  a.w0 = w->w0; a.b0 = w->b0; a.w1 = w->w1; a.b1 = w->b1; a.w2 = w->w2; a.b2 = w->b2;
+  a.c0 = w->c0;
+  a.dpe = 3 + 6 * w->pe;
+  a.din = a.c0 + a.dpe;
+  return PVDB_OK;
+}
+
+}  // namespace pvdb
+
+using namespace pvdb;
+
+extern "C" {
+
+int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs, float* rgb,
+                     int32_t precision, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(m && viewdirs && rgb, "null argument");
+  PVDB_REQUIRE(m->has_fwd, "mlp before march forward");
+  PVDB_REQUIRE(m->k0 && m->k0->C == w->c0, "k0 channels differ from the march's k0 grid");
+  PVDB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 or 1");
+  MlpArgs a;
+  int rc = mlp_args_from(w, a);
+  if (rc) return rc;
+  (void)precision;  // the BF16 tensor-core path shares this entry (mlp_tc.cu)
+  return mlp_forward_impl(m, a, viewdirs, rgb, as_stream(s));
+}
+
+int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs,
+                      const float* rgb, const float* grad_rgb, pvdb_mlp_grads* g,
+                      float* grad_k0, int32_t precision, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(m && viewdirs && rgb && grad_rgb && g && grad_k0, "null argument");
+  PVDB_REQUIRE(m->has_fwd, "mlp before march forward");
+  PVDB_REQUIRE(m->k0 && m->k0->C == w->c0, "k0 channels differ from the march's k0 grid");
+  MlpArgs a;
+  int rc = mlp_args_from(w, a);
+  if (rc) return rc;
+  (void)precision;
+  cudaStream_t st = as_stream(s);
+  // hpe/pe depend only on the weights and viewdirs: recompute them so the
+  // backward does not rely on a preceding forward call of the same weights.
+  rc = mlp_reserve(m, a.din);
+  if (rc) return rc;
+  k_pe_hpe<<<ceil_div(int64_t(m->n_rays) * kW, 256), 256, 0, st>>>(
+      viewdirs, m->n_rays, (a.dpe - 3) / 6, a, m->hpe + size_t(m->max_rays) * kW, m->hpe);
+  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  const int64_t P = mlp_param_count(a.din);
+  float* flat = m->wpart + int64_t(mlp_grid()) * P;  // spare slot after the partials
+  rc = mlp_backward_impl(m, a, rgb, grad_rgb, grad_k0, flat, st);
+  if (rc) return rc;
+  k_scatter_grads<<<ceil_div(P, 256), 256, 0, st>>>(flat, a.din, g->w0, g->b0, g->w1, g->b1, g->w2,
+                                                     g->b2);
+  PVDB_CHECK_LAUNCH("k_scatter_grads");
+  return PVDB_OK;
+}
+
+}  // extern "C"

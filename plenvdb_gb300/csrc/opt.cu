@@ -1,0 +1,255 @@
+// Per-voxel Adam over the active voxels of a leaf store (DensityOpt/ColorOpt,
+// plenvdb.h:686-790; densityvdb.cu:185-349, colorvdb.cu:179-351) and the dense
+// Adam used for the rgbnet (lib/cuda/adam_upd_kernel.cu:8-132).
+#include <cmath>
+
+#include "pvdb_internal.cuh"
+
+struct pvdb_opt_s {
+  pvdb_grid_s* params = nullptr;  // borrowed (the caller keeps it alive, plenvdb.h:695)
+  pvdb_grid_s* exp_avg = nullptr;
+  pvdb_grid_s* exp_avg_sq = nullptr;
+  pvdb_grid_s* per_lr = nullptr;  // optional ScaleGrid with the params' topology
+  int step = 0;
+  float lr, eps, beta0, beta1;
+};
+
+namespace pvdb {
+
+// Bias-corrected step size, float arithmetic on the host exactly as
+// plenvdb.h:753 / :776 and adam_upd_kernel.cu:72.
+float adam_step_size(float lr, float beta_m, float beta_v, int step) {
+  return lr * std::sqrt(1 - std::pow(beta_v, (float)step)) / (1 - std::pow(beta_m, (float)step));
+}
+
+// One thread per (slot, group); a group is 1 channel for scalar grids and a
+// 3-channel Vec3 for multi-channel grids (the reference skips a Vec3 only when
+// all three gradient components are zero, colorvdb.cu:318).
+__global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ perlr, float stepsz, float eps, float b0,
+                           float b1, int mode, int zero_after,
+                           const uint8_t* __restrict__ touched) {
+  const int G = g.C == 1 ? 1 : 3;
+  const int ngroups = g.C / G;
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (t >= int64_t(g.nleaf) * kLeafVox * ngroups) return;
+  const int64_t slot = t / ngroups;
+  const int grp = int(t % ngroups);
+  const int leaf = int(slot >> 9), vox = int(slot & 511);
+  if (touched && !touched[leaf]) return;
+  if (!((__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull)) return;
+  const int64_t base = slot * g.C + int64_t(grp) * G;
+  float gr[3];
+  bool allzero = true;
+  for (int q = 0; q < G; ++q) {
+    gr[q] = g.grad[base + q];
+    allzero = allzero && (gr[q] == 0.f);
+  }
+  if (mode == 1 && allzero) return;
+  const float lrf = mode == 2 ? perlr[slot] : 1.f;
+  for (int q = 0; q < G; ++q) {
+    const float mn = b0 * m[base + q] + (1 - b0) * gr[q];
+    const float vn = b1 * v[base + q] + (1 - b1) * gr[q] * gr[q];
+    m[base + q] = mn;
+    v[base + q] = vn;
+    const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
+    g.data[base + q] = g.data[base + q] - num / (eps + sqrtf(vn));
+    if (zero_after) g.grad[base + q] = 0.f;
+  }
+}
+
+// zero_after for voxels the Adam pass skipped (mode 1, all-zero gradient):
+// nothing to do, their gradient is already zero.
+
+__global__ void k_clear_u8(uint8_t* t, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) t[i] = 0;
+}
+
+template <int MODE>
+__global__ void k_adam_dense(float* __restrict__ p, const float* __restrict__ g,
+                             float* __restrict__ m, float* __restrict__ v,
+                             const float* __restrict__ perlr, int64_t n, float stepsz, float b1,
+                             float b2, float eps) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  if (MODE == 1 && gi == 0.f) return;
+  const float mn = b1 * m[i] + (1 - b1) * gi;
+  const float vn = b2 * v[i] + (1 - b2) * gi * gi;
+  m[i] = mn;
+  v[i] = vn;
+  if (MODE == 2)
+    p[i] -= stepsz * perlr[i] * mn / (sqrtf(vn) + eps);
+  else
+    p[i] -= stepsz * mn / (sqrtf(vn) + eps);
+}
+
+int adam_dense_launch(float* param, const float* grad, float* m, float* v, const float* perlr,
+                      int64_t n, float stepsz, float b1, float b2, float eps, int mode,
+                      cudaStream_t st) {
+  if (n <= 0) return PVDB_OK;
+  const int nb = ceil_div(n, 256);
+  if (mode == 1)
+    k_adam_dense<1><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+  else if (mode == 2)
+    k_adam_dense<2><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+  else
+    k_adam_dense<0><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+  PVDB_CHECK_LAUNCH("k_adam_dense");
+  return PVDB_OK;
+}
+
+// Runs one voxel-Adam step (used by the C ABI and the fused train step).
+int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st) {
+  pvdb_grid_s* g = o->params;
+  o->step++;
+  const float stepsz = adam_step_size(o->lr, o->beta0, o->beta1, o->step);
+  const int G = g->C == 1 ? 1 : 3;
+  const int64_t nt = g->nslots() * (g->C / G);
+  const uint8_t* touched = (mode == 1 && !g->all_touched) ? g->d_touched : nullptr;
+  if (nt) {
+    k_vdb_adam<<<ceil_div(nt, 256), 256, 0, st>>>(
+        g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
+        mode == 2 ? o->per_lr->d_data : nullptr, stepsz, o->eps, o->beta0, o->beta1, mode,
+        zero_after, touched);
+    PVDB_CHECK_LAUNCH("k_vdb_adam");
+  }
+  if (zero_after && g->nleaf) {
+    k_clear_u8<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf);
+    PVDB_CHECK_LAUNCH("k_clear_u8");
+    g->all_touched = false;
+  }
+  return PVDB_OK;
+}
+
+pvdb_grid_s* opt_params(pvdb_opt_s* o) { return o->params; }
+float opt_lr_scale(pvdb_opt_s* o, float factor) {
+  o->lr *= factor;
+  return o->lr;
+}
+
+}  // namespace pvdb
+
+using namespace pvdb;
+
+extern "C" {
+
+int pvdb_opt_create(pvdb_grid g, float lr, float eps, float beta0, float beta1, pvdb_opt* out) {
+  clear_error();
+  PVDB_REQUIRE(g && out, "null argument");
+  pvdb_opt_s* o = new pvdb_opt_s();
+  o->params = g;
+  o->lr = lr;
+  o->eps = eps;
+  o->beta0 = beta0;
+  o->beta1 = beta1;
+  int rc = pvdb_grid_create_like(g, g->C, 0.f, &o->exp_avg);
+  if (!rc) rc = pvdb_grid_create_like(g, g->C, 0.f, &o->exp_avg_sq);
+  if (rc) {
+    pvdb_opt_destroy(o);
+    return rc;
+  }
+  *out = o;
+  return PVDB_OK;
+}
+
+int pvdb_opt_destroy(pvdb_opt o) {
+  if (!o) return PVDB_OK;
+  pvdb_grid_destroy(o->exp_avg);
+  pvdb_grid_destroy(o->exp_avg_sq);
+  pvdb_grid_destroy(o->per_lr);
+  delete o;
+  return PVDB_OK;
+}
+
+int pvdb_opt_step(pvdb_opt o, int32_t mode, int32_t zero_grad_after, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  PVDB_REQUIRE(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2");
+  if (mode == 2 && !o->per_lr)
+    return set_error(PVDB_ERR_STATE, "step(2) needs set_pervoxel_lr first");
+  return opt_step_launch(o, mode, zero_grad_after, as_stream(s));
+}
+
+int pvdb_opt_zero_grad(pvdb_opt o, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  return pvdb_grid_zero_grad(o->params, s);
+}
+
+int pvdb_opt_set_grad(pvdb_opt o, const float* arr, int64_t n, int32_t mem, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  return pvdb_grid_copy_from_dense(o->params, PVDB_WHICH_GRAD, arr, n, mem, s);
+}
+
+int pvdb_opt_set_pervoxel_lr(pvdb_opt o, const float* count, int64_t n, int32_t mem,
+                             pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(o && count, "null argument");
+  pvdb_grid_s* g = o->params;
+  PVDB_REQUIRE(n == int64_t(g->reso[0]) * g->reso[1] * g->reso[2],
+               "per-voxel lr size must be reso[0]*reso[1]*reso[2]");
+  if (!o->per_lr) {
+    int rc = pvdb_grid_create_like(g, 1, 0.f, &o->per_lr);
+    if (rc) return rc;
+  }
+  return pvdb_grid_copy_from_dense(o->per_lr, PVDB_WHICH_DATA, count, n, mem, s);
+}
+
+int pvdb_opt_update_lr(pvdb_opt o, float factor) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  o->lr *= factor;
+  return PVDB_OK;
+}
+
+int pvdb_opt_get_scalars(pvdb_opt o, int32_t* step, float* lr, float* eps, float* beta0,
+                         float* beta1) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  if (step) *step = o->step;
+  if (lr) *lr = o->lr;
+  if (eps) *eps = o->eps;
+  if (beta0) *beta0 = o->beta0;
+  if (beta1) *beta1 = o->beta1;
+  return PVDB_OK;
+}
+
+int pvdb_opt_set_scalars(pvdb_opt o, int32_t step, float lr, float eps, float beta0,
+                         float beta1) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  o->step = step;
+  o->lr = lr;
+  o->eps = eps;
+  o->beta0 = beta0;
+  o->beta1 = beta1;
+  return PVDB_OK;
+}
+
+int pvdb_opt_moments(pvdb_opt o, pvdb_grid* exp_avg, pvdb_grid* exp_avg_sq) {
+  clear_error();
+  PVDB_REQUIRE(o, "null optimiser");
+  if (exp_avg) *exp_avg = o->exp_avg;
+  if (exp_avg_sq) *exp_avg_sq = o->exp_avg_sq;
+  return PVDB_OK;
+}
+
+int pvdb_adam_dense(float* param, const float* grad, float* exp_avg, float* exp_avg_sq,
+                    const float* perlr, int64_t n, int32_t step, float beta1, float beta2,
+                    float lr, float eps, int32_t mode, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(n >= 0, "negative size");
+  if (n == 0) return PVDB_OK;
+  PVDB_REQUIRE(param && grad && exp_avg && exp_avg_sq, "null argument");
+  PVDB_REQUIRE(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2");
+  PVDB_REQUIRE(mode != 2 || perlr, "mode 2 needs perlr");
+  PVDB_REQUIRE(step >= 1, "step must be >= 1");
+  const float stepsz = adam_step_size(lr, beta1, beta2, step);
+  return adam_dense_launch(param, grad, exp_avg, exp_avg_sq, perlr, n, stepsz, beta1, beta2, eps,
+                           mode, as_stream(s));
+}
+
+}  // extern "C"

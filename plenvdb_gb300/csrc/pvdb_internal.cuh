@@ -1,0 +1,256 @@
+// Internal declarations shared by the libpvdb translation units.
+//
+// Leaf store layout (device, HBM):
+//   table  int32 [ldim0*ldim1*ldim2]   leaf id of each 8^3 block of [0, 8*ldim), -1 = none
+//   origin int32 [nleaf*3]             voxel coordinate of each leaf's (0,0,0) corner
+//   mask   uint64[nleaf*8]             active bits, bit n of the leaf = voxel offset n
+//   data   f32   [nleaf*512*C]         values, voxel-major with the C channels innermost
+//   grad   f32   [nleaf*512*C]         gradient, same layout
+// A voxel's offset inside its leaf is ((x&7)<<6)|((y&7)<<3)|(z&7), the NanoVDB
+// LeafNode::CoordToOffset order (nanovdb/NanoVDB.h:3893-3899), and its "slot" is
+// leaf*512 + offset. Leaves are numbered in Morton order of their leaf
+// coordinates so that leaves adjacent along a ray sit close together.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pvdb.h"
+
+namespace pvdb {
+
+constexpr int kLeafVox = 512;
+
+// ------------------------------------------------------------- errors (host)
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* what);
+void clear_error();
+
+#define PVDB_CHECK_CUDA(call)                                  \
+  do {                                                          \
+    cudaError_t _e = (call);                                    \
+    if (_e != cudaSuccess) return ::pvdb::cuda_error(_e, #call); \
+  } while (0)
+
+// Every kernel launch is followed by exactly one PVDB_CHECK_LAUNCH (or
+// PVDB_CHECK_LAUNCHES(n) after n launches); it also counts the launches.
+void count_launches(int n);
+#define PVDB_CHECK_LAUNCHES(what, n)                                \
+  do {                                                               \
+    ::pvdb::count_launches(n);                                       \
+    cudaError_t _e = cudaGetLastError();                             \
+    if (_e != cudaSuccess) return ::pvdb::cuda_error(_e, what);      \
+  } while (0)
+#define PVDB_CHECK_LAUNCH(what) PVDB_CHECK_LAUNCHES(what, 1)
+
+#define PVDB_REQUIRE(cond, msg)                                         \
+  do {                                                                   \
+    if (!(cond)) return ::pvdb::set_error(PVDB_ERR_ARG, msg);            \
+  } while (0)
+
+// Device allocation through the library (honours the failure-injection hook).
+int dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+// Grows *p to at least `bytes` (contents not preserved).
+int dev_reserve(void** p, size_t* cap, size_t bytes);
+
+inline cudaStream_t as_stream(pvdb_stream s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int ceil_div(int64_t a, int64_t b) { return int((a + b - 1) / b); }
+
+// ------------------------------------------------------------ device view
+struct GridView {
+  int reso[3];
+  int ldim[3];
+  int C;
+  int nleaf;
+  float background;
+  const int32_t* __restrict__ table;
+  const int32_t* __restrict__ origin;
+  const uint64_t* __restrict__ mask;
+  float* data;
+  float* grad;
+};
+
+// Scratch of the deterministic gradient reduction (one per grid topology).
+struct ReduceScratch {
+  uint32_t* keys[2] = {nullptr, nullptr};
+  uint32_t* vals[2] = {nullptr, nullptr};
+  size_t cap = 0;              // elements per buffer
+  uint32_t* hist = nullptr;    // radix histograms
+  size_t hist_cap = 0;
+  uint32_t* partial = nullptr; // scan partials
+  size_t partial_cap = 0;
+};
+
+}  // namespace pvdb
+
+// Opaque handles (declared in the global namespace to match pvdb.h).
+struct pvdb_grid_s {
+  int reso[3];
+  int ldim[3];
+  int C;
+  int nleaf;
+  float background;
+  int64_t nactive;
+  int32_t* d_table = nullptr;
+  int32_t* d_origin = nullptr;
+  uint64_t* d_mask = nullptr;
+  float* d_data = nullptr;
+  float* d_grad = nullptr;
+  uint8_t* d_touched = nullptr;  // [nleaf] leaves whose gradient may be nonzero
+  bool all_touched = true;       // every leaf must be treated as touched
+  std::vector<int32_t> h_table;
+  std::vector<int32_t> h_origin;
+  std::vector<uint64_t> h_mask;
+  pvdb::ReduceScratch red;
+  // host staging for PVDB_MEM_HOST calls
+  void* d_stage = nullptr;
+  size_t stage_cap = 0;
+
+  pvdb::GridView view() const {
+    pvdb::GridView v;
+    for (int a = 0; a < 3; ++a) { v.reso[a] = reso[a]; v.ldim[a] = ldim[a]; }
+    v.C = C; v.nleaf = nleaf; v.background = background;
+    v.table = d_table; v.origin = d_origin; v.mask = d_mask; v.data = d_data; v.grad = d_grad;
+    return v;
+  }
+  int64_t nslots() const { return int64_t(nleaf) * pvdb::kLeafVox; }
+};
+
+namespace pvdb {
+
+// ------------------------------------------------------- device helpers
+__device__ __forceinline__ int leaf_of(const GridView& g, int i, int j, int k) {
+  if ((unsigned)i >= (unsigned)(g.ldim[0] << 3) || (unsigned)j >= (unsigned)(g.ldim[1] << 3) ||
+      (unsigned)k >= (unsigned)(g.ldim[2] << 3))
+    return -1;
+  return __ldg(g.table + ((i >> 3) * g.ldim[1] + (j >> 3)) * g.ldim[2] + (k >> 3));
+}
+
+__device__ __forceinline__ int vox_offset(int i, int j, int k) {
+  return ((i & 7) << 6) | ((j & 7) << 3) | (k & 7);
+}
+
+// Slot (leaf*512 + offset) of a voxel, or -1 when it lies in no allocated leaf.
+__device__ __forceinline__ int slot_of(const GridView& g, int i, int j, int k) {
+  int l = leaf_of(g, i, j, k);
+  return l < 0 ? -1 : (l << 9) | vox_offset(i, j, k);
+}
+
+// Scalar (C == 1) value at a voxel.
+__device__ __forceinline__ float value1(const GridView& g, int i, int j, int k) {
+  int s = slot_of(g, i, j, k);
+  return s < 0 ? g.background : __ldg(g.data + s);
+}
+
+// The 8 trilinear corners in the reference's visiting order
+// (densityvdb.cu:116-123): 000,001,011,010,110,111,101,100.
+__device__ __forceinline__ void corner_delta(int c, int& di, int& dj, int& dk) {
+  switch (c) {
+    case 0: di = 0; dj = 0; dk = 0; break;
+    case 1: di = 0; dj = 0; dk = 1; break;
+    case 2: di = 0; dj = 1; dk = 1; break;
+    case 3: di = 0; dj = 1; dk = 0; break;
+    case 4: di = 1; dj = 1; dk = 0; break;
+    case 5: di = 1; dj = 1; dk = 1; break;
+    case 6: di = 1; dj = 0; dk = 1; break;
+    default: di = 1; dj = 0; dk = 0; break;
+  }
+}
+
+// Floor to int as nanovdb::Vec3::floor (Floor(x) = int32(floorf(x))).
+__device__ __forceinline__ int ifloor(float x) { return int(floorf(x)); }
+
+// Density trilinear with the reference's association: for each corner in order,
+// res += ((v*(1-u))*(1-v))*(1-w) (densityvdb.cu:115-123).
+__device__ __forceinline__ float trilinear1(const GridView& g, float x, float y, float z) {
+  const int i = ifloor(x), j = ifloor(y), k = ifloor(z);
+  const float u = x - float(i), v = y - float(j), w = z - float(k);
+  const float iu = 1.f - u, iv = 1.f - v, iw = 1.f - w;
+  float r = 0.f;
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j, k), iu), iv), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j, k + 1), iu), iv), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j + 1, k + 1), iu), v), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j + 1, k), iu), v), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j + 1, k), u), v), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j + 1, k + 1), u), v), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j, k + 1), u), iv), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j, k), u), iv), iw));
+  return r;
+}
+
+// Trilinear corner weights for the multi-channel formula (colorvdb.cu:100-107):
+// scale_c = ((a*b)*c) of the three 1-u / u factors, computed before the multiply.
+__device__ __forceinline__ void corner_scales(float u, float v, float w, float s[8]) {
+  const float iu = 1.f - u, iv = 1.f - v, iw = 1.f - w;
+  s[0] = __fmul_rn(__fmul_rn(iu, iv), iw);
+  s[1] = __fmul_rn(__fmul_rn(iu, iv), w);
+  s[2] = __fmul_rn(__fmul_rn(iu, v), w);
+  s[3] = __fmul_rn(__fmul_rn(iu, v), iw);
+  s[4] = __fmul_rn(__fmul_rn(u, v), iw);
+  s[5] = __fmul_rn(__fmul_rn(u, v), w);
+  s[6] = __fmul_rn(__fmul_rn(u, iv), w);
+  s[7] = __fmul_rn(__fmul_rn(u, iv), iw);
+}
+
+// Density-style corner weight of corner c for a gradient g:
+// ((g*(1-u))*(1-v))*(1-w) pattern (densityvdb.cu:158-165).
+__device__ __forceinline__ float density_corner_term(float g, float u, float v, float w, int c) {
+  int di, dj, dk;
+  corner_delta(c, di, dj, dk);
+  const float a = di ? u : 1.f - u, b = dj ? v : 1.f - v, cc = dk ? w : 1.f - w;
+  return __fmul_rn(__fmul_rn(__fmul_rn(g, a), b), cc);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ------------------------------------------------- shared host routines
+// Device-wide exclusive scan of uint32 (n elements) into out; total (device
+// scalar, may be NULL) receives the sum. Uses the grid's reduce scratch.
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total,
+                       uint32_t** partial, size_t* partial_cap, cudaStream_t st);
+// Same with the element count on the device (n_dev, clamped to n_max); the
+// launch is sized from n_max, the work from *n_dev.
+int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
+                           const uint32_t* n_dev, uint32_t* total, uint32_t** partial,
+                           size_t* partial_cap, cudaStream_t st);
+
+// Stable LSD radix sort of (key,val) pairs, low `key_bits` bits of the keys,
+// input in rs.keys[0] (and rs.vals[0] unless iota_vals, in which case the
+// payload is the input index). Result ends in rs.keys[*out_buf], rs.vals[*out_buf].
+int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,
+                     cudaStream_t st);
+int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
+                         bool iota_vals, int* out_buf, cudaStream_t st);
+
+int scratch_reserve(ReduceScratch& rs, int64_t n);
+void free_scratch(ReduceScratch& rs);
+int num_sms();
+
+// Ensure the reduce scratch of g can hold n contributions.
+int reduce_reserve(pvdb_grid_s* g, int64_t n);
+
+// Stage profiler (prof.cu): mark i records an event after stage i of a call.
+constexpr int kProfMarks = 16;
+void prof_begin_call();
+void prof_mark(cudaStream_t st, int id);
+
+// Launch helpers shared by the train step.
+float adam_step_size(float lr, float beta_m, float beta_v, int step);
+int adam_dense_launch(float* param, const float* grad, float* m, float* v, const float* perlr,
+                      int64_t n, float stepsz, float b1, float b2, float eps, int mode,
+                      cudaStream_t st);
+
+// Number of key bits needed so that all slots and the invalid key sort apart.
+int slot_key_bits(int64_t nslots);
+
+}  // namespace pvdb

@@ -1,0 +1,377 @@
+// Device-wide scan, stable LSD radix sort and the generic point backward
+// (DensityVDB/ColorVDB backward, plenvdb.h:468-485, :557-573).
+//
+// Sizes may live on the device (n_dev != NULL): kernels are launched for the
+// host-side maximum with a fixed, SM-count-sized grid and loop over the tiles
+// that the device-side count actually needs, so the fused training step never
+// synchronises with the host.
+#include <algorithm>
+
+#include "reduce.cuh"
+
+namespace pvdb {
+
+static int g_num_sms = 0;
+int num_sms() {
+  if (!g_num_sms) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    g_num_sms = n > 0 ? n : 148;
+  }
+  return g_num_sms;
+}
+
+__device__ __forceinline__ int64_t eff_size(int64_t n_max, const uint32_t* n_dev) {
+  return n_dev ? min(n_max, (int64_t)*n_dev) : n_max;
+}
+
+// ------------------------------------------------------------------- scan
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t s = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) warp_sums[lane] = s;  // inclusive
+  }
+  __syncthreads();
+  const uint32_t warp_excl = wid ? warp_sums[wid - 1] : 0u;
+  if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
+  const uint32_t r = warp_excl + x - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n_max,
+                              const uint32_t* n_dev, uint32_t* partial) {
+  const int64_t n = eff_size(n_max, n_dev);
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t base = t * kScanTile + int64_t(threadIdx.x) * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q)
+      if (base + q < n) s += in[base + q];
+    uint32_t tot;
+    block_exclusive_scan(s, &tot);
+    if (threadIdx.x == 0) partial[t] = tot;
+  }
+}
+
+__global__ void k_scan_partials(uint32_t* partial, int64_t n_max, const uint32_t* n_dev,
+                                uint32_t* total) {
+  __shared__ uint32_t carry_s;
+  const int64_t n = eff_size(n_max, n_dev);
+  const int64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nb; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const uint32_t v = i < nb ? partial[i] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, &tot);
+    const uint32_t c = carry_s;
+    if (i < nb) partial[i] = c + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s = c + tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total) *total = carry_s;
+}
+
+__global__ void k_scan_apply(const uint32_t* __restrict__ in, uint32_t* out, int64_t n_max,
+                             const uint32_t* n_dev, const uint32_t* __restrict__ partial) {
+  const int64_t n = eff_size(n_max, n_dev);
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t base = t * kScanTile + int64_t(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+      v[q] = base + q < n ? in[base + q] : 0u;
+      s += v[q];
+    }
+    uint32_t run = block_exclusive_scan(s, nullptr) + partial[t];
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+      if (base + q < n) out[base + q] = run;
+      run += v[q];
+    }
+  }
+}
+
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total,
+                       uint32_t** partial, size_t* partial_cap, cudaStream_t st) {
+  return scan_exclusive_u32_dev(in, out, n, nullptr, total, partial, partial_cap, st);
+}
+
+int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
+                           const uint32_t* n_dev, uint32_t* total, uint32_t** partial,
+                           size_t* partial_cap, cudaStream_t st) {
+  if (n_max <= 0) {
+    if (total) PVDB_CHECK_CUDA(cudaMemsetAsync(total, 0, 4, st));
+    return PVDB_OK;
+  }
+  const int64_t nb = (n_max + kScanTile - 1) / kScanTile;
+  int rc = dev_reserve((void**)partial, partial_cap, size_t(nb) * 4);
+  if (rc) return rc;
+  const int grid = int(std::min<int64_t>(nb, int64_t(num_sms()) * 8));
+  k_scan_reduce<<<grid, kScanThreads, 0, st>>>(in, n_max, n_dev, *partial);
+  k_scan_partials<<<1, 1024, 0, st>>>(*partial, n_max, n_dev, total);
+  k_scan_apply<<<grid, kScanThreads, 0, st>>>(in, out, n_max, n_dev, *partial);
+  PVDB_CHECK_LAUNCHES("scan", 3);
+  return PVDB_OK;
+}
+
+// ------------------------------------------------------------- radix sort
+constexpr int kRsThreads = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsRounds = 16;                    // keys per lane
+constexpr int kRsTile = kRsThreads * kRsRounds;  // 4096 keys per tile
+constexpr int kRsBins = 256;
+
+// sizes[0] = n (contributions), sizes[1] = 256 * tiles (histogram length)
+__global__ void k_rs_sizes(int64_t n_max, const uint32_t* n_dev, uint32_t* sizes) {
+  const int64_t n = eff_size(n_max, n_dev);
+  sizes[0] = uint32_t(n);
+  sizes[1] = uint32_t(((n + kRsTile - 1) / kRsTile) * kRsBins);
+}
+
+__global__ void k_rs_upsweep(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ sizes,
+                             int shift, uint32_t* hist) {
+  __shared__ uint32_t h[kRsBins];
+  const int64_t n = sizes[0];
+  const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = t * kRsTile;
+    for (int q = threadIdx.x; q < kRsTile; q += kRsThreads) {
+      const int64_t i = base + q;
+      if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[int64_t(threadIdx.x) * ntiles + t] = h[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+// Stable scatter: within a tile the order is (warp, round, lane) = index order.
+__global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                               const uint32_t* __restrict__ sizes, int shift,
+                               const uint32_t* __restrict__ offsets, uint32_t* kout,
+                               uint32_t* vout) {
+  __shared__ uint32_t wh[kRsWarps][kRsBins];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t n = sizes[0];
+  const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
+  const unsigned lt = lanemask_lt();
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (int q = threadIdx.x; q < kRsWarps * kRsBins; q += kRsThreads) (&wh[0][0])[q] = 0;
+    __syncthreads();
+    const int64_t wbase = t * kRsTile + int64_t(w) * (kRsRounds * 32);
+    uint32_t key[kRsRounds];
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+      const int64_t i = wbase + r * 32 + lane;
+      key[r] = i < n ? kin[i] : 0u;
+    }
+    // phase 1: per-warp digit histogram
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+      const bool valid = wbase + r * 32 + lane < n;
+      const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (valid && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // phase 2: per digit, exclusive offsets across warps plus the tile's global base
+    {
+      const int d = threadIdx.x;  // kRsThreads == kRsBins
+      uint32_t run = offsets[int64_t(d) * ntiles + t];
+      for (int q = 0; q < kRsWarps; ++q) {
+        const uint32_t c = wh[q][d];
+        wh[q][d] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    // phase 3: stable ranks and scatter
+#pragma unroll
+    for (int r = 0; r < kRsRounds; ++r) {
+      const int64_t i = wbase + r * 32 + lane;
+      const bool valid = i < n;
+      const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      uint32_t pos = 0;
+      if (valid) pos = wh[w][d] + __popc(peers & lt);
+      __syncwarp();
+      if (valid && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+      __syncwarp();
+      if (valid) {
+        kout[pos] = key[r];
+        vout[pos] = vin ? vin[i] : uint32_t(i);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int slot_key_bits(int64_t nslots) {
+  int b = 1;
+  while ((int64_t(1) << b) <= nslots) ++b;
+  return b;
+}
+
+int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
+                         bool iota_vals, int* out_buf, cudaStream_t st) {
+  *out_buf = 0;
+  if (n_max <= 0) return PVDB_OK;
+  const int64_t ntiles_max = (n_max + kRsTile - 1) / kRsTile;
+  int rc = dev_reserve((void**)&rs.hist, &rs.hist_cap, size_t(ntiles_max) * kRsBins * 4 + 64);
+  if (rc) return rc;
+  uint32_t* sizes = rs.hist + ntiles_max * kRsBins;  // 2 scalars after the histogram
+  k_rs_sizes<<<1, 1, 0, st>>>(n_max, n_dev, sizes);
+  PVDB_CHECK_LAUNCH("k_rs_sizes");
+  const int grid = int(std::min<int64_t>(ntiles_max, int64_t(num_sms()) * 4));
+  int cur = 0;
+  bool first = true;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    k_rs_upsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur], sizes, shift, rs.hist);
+    PVDB_CHECK_LAUNCH("k_rs_upsweep");
+    rc = scan_exclusive_u32_dev(rs.hist, rs.hist, ntiles_max * kRsBins, sizes + 1, nullptr,
+                                &rs.partial, &rs.partial_cap, st);
+    if (rc) return rc;
+    k_rs_downsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
+                                                (first && iota_vals) ? nullptr : rs.vals[cur],
+                                                sizes, shift, rs.hist, rs.keys[cur ^ 1],
+                                                rs.vals[cur ^ 1]);
+    PVDB_CHECK_LAUNCH("k_rs_downsweep");
+    first = false;
+    cur ^= 1;
+  }
+  *out_buf = cur;
+  return PVDB_OK;
+}
+
+int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,
+                     cudaStream_t st) {
+  return radix_sort_pairs_dev(rs, n, nullptr, key_bits, iota_vals, out_buf, st);
+}
+
+int scratch_reserve(ReduceScratch& rs, int64_t n) {
+  if (rs.cap >= size_t(n) && rs.keys[0]) return PVDB_OK;
+  for (int b = 0; b < 2; ++b) {
+    dev_free(rs.keys[b]);
+    dev_free(rs.vals[b]);
+    rs.keys[b] = rs.vals[b] = nullptr;
+  }
+  rs.cap = 0;
+  const size_t want = std::max<size_t>(size_t(n), 4096);
+  int rc;
+  for (int b = 0; b < 2; ++b) {
+    if ((rc = dev_alloc((void**)&rs.keys[b], want * 4))) return rc;
+    if ((rc = dev_alloc((void**)&rs.vals[b], want * 4))) return rc;
+  }
+  rs.cap = want;
+  return PVDB_OK;
+}
+
+int reduce_reserve(pvdb_grid_s* g, int64_t n) { return scratch_reserve(g->red, n); }
+
+void free_scratch(ReduceScratch& rs) {
+  for (int b = 0; b < 2; ++b) {
+    dev_free(rs.keys[b]);
+    dev_free(rs.vals[b]);
+    rs.keys[b] = rs.vals[b] = nullptr;
+  }
+  dev_free(rs.hist);
+  dev_free(rs.partial);
+  rs.hist = rs.partial = nullptr;
+  rs.cap = rs.hist_cap = rs.partial_cap = 0;
+}
+
+// ------------------------------------------------- generic point backward
+struct PointSrc {
+  const float* xs;
+  const float* ys;
+  const float* zs;
+  const float* g;
+  int C;
+  __device__ __forceinline__ void pos(int64_t s, float& x, float& y, float& z) const {
+    x = xs[s]; y = ys[s]; z = zs[s];
+  }
+  __device__ __forceinline__ float gd(int64_t s) const { return g[s]; }
+  __device__ __forceinline__ bool has_c(int64_t) const { return true; }
+  __device__ __forceinline__ float gc(int64_t s, int ch) const { return g[s * C + ch]; }
+};
+
+__global__ void k_point_keys(GridView gv, const float* __restrict__ xs, const float* __restrict__ ys,
+                             const float* __restrict__ zs, int64_t n, uint32_t* keys) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= n) return;
+  emit_corner_keys(gv, xs[p], ys[p], zs[p], keys, p);
+}
+
+}  // namespace pvdb
+
+using namespace pvdb;
+
+extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys,
+                                         const float* zs, const float* grad_out, int64_t n,
+                                         int32_t mem, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(g, "null grid");
+  PVDB_REQUIRE(n >= 0, "negative size");
+  if (n == 0) return PVDB_OK;
+  PVDB_REQUIRE(xs && ys && zs && grad_out, "null argument");
+  PVDB_REQUIRE(n * 8 < int64_t(0xFFFFFFF0u), "too many points for one backward call");
+  cudaStream_t st = as_stream(s);
+  const float *dx = xs, *dy = ys, *dz = zs, *dg = grad_out;
+  if (mem == PVDB_MEM_HOST) {
+    int rc = dev_reserve(&g->d_stage, &g->stage_cap, size_t(n) * 4 * (3 + g->C));
+    if (rc) return rc;
+    float* b = (float*)g->d_stage;
+    PVDB_CHECK_CUDA(cudaMemcpyAsync(b, xs, n * 4, cudaMemcpyHostToDevice, st));
+    PVDB_CHECK_CUDA(cudaMemcpyAsync(b + n, ys, n * 4, cudaMemcpyHostToDevice, st));
+    PVDB_CHECK_CUDA(cudaMemcpyAsync(b + 2 * n, zs, n * 4, cudaMemcpyHostToDevice, st));
+    PVDB_CHECK_CUDA(cudaMemcpyAsync(b + 3 * n, grad_out, n * 4 * g->C, cudaMemcpyHostToDevice, st));
+    dx = b; dy = b + n; dz = b + 2 * n; dg = b + 3 * n;
+  }
+  const int64_t nc = n * 8;
+  int rc = reduce_reserve(g, nc);
+  if (rc) return rc;
+  k_point_keys<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), dx, dy, dz, n, g->red.keys[0]);
+  PVDB_CHECK_LAUNCH("k_point_keys");
+  int buf = 0;
+  rc = radix_sort_pairs(g->red, nc, slot_key_bits(g->nslots()), true, &buf, st);
+  if (rc) return rc;
+  PointSrc src{dx, dy, dz, dg, g->C};
+  const int grid = int(std::min<int64_t>(ceil_div(nc, 256), int64_t(num_sms()) * 16));
+  k_segment_reduce<PointSrc><<<grid, 256, 0, st>>>(
+      g->red.keys[buf], g->red.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
+      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched);
+  PVDB_CHECK_LAUNCH("k_segment_reduce");
+  if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  return PVDB_OK;
+}

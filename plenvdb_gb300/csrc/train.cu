@@ -1,0 +1,212 @@
+// One fine-stage training iteration on device-resident rays (run.py:516-598):
+// march forward, rgbnet, composite, the reference losses (run.py:551-575),
+// the full backward, TV on both grids (run.py:578-584), voxel Adam (mode 1,
+// configs/default.py:76) on both grids, dense Adam on the rgbnet
+// (masked_adam.py:128-158, mode 0) and the lr decay (run.py:592-598).
+// Nothing synchronises with the host.
+#include <cmath>
+
+#include "march.cuh"
+
+struct pvdb_opt_s;
+
+namespace pvdb {
+
+struct MlpArgs {
+  const float* w0; const float* b0;
+  const float* w1; const float* b1;
+  const float* w2; const float* b2;
+  int c0, dpe, din;
+};
+int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, float* rgb,
+                     cudaStream_t st);
+int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* rgb, const float* grad_rgb,
+                      float* grad_k0, float* grad_flat, cudaStream_t st);
+int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
+                       const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
+                       const int32_t* mshape, cudaStream_t st);
+int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_last,
+                        const float* grad_k0, cudaStream_t st);
+int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
+                           cudaStream_t st);
+int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st);
+pvdb_grid_s* opt_params(pvdb_opt_s* o);
+float opt_lr_scale(pvdb_opt_s* o, float factor);
+
+struct LossW {
+  float main, ent, rgbper, bg;
+};
+
+// Per ray: losses and their gradients w.r.t. rgb_marched (folded into the
+// per-row colour gradient), alphainv_last, and the colour weights.
+__global__ void __launch_bounds__(256)
+    k_loss(MarchW W, const float* __restrict__ rgb, const float* __restrict__ rgbm,
+           const float* __restrict__ target, int R, LossW L, float* grad_rgb, float* grad_w,
+           float* grad_last, float* loss_part) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * 8 + warp;
+  if (r >= R) return;
+  const float t0 = target[r * 3], t1 = target[r * 3 + 1], t2 = target[r * 3 + 2];
+  const float e0 = rgbm[r * 3] - t0, e1 = rgbm[r * 3 + 1] - t1, e2 = rgbm[r * 3 + 2] - t2;
+  // d/d rgb_marched of weight_main * mean((rgbm-target)^2) over R*3 entries
+  const float cm = L.main * 2.f / (3.f * float(R));
+  const float g0 = cm * e0, g1 = cm * e1, g2 = cm * e2;
+  const int n = int(W.n_color[r]);
+  const int64_t off = W.color_off[r];
+  const float cp = L.rgbper * 2.f / float(R);
+  float per = 0.f;
+  for (int j = lane; j < n; j += 32) {
+    const int64_t m = off + j;
+    const float w = W.r_w[m];
+    const float y0 = rgb[m * 3], y1 = rgb[m * 3 + 1], y2 = rgb[m * 3 + 2];
+    const float d0 = y0 - t0, d1 = y1 - t1, d2 = y2 - t2;
+    per += (d0 * d0 + d1 * d1 + d2 * d2) * w;
+    grad_rgb[m * 3] = w * g0 + cp * w * d0;
+    grad_rgb[m * 3 + 1] = w * g1 + cp * w * d1;
+    grad_rgb[m * 3 + 2] = w * g2 + cp * w * d2;
+    grad_w[m] = g0 * y0 + g1 * y1 + g2 * y2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) per += __shfl_xor_sync(0xffffffffu, per, o);
+  if (lane == 0) {
+    const float T = W.T_last[r];
+    const float p = fminf(fmaxf(T, 1e-6f), 1.f - 1e-6f);
+    const float ent = -(p * logf(p) + (1.f - p) * logf(1.f - p));
+    const float dent = (T > 1e-6f && T < 1.f - 1e-6f) ? logf((1.f - p) / p) : 0.f;
+    grad_last[r] = L.bg * (g0 + g1 + g2) + L.ent / float(R) * dent;
+    loss_part[r] = L.main * (e0 * e0 + e1 * e1 + e2 * e2) / (3.f * float(R)) +
+                   L.ent * ent / float(R) + L.rgbper * per / float(R);
+  }
+}
+
+// Fixed-order sum of the per-ray loss partials (one block).
+__global__ void k_loss_sum(const float* __restrict__ part, int R, float* out) {
+  __shared__ float s[1024];
+  float acc = 0.f;
+  for (int i = threadIdx.x; i < R; i += blockDim.x) acc += part[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = s[0];
+}
+
+static int train_reserve(pvdb_march_s* m, int C) {
+  const size_t rows = size_t(m->slots);
+  if (m->t_cap_rows >= rows && m->t_rgb) return PVDB_OK;
+  void** ps[] = {(void**)&m->t_rgb, (void**)&m->t_grad_rgb, (void**)&m->t_grad_w,
+                 (void**)&m->t_grad_k0, (void**)&m->t_grad_last, (void**)&m->t_loss_part,
+                 (void**)&m->t_rgb_marched};
+  for (void** p : ps) {
+    dev_free(*p);
+    *p = nullptr;
+  }
+  const size_t R = m->max_rays;
+  int rc;
+  if ((rc = dev_alloc((void**)&m->t_rgb, rows * 12)) ||
+      (rc = dev_alloc((void**)&m->t_grad_rgb, rows * 12)) ||
+      (rc = dev_alloc((void**)&m->t_grad_w, rows * 4)) ||
+      (rc = dev_alloc((void**)&m->t_grad_k0, rows * 4 * size_t(C))) ||
+      (rc = dev_alloc((void**)&m->t_grad_last, R * 4)) ||
+      (rc = dev_alloc((void**)&m->t_loss_part, R * 4)) ||
+      (rc = dev_alloc((void**)&m->t_rgb_marched, R * 12)))
+    return rc;
+  m->t_cap_rows = rows;
+  return PVDB_OK;
+}
+
+}  // namespace pvdb
+
+using namespace pvdb;
+
+extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_opt,
+                               pvdb_rgbnet_state* net, const float* rays_o, const float* rays_d,
+                               const float* viewdirs, const float* target, int32_t n_rays,
+                               const pvdb_train_config* cfg, float* loss_out, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(m && density_opt && k0_opt && net && cfg && loss_out, "null argument");
+  PVDB_REQUIRE(n_rays > 0 && n_rays <= m->max_rays, "n_rays must be in 1..max_rays");
+  PVDB_REQUIRE(rays_o && rays_d && viewdirs && target, "null rays");
+  PVDB_REQUIRE(net->params && net->grads && net->exp_avg && net->exp_avg_sq && net->step &&
+                   net->lr,
+               "null rgbnet state");
+  PVDB_REQUIRE(net->width == 128 && net->c0 > 0 && net->c0 <= 16 && net->pe >= 0 && net->pe <= 4,
+               "unsupported rgbnet shape");
+  pvdb_grid_s* dg = opt_params(density_opt);
+  pvdb_grid_s* kg = opt_params(k0_opt);
+  PVDB_REQUIRE(dg->C == 1 && kg->C == net->c0, "grid channels do not match the rgbnet");
+  cudaStream_t st = as_stream(s);
+  int rc = train_reserve(m, kg->C);
+  if (rc) return rc;
+  // parameters in the flat layout [w0,b0,w1,b1,w2,b2]
+  MlpArgs a;
+  a.c0 = net->c0;
+  a.dpe = 3 + 6 * net->pe;
+  a.din = a.c0 + a.dpe;
+  const int W = 128;
+  a.w0 = net->params;
+  a.b0 = a.w0 + W * a.din;
+  a.w1 = a.b0 + W;
+  a.b1 = a.w1 + W * W;
+  a.w2 = a.b1 + W;
+  a.b2 = a.w2 + 3 * W;
+  const int64_t P = int64_t(W) * a.din + W + W * W + W + 3 * W + 3;
+
+  prof_begin_call();
+  prof_mark(st, 0);
+  struct ProfGuard {
+    pvdb_march_s* m;
+    ~ProfGuard() { m->prof = false; }
+  } guard{m};
+  m->prof = true;
+  rc = march_forward_impl(m, dg, kg, rays_o, rays_d, n_rays, &cfg->march, nullptr, nullptr, st);
+  if (rc) return rc;
+  rc = mlp_forward_impl(m, a, viewdirs, m->t_rgb, st);
+  if (rc) return rc;
+  prof_mark(st, 3);
+  rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
+  if (rc) return rc;
+  LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
+  k_loss<<<ceil_div(n_rays, 8), 256, 0, st>>>(m->w, m->t_rgb, m->t_rgb_marched, target, n_rays, L,
+                                              m->t_grad_rgb, m->t_grad_w, m->t_grad_last,
+                                              m->t_loss_part);
+  PVDB_CHECK_LAUNCH("k_loss");
+  k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, loss_out);
+  PVDB_CHECK_LAUNCH("k_loss_sum");
+  prof_mark(st, 4);
+  rc = mlp_backward_impl(m, a, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads, st);
+  if (rc) return rc;
+  prof_mark(st, 5);
+  rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);
+  if (rc) return rc;
+  // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
+  const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
+  if (cfg->tv_weight_density > 0.f) {
+    const float w = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
+    rc = pvdb_grid_tv_add_grad(dg, w, w, w, cfg->tv_dense_mode, 0, s);
+    if (rc) return rc;
+  }
+  if (cfg->tv_weight_k0 > 0.f) {
+    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
+    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0, s);
+    if (rc) return rc;
+  }
+  prof_mark(st, 9);
+  rc = opt_step_launch(density_opt, 1, 1, st);
+  if (rc) return rc;
+  rc = opt_step_launch(k0_opt, 1, 1, st);
+  if (rc) return rc;
+  prof_mark(st, 10);
+  *net->step += 1;
+  const float stepsz = adam_step_size(*net->lr, cfg->rgbnet_beta1, cfg->rgbnet_beta2, *net->step);
+  rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P, stepsz,
+                         cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0, st);
+  if (rc) return rc;
+  prof_mark(st, 11);
+  *net->lr *= cfg->lr_decay_factor;
+  opt_lr_scale(density_opt, cfg->lr_decay_factor);
+  opt_lr_scale(k0_opt, cfg->lr_decay_factor);
+  return PVDB_OK;
+}

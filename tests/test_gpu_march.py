@@ -1,0 +1,220 @@
+"""GPU parity of the fused ray-march stages (sample, MLP, composite) and of the
+fused train step against the CPU oracle (FP32-mimic for exact structure, FP64
+for the stated tolerances: samples/RGB 1e-5 relative, gradients 1e-4)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RESO = 40
+
+
+@pytest.fixture(scope="module")
+def setup(lib):
+    import torch
+    from plenvdb_gb300.march import MarchWorkspace, march_params
+    from plenvdb_gb300.scene import (CameraConfig, SceneConfig, build_grids, random_rays,
+                                     scene_dense)
+    from plenvdb_gb300.trainer import FineStageConfig
+    scfg = SceneConfig(reso=RESO, n_ellipsoids=5, seed=11)
+    cfg = FineStageConfig(reso=RESO)
+    cam = CameraConfig()
+    ro, rd, vd = random_rays(cam, 700, 6, seed=4)
+    active, dens, k0 = scene_dense(scfg)
+    R3 = (RESO,) * 3
+    og = O.OGridData(R3, dens, active, background=scfg.background)
+    ok = O.OGridData(R3, k0, active, background=0.0)
+    op = O.march_params(cfg.xyz_min, cfg.xyz_max, cfg.near, cfg.stepdist, cfg.act_shift,
+                        cfg.interval, cfg.fast_color_thres)
+    gp = march_params(cfg.xyz_min, cfg.xyz_max, cfg.near, cfg.stepdist, cfg.act_shift,
+                      cfg.interval, cfg.fast_color_thres)
+    return dict(scfg=scfg, cfg=cfg, ro=ro, rd=rd, vd=vd, og=og, ok=ok, op=op, gp=gp)
+
+
+def _march(setup):
+    import torch
+    from plenvdb_gb300.march import MarchSample, MarchWorkspace
+    from plenvdb_gb300.scene import build_grids
+    s = setup
+    dg, kg = build_grids(s["scfg"])
+    ws = MarchWorkspace(1024, s["cfg"].xyz_min, s["cfg"].xyz_max, s["cfg"].stepdist)
+    dummy = torch.zeros(1, device="cuda", requires_grad=True)
+    ro, rd = torch.from_numpy(s["ro"]).cuda(), torch.from_numpy(s["rd"]).cuda()
+    out = MarchSample.apply(dummy, ws, dg, kg, ro, rd, s["gp"])
+    return dg, kg, ws, dummy, out
+
+
+def test_sample_stage_matches_oracle_fp32_structure(setup):
+    import torch
+    dg, kg, ws, dummy, (w, last, k0, rid) = _march(setup)
+    om = O.March(setup["og"], setup["ok"], setup["ro"], setup["rd"], setup["op"], fp32=True)
+    torch.cuda.synchronize()
+    assert om.M > 1000
+    np.testing.assert_array_equal(rid.cpu().numpy(), om.ray_id)
+    # bit-identical transmittance chain and positions
+    np.testing.assert_array_equal(last.cpu().numpy(), om.T_last.astype(np.float32))
+    np.testing.assert_allclose(w.cpu().numpy(), om.weight, rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(k0.cpu().numpy(), om.k0, rtol=1e-6, atol=1e-7)
+
+
+def test_sample_stage_within_1e5_of_fp64(setup):
+    import torch
+    dg, kg, ws, dummy, (w, last, k0, rid) = _march(setup)
+    om = O.March(setup["og"], setup["ok"], setup["ro"], setup["rd"], setup["op"], fp32=False)
+    torch.cuda.synchronize()
+    if om.M != w.shape[0] or not np.array_equal(om.ray_id, rid.cpu().numpy()):
+        pytest.skip("a threshold decision differs between FP32 and FP64 on this draw")
+    np.testing.assert_allclose(last.cpu().numpy(), om.T_last, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(w.cpu().numpy(), om.weight, rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(k0.cpu().numpy(), om.k0, rtol=1e-5, atol=1e-7)
+
+
+def test_sample_backward_matches_fp64_and_is_deterministic(setup):
+    import torch
+    from plenvdb_gb300 import _lib as L
+    rng = np.random.default_rng(7)
+    results = []
+    for rep in range(2):
+        dg, kg, ws, dummy, (w, last, k0, rid) = _march(setup)
+        M, R = w.shape[0], last.shape[0]
+        gw = torch.from_numpy(rng.normal(0, 1, M).astype(np.float32) if rep == 0 else gw_np).cuda()
+        if rep == 0:
+            gw_np = gw.cpu().numpy()
+            gl_np = np.random.default_rng(8).normal(0, 1, R).astype(np.float32)
+            gk_np = np.random.default_rng(9).normal(0, 1, (M, 12)).astype(np.float32)
+        gl = torch.from_numpy(gl_np).cuda()
+        gk = torch.from_numpy(gk_np).cuda()
+        torch.autograd.backward([w, last, k0], [gw, gl, gk])
+        gd = dg.get_dense_grid(which=L.WHICH_GRAD).reshape((RESO,) * 3)
+        gkk = kg.get_dense_grid(which=L.WHICH_GRAD).reshape((RESO,) * 3 + (12,))
+        results.append((gd, gkk))
+    assert np.array_equal(results[0][0], results[1][0]), "density grad not reproducible"
+    assert np.array_equal(results[0][1], results[1][1]), "k0 grad not reproducible"
+    om = O.March(setup["og"], setup["ok"], setup["ro"], setup["rd"], setup["op"], fp32=False)
+    if om.M != gw_np.size:
+        pytest.skip("a threshold decision differs between FP32 and FP64 on this draw")
+    ref_d, ref_k = om.backward_sample(gw_np, gl_np, gk_np)
+    gd, gkk = results[0]
+    scale_d = np.abs(ref_d).max()
+    scale_k = np.abs(ref_k).max()
+    np.testing.assert_allclose(gd, ref_d, rtol=1e-4, atol=1e-4 * scale_d)
+    np.testing.assert_allclose(gkk, ref_k, rtol=1e-4, atol=1e-5 * scale_k)
+
+
+def test_mlp_and_composite_match_fp64(setup):
+    import torch
+    from plenvdb_gb300.march import CompositeFn, RgbNetFn
+    from plenvdb_gb300.scene import rgbnet_init
+    dg, kg, ws, dummy, (w, last, k0, rid) = _march(setup)
+    params = [p.cuda().requires_grad_() for p in rgbnet_init(seed=3)]
+    vd = torch.from_numpy(setup["vd"]).cuda()
+    k0r = k0.detach().clone().requires_grad_()
+    rgb = RgbNetFn.apply(k0r, vd, ws, 4, 0, *params)
+    wr = w.detach().clone().requires_grad_()
+    lr = last.detach().clone().requires_grad_()
+    rgbm = CompositeFn.apply(wr, rgb, lr, ws, 1.0)
+    # fp64 torch reference of the same stages
+    P64 = [p.detach().double().requires_grad_() for p in params]
+    k64 = k0.detach().double().requires_grad_()
+    w64 = w.detach().double().requires_grad_()
+    l64 = last.detach().double().requires_grad_()
+    v = vd.double()
+    freq = torch.tensor([1.0, 2.0, 4.0, 8.0], dtype=torch.float64, device="cuda")
+    emb = (v.unsqueeze(-1) * freq).flatten(-2)
+    pe = torch.cat([v, emb.sin(), emb.cos()], -1)[rid.long()]
+    x = torch.cat([k64, pe], -1)
+    h = torch.relu(x @ P64[0].T + P64[1])
+    h = torch.relu(h @ P64[2].T + P64[3])
+    rgb64 = torch.sigmoid(h @ P64[4].T + P64[5])
+    out64 = torch.zeros(last.shape[0], 3, dtype=torch.float64, device="cuda")
+    out64 = out64.index_add(0, rid.long(), w64[:, None] * rgb64) + l64[:, None] * 1.0
+    np.testing.assert_allclose(rgb.detach().cpu().numpy(), rgb64.detach().cpu().numpy(),
+                               rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(rgbm.detach().cpu().numpy(), out64.detach().cpu().numpy(),
+                               rtol=1e-5, atol=1e-6)
+    g = torch.randn(last.shape[0], 3, device="cuda", dtype=torch.float32,
+                    generator=torch.Generator(device="cuda").manual_seed(1))
+    rgbm.backward(g)
+    out64.backward(g.double())
+    for a, b in zip(params, P64):
+        scale = b.grad.abs().max().item()
+        np.testing.assert_allclose(a.grad.cpu().numpy(), b.grad.cpu().numpy(), rtol=1e-4,
+                                   atol=1e-5 * scale)
+    for a, b in ((k0r, k64), (wr, w64), (lr, l64)):
+        scale = b.grad.abs().max().item()
+        np.testing.assert_allclose(a.grad.cpu().numpy(), b.grad.cpu().numpy(), rtol=1e-4,
+                                   atol=1e-5 * scale)
+
+
+def test_fused_train_step_equals_staged_autograd(setup):
+    """pvdb_train_step == the three autograd stages + torch losses + the
+    reference optimiser calls, for one iteration."""
+    import torch
+    from plenvdb_gb300 import ColorOpt, DensityOpt
+    from plenvdb_gb300.march import CompositeFn, MarchSample, MarchWorkspace, RgbNetFn
+    from plenvdb_gb300.masked_adam import MaskedAdam
+    from plenvdb_gb300.scene import build_grids, rgbnet_init
+    from plenvdb_gb300.trainer import FineStageTrainer
+    s = setup
+    cfg = s["cfg"]
+    ro, rd, vd = (torch.from_numpy(a).cuda() for a in (s["ro"], s["rd"], s["vd"]))
+    R = ro.shape[0]
+    tgt = torch.rand(R, 3, generator=torch.Generator().manual_seed(5)).cuda()
+    # fused
+    dg1, kg1 = build_grids(s["scfg"])
+    tr = FineStageTrainer(dg1, kg1, rgbnet_init(seed=2), cfg, max_rays=1024)
+    loss_f = float(tr.step(ro, rd, vd, tgt))
+    # staged
+    dg2, kg2 = build_grids(s["scfg"])
+    dg2.zero_grad(); kg2.zero_grad()
+    dopt = DensityOpt(dg2, cfg.lr_density, cfg.eps, *cfg.betas)
+    kopt = ColorOpt(kg2, cfg.lr_k0, cfg.eps, *cfg.betas)
+    params = [p.cuda().requires_grad_() for p in rgbnet_init(seed=2)]
+    netopt = MaskedAdam([{"params": params, "lr": cfg.lr_rgbnet, "skip_zero_grad": False}],
+                        betas=cfg.betas, eps=cfg.eps)
+    ws = MarchWorkspace(1024, cfg.xyz_min, cfg.xyz_max, cfg.stepdist)
+    dummy = torch.zeros(1, device="cuda", requires_grad=True)
+    w, last, k0, rid = MarchSample.apply(dummy, ws, dg2, kg2, ro, rd, s["gp"])
+    rgb = RgbNetFn.apply(k0, vd, ws, 4, 0, *params)
+    rgbm = CompositeFn.apply(w, rgb, last, ws, cfg.bg)
+    loss = cfg.weight_main * torch.nn.functional.mse_loss(rgbm, tgt)
+    pout = last.clamp(1e-6, 1 - 1e-6)
+    loss = loss + cfg.weight_entropy_last * -(pout * torch.log(pout) + (1 - pout) * torch.log(1 - pout)).mean()
+    rgbper = (rgb - tgt[rid.long()]).pow(2).sum(-1)
+    loss = loss + cfg.weight_rgbper * (rgbper * w.detach()).sum() / R
+    loss.backward()
+    wsz = max(dg2.reso) / 128.0
+    dg2.total_variation_add_grad(cfg.tv_weight / R * wsz, cfg.tv_weight / R * wsz,
+                                 cfg.tv_weight / R * wsz, False)
+    kg2.total_variation_add_grad(cfg.tv_weight / R * wsz, cfg.tv_weight / R * wsz,
+                                 cfg.tv_weight / R * wsz, False)
+    netopt.step()
+    dopt.step(1)
+    kopt.step(1)
+    torch.cuda.synchronize()
+    assert abs(loss_f - loss.item()) <= 1e-5 * abs(loss.item())
+    np.testing.assert_allclose(dg1.get_dense_grid(), dg2.get_dense_grid(), rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(kg1.get_dense_grid(), kg2.get_dense_grid(), rtol=1e-5, atol=1e-5)
+    flat = torch.cat([p.detach().reshape(-1) for p in params])
+    np.testing.assert_allclose(tr.params.cpu().numpy(), flat.cpu().numpy(), rtol=1e-5, atol=1e-6)
+
+
+def test_fused_train_loss_decreases_and_is_deterministic(setup):
+    import torch
+    from plenvdb_gb300.scene import build_grids, rgbnet_init
+    from plenvdb_gb300.trainer import FineStageTrainer
+    s = setup
+    ro, rd, vd = (torch.from_numpy(a).cuda() for a in (s["ro"], s["rd"], s["vd"]))
+    tgt = torch.rand(ro.shape[0], 3, generator=torch.Generator().manual_seed(6)).cuda()
+    runs = []
+    for _ in range(2):
+        dg, kg = build_grids(s["scfg"])
+        tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), s["cfg"], max_rays=1024)
+        losses = [float(tr.step(ro, rd, vd, tgt)) for _ in range(30)]
+        runs.append((losses, dg.get_dense_grid(), tr.params.cpu().numpy()))
+    assert runs[0][0][-1] < 0.8 * runs[0][0][0]
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1])
+    assert np.array_equal(runs[0][2], runs[1][2])

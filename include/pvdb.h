@@ -135,6 +135,21 @@ int pvdb_grid_sample(pvdb_grid g, const float* xs, const float* ys, const float*
 int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys, const float* zs,
                               const float* grad_out, int64_t n, int32_t mem, pvdb_stream s);
 
+/* Same result as pvdb_grid_sample_backward (device buffers only), for callers
+ * that cannot let the library allocate device memory: processes that reserve
+ * all device memory up front through their own pool or run under a fixed
+ * memory budget, and callers that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree. No counterpart in the reference.
+ * The call allocates nothing: its scratch is one fixed file-scope device array
+ * (about 4.3 MB, held on every GPU that loads the library until exit) that
+ * limits a call to n <= 32768 points (PVDB_ERR_ARG beyond that). The first
+ * call on a device looks up that array's address (cudaGetSymbolAddress); make
+ * it before any stream capture. All calls share the array, so calls that
+ * overlap on the GPU (e.g. on two streams) race. */
+int pvdb_grid_sample_backward_noalloc(pvdb_grid g, const float* xs, const float* ys,
+                                      const float* zs, const float* grad_out, int64_t n,
+                                      pvdb_stream s);
+
 /* forward_single (plenvdb.h:503-523, densityvdb.cu:376-403,
  * colorvdb.cu:380-413): value at integer coordinates (stored value inside an
  * allocated leaf whether active or not, else background); active_out (may be

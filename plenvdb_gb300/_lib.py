@@ -101,6 +101,7 @@ _SIGS = {
     "pvdb_grid_set_values_by_mask": (C.c_int, [vp, vp, i64, f32, i32, vp]),
     "pvdb_grid_sample": (C.c_int, [vp, vp, vp, vp, i64, vp, i32, vp]),
     "pvdb_grid_sample_backward": (C.c_int, [vp, vp, vp, vp, vp, i64, i32, vp]),
+    "pvdb_grid_sample_backward_noalloc": (C.c_int, [vp, vp, vp, vp, vp, i64, vp]),
     "pvdb_grid_lookup": (C.c_int, [vp, vp, vp, vp, i64, vp, vp, i32, vp]),
     "pvdb_grid_tv_add_grad": (C.c_int, [vp, f32, f32, f32, i32, i32, vp]),
     "pvdb_grid_zero_grad": (C.c_int, [vp, vp]),

@@ -370,9 +370,10 @@ typedef struct pvdb_mlp_weights {
 } pvdb_mlp_weights;
 
 /* rgb[m] = sigmoid(MLP([k0[m], PE(viewdirs[ray_id[m]])])) for rows m < totals[1]
- * of the march workspace. */
-int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs,
-                     float* rgb, int32_t precision, pvdb_stream s);
+ * of the march workspace (ray ids from the workspace). k0 [M, c0] is the
+ * caller's feature rows; NULL uses the workspace's k0 rows. */
+int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
+                     const float* viewdirs, float* rgb, int32_t precision, pvdb_stream s);
 
 typedef struct pvdb_mlp_grads {
   float* w0; float* b0; float* w1; float* b1; float* w2; float* b2; /* overwritten */
@@ -381,9 +382,9 @@ typedef struct pvdb_mlp_grads {
 /* Given grad_rgb [M,3] (gradient w.r.t. the sigmoid output) and rgb, writes the
  * weight gradients (deterministic: fixed-order reduction of per-CTA partials)
  * and grad_k0 [M, c0]. */
-int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs,
-                      const float* rgb, const float* grad_rgb, pvdb_mlp_grads* g,
-                      float* grad_k0, int32_t precision, pvdb_stream s);
+int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
+                      const float* viewdirs, const float* rgb, const float* grad_rgb,
+                      pvdb_mlp_grads* g, float* grad_k0, int32_t precision, pvdb_stream s);
 
 /* ------------------------------------------------------- fused train step
  * One fine-stage iteration (run.py:516-598) on device-resident rays:

@@ -139,9 +139,9 @@ _SIGS = {
     "pvdb_march_backward": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "pvdb_composite_forward": (C.c_int, [vp, vp, f32, vp, i32, vp]),
     "pvdb_composite_backward": (C.c_int, [vp, vp, vp, f32, vp, vp, vp, i32, vp]),
-    "pvdb_mlp_forward": (C.c_int, [vp, C.POINTER(MlpWeights), vp, vp, i32, vp]),
-    "pvdb_mlp_backward": (C.c_int, [vp, C.POINTER(MlpWeights), vp, vp, vp, C.POINTER(MlpGrads),
-                                    vp, i32, vp]),
+    "pvdb_mlp_forward": (C.c_int, [vp, C.POINTER(MlpWeights), vp, vp, vp, i32, vp]),
+    "pvdb_mlp_backward": (C.c_int, [vp, C.POINTER(MlpWeights), vp, vp, vp, vp,
+                                    C.POINTER(MlpGrads), vp, i32, vp]),
     "pvdb_train_step": (C.c_int, [vp, vp, vp, C.POINTER(RgbnetState), vp, vp, vp, vp, i32,
                                   C.POINTER(TrainConfig), vp, vp]),
     "pvdb_renderer_create": (C.c_int, [i32, i32, i32, i32, C.POINTER(vp)]),

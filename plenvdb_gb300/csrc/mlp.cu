@@ -402,8 +402,14 @@ static int mlp_reserve(pvdb_march_s* m, int din) {
   return dev_reserve((void**)&m->wpart, &m->wpart_cap, (size_t(mlp_grid()) + 1) * P * 4);
 }
 
-int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, float* rgb,
-                     cudaStream_t st) {
+int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
+                        const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
+                        const int32_t* ray, const float* hpe, const uint32_t* totals, float* out,
+                        int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
+                        cudaStream_t st);
+
+int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
+                     const float* viewdirs, float* rgb, int precision, cudaStream_t st) {
   const int R = m->n_rays;
   if (R <= 0) return PVDB_OK;
   int rc = mlp_reserve(m, a.din);
@@ -412,16 +418,14 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, f
   float* pe = m->hpe + size_t(m->max_rays) * kW;
   k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
-  static bool attr = false;
-  if (!attr) {
-    PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(sizeof(MlpSmem))));
-    PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(sizeof(MlpBwdSmem))));
-    attr = true;
-  }
+  if (precision == 1)
+    return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
+                               m->w.r_ray, hpe, m->w.totals, rgb, 0, &m->mlp_packed,
+                               &m->mlp_packed_cap, m->w.totals + 3, st);
+  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(sizeof(MlpSmem))));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
-      a, m->w.r_k0, m->w.r_ray, hpe, m->w.totals, rgb, 0);
+      a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_f32");
   return PVDB_OK;
 }
@@ -430,12 +434,16 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, f
 // viewdirs [R,3]; M = totals[1]. hpe_buf holds R*(128+32) floats.
 int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
                      const float* viewdirs, int R, const uint32_t* totals, float* out,
-                     int out_logits, float* hpe_buf, cudaStream_t st) {
+                     int out_logits, float* hpe_buf, int precision, void** blob,
+                     size_t* blob_cap, uint32_t* err, cudaStream_t st) {
   if (R <= 0) return PVDB_OK;
   float* hpe = hpe_buf;
   float* pe = hpe_buf + size_t(R) * kW;
   k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
+  if (precision == 1)
+    return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, hpe,
+                               totals, out, out_logits, blob, blob_cap, err, st);
   PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(sizeof(MlpSmem))));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
@@ -445,8 +453,8 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
 }
 
 // hpe/pe of the current forward must still be in the workspace.
-int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* rgb, const float* grad_rgb,
-                      float* grad_k0, float* grad_flat, cudaStream_t st) {
+int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
+                      const float* grad_rgb, float* grad_k0, float* grad_flat, cudaStream_t st) {
   const int R = m->n_rays;
   const int64_t P = mlp_param_count(a.din);
   if (R <= 0) {
@@ -459,7 +467,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* rgb, const
                                        int(sizeof(MlpBwdSmem))));
   const int G = mlp_grid();
   k_mlp_bwd_f32<<<G, kMlpThreads, sizeof(MlpBwdSmem), st>>>(
-      a, m->w.r_k0, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
+      a, k0rows, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
       grad_rgb, grad_k0, m->wpart);
   PVDB_CHECK_LAUNCH("k_mlp_bwd_f32");
   k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
@@ -485,8 +493,8 @@ using namespace pvdb;
 
 extern "C" {
 
-int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs, float* rgb,
-                     int32_t precision, pvdb_stream s) {
+int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
+                     const float* viewdirs, float* rgb, int32_t precision, pvdb_stream s) {
   clear_error();
   PVDB_REQUIRE(m && viewdirs && rgb, "null argument");
   PVDB_REQUIRE(m->has_fwd, "mlp before march forward");
@@ -495,13 +503,12 @@ int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewd
   MlpArgs a;
   int rc = mlp_args_from(w, a);
   if (rc) return rc;
-  (void)precision;  // the BF16 tensor-core path shares this entry (mlp_tc.cu)
-  return mlp_forward_impl(m, a, viewdirs, rgb, as_stream(s));
+  return mlp_forward_impl(m, a, k0 ? k0 : m->w.r_k0, viewdirs, rgb, precision, as_stream(s));
 }
 
-int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* viewdirs,
-                      const float* rgb, const float* grad_rgb, pvdb_mlp_grads* g,
-                      float* grad_k0, int32_t precision, pvdb_stream s) {
+int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
+                      const float* viewdirs, const float* rgb, const float* grad_rgb,
+                      pvdb_mlp_grads* g, float* grad_k0, int32_t precision, pvdb_stream s) {
   clear_error();
   PVDB_REQUIRE(m && viewdirs && rgb && grad_rgb && g && grad_k0, "null argument");
   PVDB_REQUIRE(m->has_fwd, "mlp before march forward");
@@ -520,7 +527,7 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* view
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   const int64_t P = mlp_param_count(a.din);
   float* flat = m->wpart + int64_t(mlp_grid()) * P;  // spare slot after the partials
-  rc = mlp_backward_impl(m, a, rgb, grad_rgb, grad_k0, flat, st);
+  rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, st);
   if (rc) return rc;
   k_scatter_grads<<<ceil_div(P, 256), 256, 0, st>>>(flat, a.din, g->w0, g->b0, g->w1, g->b1, g->w2,
                                                      g->b2);

@@ -39,7 +39,8 @@ struct MlpArgs {
 };
 int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
                      const float* viewdirs, int R, const uint32_t* totals, float* out,
-                     int out_logits, float* hpe_buf, cudaStream_t st);
+                     int out_logits, float* hpe_buf, int precision, void** blob,
+                     size_t* blob_cap, uint32_t* err, cudaStream_t st);
 
 struct RenderP {
   int H, W, inverse_y;
@@ -260,6 +261,8 @@ struct pvdb_renderer_s {
   int32_t* d_rpix = nullptr;
   float* d_logits = nullptr;
   int64_t rows_cap = 0;
+  void* d_packed = nullptr;  // BF16 weight tiles of the tensor-core rgbnet
+  size_t packed_cap = 0;
 };
 
 static int renderer_grow_rows(pvdb_renderer_s* r, int64_t need) {
@@ -312,7 +315,7 @@ int pvdb_renderer_destroy(pvdb_renderer r) {
   pvdb_grid_destroy(r->topo);
   void* ptrs[] = {r->d_rows, r->d_den, r->d_col, r->d_colh, r->d_params, r->d_n, r->d_off,
                   r->d_T, r->d_viewdirs, r->d_hpe, r->d_image, r->d_totals, r->scan_partial,
-                  r->d_rk0, r->d_rw, r->d_rpix, r->d_logits};
+                  r->d_rk0, r->d_rw, r->d_rpix, r->d_logits, r->d_packed};
   for (void* p : ptrs) dev_free(p);
   delete r;
   return PVDB_OK;
@@ -481,7 +484,7 @@ int pvdb_renderer_render(pvdb_renderer r, int32_t precision, pvdb_stream s) {
     if (!r->flags[q])
       return set_error(PVDB_ERR_STATE,
                        "render needs load_data, load_params, setScene, setKwargs and input_a_c2w");
-  (void)precision;
+  PVDB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (FP32) or 1 (BF16 rgbnet)");
   cudaStream_t st = as_stream(s);
   RenderP P{};
   P.H = r->H;
@@ -550,7 +553,7 @@ int pvdb_renderer_render(pvdb_renderer r, int32_t precision, pvdb_stream s) {
   a.din = din;
   if (total) {
     rc = mlp_forward_rows(a, r->d_rk0, r->d_rpix, r->d_viewdirs, HW, r->d_totals, r->d_logits, 1,
-                          r->d_hpe, st);
+                          r->d_hpe, precision, &r->d_packed, &r->packed_cap, r->d_totals + 3, st);
     if (rc) return rc;
   }
   prof_mark(st, 4);

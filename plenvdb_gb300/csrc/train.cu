@@ -18,10 +18,10 @@ struct MlpArgs {
   const float* w2; const float* b2;
   int c0, dpe, din;
 };
-int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, float* rgb,
-                     cudaStream_t st);
-int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* rgb, const float* grad_rgb,
-                      float* grad_k0, float* grad_flat, cudaStream_t st);
+int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
+                     const float* viewdirs, float* rgb, int precision, cudaStream_t st);
+int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
+                      const float* grad_rgb, float* grad_k0, float* grad_flat, cudaStream_t st);
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st);
@@ -163,7 +163,7 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   m->prof = true;
   rc = march_forward_impl(m, dg, kg, rays_o, rays_d, n_rays, &cfg->march, nullptr, nullptr, st);
   if (rc) return rc;
-  rc = mlp_forward_impl(m, a, viewdirs, m->t_rgb, st);
+  rc = mlp_forward_impl(m, a, m->w.r_k0, viewdirs, m->t_rgb, cfg->precision, st);
   if (rc) return rc;
   prof_mark(st, 3);
   rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
@@ -176,7 +176,7 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, loss_out);
   PVDB_CHECK_LAUNCH("k_loss_sum");
   prof_mark(st, 4);
-  rc = mlp_backward_impl(m, a, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads, st);
+  rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads, st);
   if (rc) return rc;
   prof_mark(st, 5);
   rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);

@@ -154,21 +154,22 @@ class RgbNetFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, k0, viewdirs, ws: MarchWorkspace, pe, precision, w0, b0, w1, b1, w2, b2):
         M = k0.shape[0]
+        k0 = k0.detach().float().contiguous()
         viewdirs = viewdirs.float().contiguous()
         ws_params = [t.detach().float().contiguous() for t in (w0, b0, w1, b1, w2, b2)]
         rgb = torch.empty(M, 3, device=k0.device, dtype=torch.float32)
         s = _mlp_struct(*ws_params, k0.shape[1], pe)
         if M:
-            L.call("pvdb_mlp_forward", ws.h, C.byref(s), L.ptr(viewdirs), L.ptr(rgb),
+            L.call("pvdb_mlp_forward", ws.h, C.byref(s), L.ptr(k0), L.ptr(viewdirs), L.ptr(rgb),
                    int(precision), L.stream_of())
-        ctx.save_for_backward(viewdirs, rgb, *ws_params)
+        ctx.save_for_backward(k0, viewdirs, rgb, *ws_params)
         ctx.ws, ctx.pe, ctx.precision, ctx.gen = ws, pe, precision, ws.generation
         ctx.c0 = k0.shape[1]
         return rgb
 
     @staticmethod
     def backward(ctx, g_rgb):
-        viewdirs, rgb, w0, b0, w1, b1, w2, b2 = ctx.saved_tensors
+        k0, viewdirs, rgb, w0, b0, w1, b1, w2, b2 = ctx.saved_tensors
         ws = ctx.ws
         if ws.generation != ctx.gen:
             raise RuntimeError("march workspace was reused before this backward ran")
@@ -179,7 +180,7 @@ class RgbNetFn(torch.autograd.Function):
             s = _mlp_struct(w0, b0, w1, b1, w2, b2, ctx.c0, ctx.pe)
             g = L.MlpGrads()
             g.w0, g.b0, g.w1, g.b1, g.w2, g.b2 = (L.ptr(t) for t in grads)
-            L.call("pvdb_mlp_backward", ws.h, C.byref(s), L.ptr(viewdirs), L.ptr(rgb),
+            L.call("pvdb_mlp_backward", ws.h, C.byref(s), L.ptr(k0), L.ptr(viewdirs), L.ptr(rgb),
                    L.ptr(g_rgb.float().contiguous()), C.byref(g), L.ptr(gk0), int(ctx.precision),
                    L.stream_of())
         return (gk0, None, None, None, None, *grads)

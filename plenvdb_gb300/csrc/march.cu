@@ -643,6 +643,7 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
   if (total_kept) *total_kept = t[0];
   if (total_rows) *total_rows = t[1];
   if (t[3] & 1u) return set_error(PVDB_ERR_STATE, "a ray had more samples than samples_cap");
+  if (t[3] & 2u) return set_error(PVDB_ERR_TIMEOUT, "a tensor-core MMA wait timed out");
   return PVDB_OK;
 }
 

@@ -452,9 +452,17 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
   return PVDB_OK;
 }
 
+int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
+                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
+                         const int32_t* ray, const float* hpe, const float* pe, int pe_stride,
+                         const uint32_t* totals, const float* rgb, const float* grad_rgb,
+                         float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
+                         uint32_t* err, cudaStream_t st);
+
 // hpe/pe of the current forward must still be in the workspace.
 int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
-                      const float* grad_rgb, float* grad_k0, float* grad_flat, cudaStream_t st) {
+                      const float* grad_rgb, float* grad_k0, float* grad_flat, int precision,
+                      cudaStream_t st) {
   const int R = m->n_rays;
   const int64_t P = mlp_param_count(a.din);
   if (R <= 0) {
@@ -463,9 +471,19 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
   }
   int rc = mlp_reserve(m, a.din);
   if (rc) return rc;
+  const int G = mlp_grid();
+  if (precision == 1) {
+    rc = mlp_tc_backward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, m->w.r_ray,
+                              m->hpe, m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, rgb,
+                              grad_rgb, grad_k0, m->wpart, G, &m->mlp_packed, &m->mlp_packed_cap,
+                              m->w.totals + 3, st);
+    if (rc) return rc;
+    k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+    PVDB_CHECK_LAUNCH("k_wgrad_reduce");
+    return PVDB_OK;
+  }
   PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(sizeof(MlpBwdSmem))));
-  const int G = mlp_grid();
   k_mlp_bwd_f32<<<G, kMlpThreads, sizeof(MlpBwdSmem), st>>>(
       a, k0rows, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
       grad_rgb, grad_k0, m->wpart);
@@ -516,7 +534,7 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   MlpArgs a;
   int rc = mlp_args_from(w, a);
   if (rc) return rc;
-  (void)precision;
+  PVDB_REQUIRE(precision == 0 || precision == 1, "precision must be 0 (fp32) or 1 (bf16)");
   cudaStream_t st = as_stream(s);
   // hpe/pe depend only on the weights and viewdirs: recompute them so the
   // backward does not rely on a preceding forward call of the same weights.
@@ -527,7 +545,7 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   const int64_t P = mlp_param_count(a.din);
   float* flat = m->wpart + int64_t(mlp_grid()) * P;  // spare slot after the partials
-  rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, st);
+  rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, precision, st);
   if (rc) return rc;
   k_scatter_grads<<<ceil_div(P, 256), 256, 0, st>>>(flat, a.din, g->w0, g->b0, g->w1, g->b1, g->w2,
                                                      g->b2);

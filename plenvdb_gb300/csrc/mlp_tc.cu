@@ -30,6 +30,10 @@ constexpr uint32_t kOffW0 = 0;
 constexpr uint32_t kOffW1 = kOffW0 + 128 * 16 * 2;    // 4096
 constexpr uint32_t kOffW2 = kOffW1 + 128 * 128 * 2;   // 36864
 constexpr uint32_t kPackFwdBytes = kOffW2 + 16 * 128 * 2;  // 40960
+constexpr uint32_t kOffW1T = kPackFwdBytes;                // W1T [128x128]
+constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16x128]
+constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T [128x16]
+constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 81920
 // shared-memory layout of the forward kernel
 constexpr uint32_t kSmX = kPackFwdBytes;              // X tile [128x16] bf16
 constexpr uint32_t kSmH = kSmX + 128 * 16 * 2;        // H tile [128x128] bf16
@@ -49,8 +53,10 @@ struct MlpArgsTc {
   int c0, dpe, din;
 };
 
-// FP32 nn.Linear weights -> BF16 canonical K-major tiles (one thread per element).
-__global__ void k_pack_fwd(MlpArgsTc a, uint8_t* blob) {
+// FP32 nn.Linear weights -> BF16 canonical K-major tiles (one thread per
+// element). The forward uses the first kPackFwdBytes; the backward adds the
+// transposed tiles W1T [k][n], W0kT [q][n] and W2T [n][c].
+__global__ void k_pack(MlpArgsTc a, uint8_t* blob, int with_bwd) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   __nv_bfloat16* w0 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0);
   __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1);
@@ -66,6 +72,22 @@ __global__ void k_pack_fwd(MlpArgsTc a, uint8_t* blob) {
   if (t < 16 * 128) {
     const int n = t / 128, k = t % 128;
     w2[tc::kmaj(n, k, 128) / 2] = __float2bfloat16_rn(n < 3 ? a.w2[n * 128 + k] : 0.f);
+  }
+  if (!with_bwd) return;
+  __nv_bfloat16* w1t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1T);
+  __nv_bfloat16* w0t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0T);
+  __nv_bfloat16* w2t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW2T);
+  if (t < 128 * 128) {  // W1T[k][n] = w1[n][k]
+    const int k = t / 128, n = t % 128;
+    w1t[tc::kmaj(k, n, 128) / 2] = __float2bfloat16_rn(a.w1[n * 128 + k]);
+  }
+  if (t < 16 * 128) {  // W0kT[q][n] = w0[n][q] for q < c0
+    const int q = t / 128, n = t % 128;
+    w0t[tc::kmaj(q, n, 128) / 2] = __float2bfloat16_rn(q < a.c0 ? a.w0[n * a.din + q] : 0.f);
+  }
+  if (t < 128 * 16) {  // W2T[n][c] = w2[c][n] for c < 3
+    const int n = t / 16, c = t % 16;
+    w2t[tc::kmaj(n, c, 16) / 2] = __float2bfloat16_rn(c < 3 ? a.w2[c * 128 + n] : 0.f);
   }
 }
 
@@ -249,6 +271,415 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+
+// ---------------------------------------------------------------- backward
+// Per 128-row tile (one CTA per SM, persistent, all 512 TMEM columns):
+//   recompute  Z0 = X.W0k^T -> H0 = relu(Z0 + hpe);  Z1 = H0.W1^T -> H1 = relu(Z1 + b1)
+//   dl   = grad_rgb * y (1 - y)                       [128 x 3] (sigmoid backward)
+//   dZ1  = (dl . W2) * [H1 > 0]                       MMA K=16 (W2T)
+//   dZ0  = (dZ1 . W1) * [H0 > 0]                      MMA K=128 (W1T)
+//   gk0  = dZ0 . W0k                                  MMA N=16 (W0kT)
+//   dW2 += H1^T . dl      dW1|db1 += dZ1^T . [H0|1]   dW0|db0 += dZ0^T . [k0|PE|1]
+// The three weight-gradient accumulators stay in TMEM across all tiles of the
+// CTA (a ones column in H0 and in X turns the bias sums into one more MMA
+// column); the transposed operands are the same shared-memory tiles read
+// through MN-major descriptors. db2 is a per-thread FP32 sum. At the end the
+// CTA writes its partial gradients in the flat parameter layout; the partials
+// are summed over CTAs in a fixed order, so the result is deterministic.
+//
+// Shared memory (bytes). The tiles read through MN-major descriptors come
+// first and the weights (77824 B) last.
+constexpr uint32_t kBdZ1 = 0;                        // dZ1 [128 r][128 n]
+constexpr uint32_t kBdZ0 = kBdZ1 + 128 * 128 * 2;    // dZ0 [128 r][128 n]
+constexpr uint32_t kBH1 = kBdZ0 + 128 * 128 * 2;     // H1  [128 r][128 n]
+constexpr uint32_t kBH0 = kBH1 + 128 * 128 * 2;      // H0  [128 r][144 k], col 128 = 1
+constexpr uint32_t kBX = kBH0 + 128 * 144 * 2;       // X   [128 r][48 q]: k0 | PE | 1 | 0
+constexpr uint32_t kBDl = kBX + 128 * 48 * 2;        // dl  [128 r][16 c]
+constexpr uint32_t kBW = kBDl + 128 * 16 * 2;        // weights
+constexpr uint32_t kBW0k = kBW;                      // W0k  [128 n][16 q]
+constexpr uint32_t kBW1 = kBW0k + 128 * 16 * 2;      // W1   [128 n][128 k]
+constexpr uint32_t kBW1T = kBW1 + 128 * 128 * 2;     // W1T  [128 k][128 n]
+constexpr uint32_t kBW0T = kBW1T + 128 * 128 * 2;    // W0kT [16 q][128 n]
+constexpr uint32_t kBW2T = kBW0T + 16 * 128 * 2;     // W2T  [128 n][16 c]
+constexpr uint32_t kBB1 = kBW2T + 128 * 16 * 2;      // b1 f32[128]
+constexpr uint32_t kBBar = kBB1 + 128 * 4;
+constexpr uint32_t kBTmem = kBBar + 8;
+constexpr uint32_t kBFlag = kBTmem + 4;
+constexpr uint32_t kSmBwdBytes = kBFlag + 12;
+static_assert(kSmBwdBytes <= 232448, "backward tile exceeds 227 KB of shared memory");
+// TMEM columns
+constexpr uint32_t kTA = 0;      // Z0, then dZ1 (pre-mask)
+constexpr uint32_t kTB = 128;    // Z1, then dH0
+constexpr uint32_t kTG = 256;    // grad k0 [128 x 16]
+constexpr uint32_t kTW2 = 272;   // dW2 [128 n x 16 c]
+constexpr uint32_t kTW0 = 288;   // dW0|db0 [128 n x 48 q]
+constexpr uint32_t kTW1 = 336;   // dW1|db1 [128 n x 144 k]
+constexpr uint32_t kTmemBwdCols = 512;
+
+__device__ __forceinline__ bool bf16_pos(uint32_t bits16) { return (bits16 & 0x7FFFu) != 0u; }
+
+// relu mask of 8 BF16 activations (a uint4) applied to 8 FP32 values.
+__device__ __forceinline__ uint4 mask_pack(const float* v, uint4 h) {
+  const uint32_t w[4] = {h.x, h.y, h.z, h.w};
+  float o[8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    o[2 * i] = bf16_pos(w[i] & 0xFFFFu) ? v[2 * i] : 0.f;
+    o[2 * i + 1] = bf16_pos(w[i] >> 16) ? v[2 * i + 1] : 0.f;
+  }
+  uint4 pk;
+  pk.x = tc::pack_bf16(o[0], o[1]);
+  pk.y = tc::pack_bf16(o[2], o[3]);
+  pk.z = tc::pack_bf16(o[4], o[5]);
+  pk.w = tc::pack_bf16(o[6], o[7]);
+  return pk;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_mlp_bwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const float* __restrict__ k0,
+                 const int32_t* __restrict__ ray, const float* __restrict__ hpe,
+                 const float* __restrict__ pe, int pe_stride, const uint32_t* __restrict__ totals,
+                 const float* __restrict__ rgb, const float* __restrict__ grad_rgb,
+                 float* grad_k0, float* wpart, uint32_t* err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  const int64_t M = totals[1];
+  const int64_t ntiles = (M + 127) / 128;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t P = int64_t(kW) * a.din + kW + kW * kW + kW + 3 * kW + 3;
+  float* pw0 = wpart + int64_t(blockIdx.x) * P;
+  float* pb0 = pw0 + kW * a.din;
+  float* pw1 = pb0 + kW;
+  float* pb1 = pw1 + kW * kW;
+  float* pw2 = pb1 + kW;
+  float* pb2 = pw2 + 3 * kW;
+  if (blockIdx.x >= ntiles) {
+    for (int64_t i = tid; i < P; i += kTcThreads) pw0[i] = 0.f;
+    return;
+  }
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kBBar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kBTmem);
+  uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kBFlag);
+  float* b1s = reinterpret_cast<float*>(sm + kBB1);
+  {
+    const int4* src = reinterpret_cast<const int4*>(blob);
+    int4* dst = reinterpret_cast<int4*>(sm + kBW);
+    // W0k, W1 (blob 0..36864) and W1T, W0kT, W2T (blob 40960..81920)
+    for (int i = tid; i < int(kOffW2 / 16); i += kTcThreads) dst[i] = __ldg(src + i);
+    for (int i = tid; i < int((kPackAllBytes - kOffW1T) / 16); i += kTcThreads)
+      dst[kOffW2 / 16 + i] = __ldg(src + kOffW1T / 16 + i);
+  }
+  if (tid < 128) {
+    b1s[tid] = a.b1[tid];
+    // H0 columns 128..143: [1, 0 x 15] for every row
+    uint4 one = make_uint4(tc::pack_bf16(1.f, 0.f), 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 128, 144)) = one;
+    *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 136, 144)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  if (tid == 0) {
+    *flag = 0;
+    tc::mbar_init(bar, 1);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_slot, kTmemBwdCols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t sb = tc::smem_addr(sm);
+  const uint32_t id_r128 = tc::idesc_bf16(128, 128);              // K-major A and B
+  const uint32_t id_r16 = tc::idesc_bf16(128, 16);                // grad k0
+  const uint32_t id_w2 = tc::idesc_bf16(128, 16, true, true);     // H1^T . dl
+  const uint32_t id_w1 = tc::idesc_bf16(128, 144, true, true);    // dZ1^T . H0
+  const uint32_t id_w0 = tc::idesc_bf16(128, 48, true, true);     // dZ0^T . X
+  const int q4 = warp & 3, half = warp >> 2;
+  const int row = 32 * q4 + lane;
+  const uint32_t t_lane = tmem + (uint32_t(32 * q4) << 16);
+  float db2[3] = {0.f, 0.f, 0.f};
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int64_t row0 = t * 128;
+    // ---- X tile [k0 | PE | 1 | 0]: 6 chunks of 8 columns per row
+    for (int c = tid; c < 128 * 6; c += kTcThreads) {
+      const int r = c / 6, qb = (c % 6) * 8;
+      const int64_t m = row0 + r;
+      float v[8];
+      if (m < M) {
+        const int64_t rr = ray[m];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int qq = qb + i;
+          v[i] = qq < a.c0 ? k0[m * a.c0 + qq]
+                 : qq < a.din ? pe[rr * pe_stride + (qq - a.c0)]
+                 : qq == a.din ? 1.f : 0.f;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = 0.f;
+      }
+      uint4 pk;
+      pk.x = tc::pack_bf16(v[0], v[1]);
+      pk.y = tc::pack_bf16(v[2], v[3]);
+      pk.z = tc::pack_bf16(v[4], v[5]);
+      pk.w = tc::pack_bf16(v[6], v[7]);
+      *reinterpret_cast<uint4*>(sm + kBX + tc::kmaj(r, qb, 48)) = pk;
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX, 128, 768),
+                   tc::make_desc(sb + kBW0k, 128, 256), id_r128, 0);
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    // ---- H0 = relu(Z0 + hpe[ray])
+    {
+      const int64_t m = row0 + row;
+      const bool valid = m < M;
+      const float* hp = hpe + int64_t(valid ? ray[m] : 0) * kW + 64 * half;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float v[16];
+        tc::tmem_ld16(t_lane + kTA + uint32_t(64 * half + 16 * j), v);
+#pragma unroll
+        for (int i = 0; i < 16; i += 4) {
+          const float4 h4 = valid ? __ldg(reinterpret_cast<const float4*>(hp + 16 * j + i))
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[i] = fmaxf(v[i] + h4.x, 0.f);
+          v[i + 1] = fmaxf(v[i + 1] + h4.y, 0.f);
+          v[i + 2] = fmaxf(v[i + 2] + h4.z, 0.f);
+          v[i + 3] = fmaxf(v[i + 3] + h4.w, 0.f);
+        }
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int o = 8 * c;
+          uint4 pk;
+          pk.x = tc::pack_bf16(v[o], v[o + 1]);
+          pk.y = tc::pack_bf16(v[o + 2], v[o + 3]);
+          pk.z = tc::pack_bf16(v[o + 4], v[o + 5]);
+          pk.w = tc::pack_bf16(v[o + 6], v[o + 7]);
+          *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(row, 64 * half + 16 * j + o, 144)) = pk;
+        }
+      }
+    }
+    tc::fence_before();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTB, tc::make_desc(sb + kBH0 + 256 * s, 128, 2304),
+                     tc::make_desc(sb + kBW1 + 256 * s, 128, 2048), id_r128, s > 0);
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    // ---- H1 = relu(Z1 + b1); dl = grad_rgb * y * (1 - y)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float v[16];
+      const int cb = 64 * half + 16 * j;
+      tc::tmem_ld16(t_lane + kTB + uint32_t(cb), v);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int o = 8 * c;
+        uint4 pk;
+        pk.x = tc::pack_bf16(fmaxf(v[o] + b1s[cb + o], 0.f), fmaxf(v[o + 1] + b1s[cb + o + 1], 0.f));
+        pk.y = tc::pack_bf16(fmaxf(v[o + 2] + b1s[cb + o + 2], 0.f), fmaxf(v[o + 3] + b1s[cb + o + 3], 0.f));
+        pk.z = tc::pack_bf16(fmaxf(v[o + 4] + b1s[cb + o + 4], 0.f), fmaxf(v[o + 5] + b1s[cb + o + 5], 0.f));
+        pk.w = tc::pack_bf16(fmaxf(v[o + 6] + b1s[cb + o + 6], 0.f), fmaxf(v[o + 7] + b1s[cb + o + 7], 0.f));
+        *reinterpret_cast<uint4*>(sm + kBH1 + tc::kmaj(row, cb + o, 128)) = pk;
+      }
+    }
+    if (half == 0) {
+      const int64_t m = row0 + row;
+      float d[3] = {0.f, 0.f, 0.f};
+      if (m < M) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float y = rgb[m * 3 + c];
+          d[c] = grad_rgb[m * 3 + c] * (1.f - y) * y;
+          db2[c] += d[c];
+        }
+      }
+      *reinterpret_cast<uint4*>(sm + kBDl + tc::kmaj(row, 0, 16)) =
+          make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
+      *reinterpret_cast<uint4*>(sm + kBDl + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    tc::fence_before();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      // dZ1 (pre-mask) = dl . W2
+      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBDl, 128, 256),
+                   tc::make_desc(sb + kBW2T, 128, 256), id_r128, 0);
+      // dW2 += H1^T . dl  (A: H1 MN-major, B: dl MN-major; K = rows)
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTW2, tc::make_desc(sb + kBH1 + 4096 * s, 2048, 128),
+                     tc::make_desc(sb + kBDl + 512 * s, 256, 128), id_w2, (!first || s > 0));
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    // ---- dZ1 = (dl . W2) * [H1 > 0]
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float v[16];
+      const int cb = 64 * half + 16 * j;
+      tc::tmem_ld16(t_lane + kTA + uint32_t(cb), v);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const uint32_t off = tc::kmaj(row, cb + 8 * c, 128);
+        const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH1 + off);
+        *reinterpret_cast<uint4*>(sm + kBdZ1 + off) = mask_pack(v + 8 * c, h);
+      }
+    }
+    tc::fence_before();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      // dH0 = dZ1 . W1
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTB, tc::make_desc(sb + kBdZ1 + 256 * s, 128, 2048),
+                     tc::make_desc(sb + kBW1T + 256 * s, 128, 2048), id_r128, s > 0);
+      // dW1|db1 += dZ1^T . [H0 | 1]
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTW1, tc::make_desc(sb + kBdZ1 + 4096 * s, 2048, 128),
+                     tc::make_desc(sb + kBH0 + 4608 * s, 2304, 128), id_w1, (!first || s > 0));
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    // ---- dZ0 = dH0 * [H0 > 0]
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float v[16];
+      const int cb = 64 * half + 16 * j;
+      tc::tmem_ld16(t_lane + kTB + uint32_t(cb), v);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH0 + tc::kmaj(row, cb + 8 * c, 144));
+        *reinterpret_cast<uint4*>(sm + kBdZ0 + tc::kmaj(row, cb + 8 * c, 128)) = mask_pack(v + 8 * c, h);
+      }
+    }
+    tc::fence_before();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      // grad k0 = dZ0 . W0k
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTG, tc::make_desc(sb + kBdZ0 + 256 * s, 128, 2048),
+                     tc::make_desc(sb + kBW0T + 256 * s, 128, 2048), id_r16, s > 0);
+      // dW0|db0 += dZ0^T . X
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem + kTW0, tc::make_desc(sb + kBdZ0 + 4096 * s, 2048, 128),
+                     tc::make_desc(sb + kBX + 1536 * s, 768, 128), id_w0, (!first || s > 0));
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    if (half == 0) {
+      float v[16];
+      tc::tmem_ld16(t_lane + kTG, v);
+      const int64_t m = row0 + row;
+      if (m < M) {
+#pragma unroll
+        for (int qq = 0; qq < 16; ++qq)
+          if (qq < a.c0) grad_k0[m * a.c0 + qq] = v[qq];
+      }
+    }
+    first = false;
+    tc::fence_before();
+    __syncthreads();
+  }
+  if (!ok) {
+    tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
+    __syncthreads();
+    for (int64_t i = tid; i < P; i += kTcThreads) pw0[i] = 0.f;
+  } else {
+    tc::fence_after();
+    // partial gradients of this CTA: thread (q4, lane) holds row n = 32*q4 + lane
+    const int n = row;
+    if (half == 0) {
+      float v[16];
+      tc::tmem_ld16(t_lane + kTW2, v);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pw2[c * kW + n] = v[c];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {  // dW0|db0 columns 0..31
+        tc::tmem_ld16(t_lane + kTW0 + 16 * j, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int qq = 16 * j + i;
+          if (qq < a.din) pw0[n * a.din + qq] = v[i];
+          else if (qq == a.din) pb0[n] = v[i];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {  // dW1 columns 0..63
+        tc::tmem_ld16(t_lane + kTW1 + 16 * j, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) pw1[n * kW + 16 * j + i] = v[i];
+      }
+      tc::tmem_ld16(t_lane + kTW1 + 128, v);  // db1
+      pb1[n] = v[0];
+    } else {
+      float v[16];
+      tc::tmem_ld16(t_lane + kTW0 + 32, v);  // dW0|db0 columns 32..47
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int qq = 32 + i;
+        if (qq < a.din) pw0[n * a.din + qq] = v[i];
+        else if (qq == a.din) pb0[n] = v[i];
+      }
+#pragma unroll
+      for (int j = 4; j < 8; ++j) {  // dW1 columns 64..127
+        tc::tmem_ld16(t_lane + kTW1 + 16 * j, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) pw1[n * kW + 16 * j + i] = v[i];
+      }
+    }
+    // db2: fixed-order block sum of the per-row partials (X tile as scratch)
+    float* red = reinterpret_cast<float*>(sm + kBX);
+    __syncthreads();
+    if (half == 0)
+      for (int c = 0; c < 3; ++c) red[c * 128 + row] = db2[c];
+    __syncthreads();
+    if (tid < 3) {
+      float acc = 0.f;
+      for (int i = 0; i < 128; ++i) acc += red[tid * 128 + i];
+      pb2[tid] = acc;
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemBwdCols);
+}
+
 }  // namespace
 
 // Packs the weights and runs the forward over rows k0rows [M, c0] (M = totals[1]).
@@ -258,16 +689,40 @@ int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const
                         int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
                         cudaStream_t st) {
   if (c0 > 16) return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 channels");
-  int rc = dev_reserve(blob, blob_cap, kPackFwdBytes);
+  int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
   if (rc) return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
-  k_pack_fwd<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob));
-  PVDB_CHECK_LAUNCH("k_pack_fwd");
+  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 0);
+  PVDB_CHECK_LAUNCH("k_pack");
   PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(kSmFwdBytes)));
   k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
       a, static_cast<const uint8_t*>(*blob), k0rows, ray, hpe, totals, out, out_logits, err);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_tc");
+  return PVDB_OK;
+}
+
+// Weight and k0 gradients of the rows k0rows [M, c0] (M = totals[1]); per-CTA
+// partials go to wpart (num_sms() x P floats), the caller sums them.
+int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
+                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
+                         const int32_t* ray, const float* hpe, const float* pe, int pe_stride,
+                         const uint32_t* totals, const float* rgb, const float* grad_rgb,
+                         float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
+                         uint32_t* err, cudaStream_t st) {
+  if (c0 > 16 || c0 + dpe + 1 > 48)
+    return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
+  int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
+  if (rc) return rc;
+  MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
+  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 1);
+  PVDB_CHECK_LAUNCH("k_pack");
+  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kSmBwdBytes)));
+  k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob), k0rows,
+                                                      ray, hpe, pe, pe_stride, totals, rgb, grad_rgb,
+                                                      grad_k0, wpart, err);
+  PVDB_CHECK_LAUNCH("k_mlp_bwd_tc");
   return PVDB_OK;
 }
 

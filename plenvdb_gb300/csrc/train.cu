@@ -21,7 +21,8 @@ struct MlpArgs {
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
                      const float* viewdirs, float* rgb, int precision, cudaStream_t st);
 int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
-                      const float* grad_rgb, float* grad_k0, float* grad_flat, cudaStream_t st);
+                      const float* grad_rgb, float* grad_k0, float* grad_flat, int precision,
+                      cudaStream_t st);
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st);
@@ -176,7 +177,8 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, loss_out);
   PVDB_CHECK_LAUNCH("k_loss_sum");
   prof_mark(st, 4);
-  rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads, st);
+  rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads,
+                         cfg->precision, st);
   if (rc) return rc;
   prof_mark(st, 5);
   rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);

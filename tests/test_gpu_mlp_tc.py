@@ -105,3 +105,113 @@ def test_render_bf16_close_to_fp32(lib):
     d = np.abs(imgs[0] - imgs[1])
     assert d.max() < 2e-2 and d.mean() < 1e-3, (d.max(), d.mean())
     assert np.abs(imgs[0] - 1.0).max() > 0.1  # the scene is visible
+
+
+@pytest.mark.parametrize("seed", [3, 7])
+def test_tc_backward_matches_fp64(rows, seed):
+    """Gradients of both rgbnet paths against FP64 autograd, for a loss-like
+    upstream gradient (MSE towards a constant colour, so the per-row terms of
+    a weight gradient do not cancel). Norm-relative bounds: FP32 1e-4; BF16
+    weights 1e-2. BF16 k0 gradients 1e-1: a row's k0 gradient sums 128 hidden
+    units, and BF16 rounding of the forward flips the ReLU of a unit whose
+    pre-activation is within rounding of zero, which moves that row by about
+    1/sqrt(128); the BF16 backward is the exact gradient of the BF16 forward
+    (checked tightly against an emulation below)."""
+    import torch
+    from plenvdb_gb300.march import RgbNetFn
+    from plenvdb_gb300.scene import rgbnet_init
+    ws, k0, rid, vd, _ = rows
+    params = [t.cuda() for t in rgbnet_init(seed=seed)]
+    k0s = (k0 * 10).detach().contiguous()
+    M = k0s.shape[0]
+    with torch.no_grad():
+        y64 = _torch_rgb(k0s, rid, vd, params)
+    G = ((y64 - 0.3) * (2.0 / M)).float()
+    ref_in = [k0s.double().requires_grad_()] + [p.double().requires_grad_() for p in params]
+    (_torch_rgb(ref_in[0], rid, vd, ref_in[1:]) * G.double()).sum().backward()
+    ref = [t.grad for t in ref_in]
+    names = ["k0", "w0", "b0", "w1", "b1", "w2", "b2"]
+    for prec in (0, 1):
+        ins = [k0s.clone().requires_grad_()] + [p.clone().requires_grad_() for p in params]
+        rgb = RgbNetFn.apply(ins[0], vd, ws, 4, prec, *ins[1:])
+        (rgb * G).sum().backward()
+        ws.totals()  # raises on a tensor-core timeout flag
+        msgs = []
+        for name, t, r in zip(names, ins, ref):
+            nrel = ((t.grad.double() - r).norm() / r.norm()).item()
+            tol = 1e-4 if prec == 0 else (1e-1 if name == "k0" else 1e-2)
+            msgs.append((prec, name, nrel, tol))
+        print(msgs)
+        assert all(nrel <= tol for _, _, nrel, tol in msgs), msgs
+
+
+def test_tc_backward_deterministic(rows):
+    import torch
+    from plenvdb_gb300.march import RgbNetFn
+    from plenvdb_gb300.scene import rgbnet_init
+    ws, k0, rid, vd, _ = rows
+    params = [t.cuda() for t in rgbnet_init(seed=1)]
+    G = torch.full((k0.shape[0], 3), 1e-3, device="cuda")
+    out = []
+    for _ in range(2):
+        ins = [k0.detach().clone().requires_grad_()] + [p.clone().requires_grad_() for p in params]
+        (RgbNetFn.apply(ins[0], vd, ws, 4, 1, *ins[1:]) * G).sum().backward()
+        out.append([t.grad.clone() for t in ins])
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
+
+
+def _bf(x):
+    import torch
+    return x.to(torch.bfloat16).double()
+
+
+def _emulated_bf16_backward(k0, rid, vd, params, y, G):
+    """FP64 restatement of the tensor-core backward with BF16 rounding at the
+    same points as the kernel: operands rounded, sums exact."""
+    import torch
+    w0, b0, w1, b1, w2, b2 = [t.double() for t in params]
+    c0 = k0.shape[1]
+    v = vd.double()
+    freq = torch.tensor([1.0, 2.0, 4.0, 8.0], dtype=torch.float64, device="cuda")
+    emb = (v.unsqueeze(-1) * freq).flatten(-2)
+    pe = torch.cat([v, emb.sin(), emb.cos()], -1)
+    hpe = (pe @ w0[:, c0:].T + b0)[rid.long()]
+    pe = pe[rid.long()]
+    x = _bf(k0)
+    h0 = _bf(torch.relu(x @ _bf(w0[:, :c0]).T + hpe))
+    h1 = _bf(torch.relu(h0 @ _bf(w1).T + b1))
+    dl32 = G.double() * (1 - y.double()) * y.double()
+    dl = _bf(dl32)
+    dz1 = _bf((dl @ _bf(w2)) * (h1 > 0))
+    dz0 = _bf((dz1 @ _bf(w1)) * (h0 > 0))
+    gk0 = dz0 @ _bf(w0[:, :c0])
+    xin = torch.cat([x, _bf(pe)], -1)
+    return [gk0, dz0.T @ xin, dz0.sum(0), dz1.T @ h0, dz1.sum(0), dl.T @ h1, dl32.sum(0)]
+
+
+def test_tc_backward_matches_emulated_bf16(rows):
+    import torch
+    from plenvdb_gb300.march import RgbNetFn
+    from plenvdb_gb300.scene import rgbnet_init
+    ws, k0, rid, vd, _ = rows
+    params = [t.cuda() for t in rgbnet_init(seed=3)]
+    g = torch.Generator(device="cuda").manual_seed(11)
+    k0s = (k0 * 10).detach().contiguous()
+    G = torch.randn(k0s.shape[0], 3, device="cuda", generator=g) * 1e-3
+    ins = [k0s.clone().requires_grad_()] + [p.clone().requires_grad_() for p in params]
+    rgb = RgbNetFn.apply(ins[0], vd, ws, 4, 1, *ins[1:])
+    (rgb * G).sum().backward()
+    ws.totals()
+    ref = _emulated_bf16_backward(k0s, rid, vd, params, rgb.detach(), G)
+    names = ["k0", "w0", "b0", "w1", "b1", "w2", "b2"]
+    msgs, bad = [], []
+    for name, t, r in zip(names, ins, ref):
+        scale = r.abs().max().item()
+        err = (t.grad.double() - r).abs().max().item()
+        nrel = ((t.grad.double() - r).norm() / r.norm()).item()
+        msgs.append(f"{name}: maxerr/scale={err / scale:.2e} norm-rel={nrel:.2e}")
+        if err > 2e-3 * scale:
+            bad.append(name)
+    print("\n".join(msgs))
+    assert not bad, msgs

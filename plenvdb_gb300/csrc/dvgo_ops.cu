@@ -58,7 +58,9 @@ __global__ void k_a2w(const float* __restrict__ alpha, int n_rays, float* w, flo
     T[i] = Tc;
     w[i] = Tc * alpha[i];
     Tc = trans_step(Tc, alpha[i]);
-    if ((double)Tc < 1e-3) {
+    // Tc < 1e-3 (a double literal): no float lies in [1e-3, 1e-3f), so the
+    // FP32 compare against 1e-3f is the same test
+    if (Tc < 1e-3f) {
       ++i;
       break;
     }

@@ -13,8 +13,9 @@
 // k_march_gather compacts the colour samples (weight > thres, dvgo.py:329-335)
 // into dense rows and samples the k0 grid there (colorvdb.cu:81-111).
 //
-// Backward (k_march_bwd) recomputes transmittance from the saved alphas,
-// runs alpha2weight_backward (:653-677) and raw2alpha_backward (:506-517),
+// Backward (k_march_bwd) recovers transmittance from the saved alphas and
+// weights, runs alpha2weight_backward (:653-677) as a suffix scan and
+// raw2alpha_backward (:506-517),
 // and emits the 8 corner keys of every kept sample; a stable radix sort by
 // voxel slot and a sequential per-slot sum (reduce.cuh) then add the density
 // and k0 gradients deterministically.
@@ -215,75 +216,53 @@ __global__ void __launch_bounds__(kMarchThreads)
   }
 }
 
-// Backward of the composite chain for one ray. Shared memory holds the
-// transmittance at the start of each 32-sample chunk (pass 1); pass 2 walks
-// the chunks backwards, recomputing T within the chunk forwards and then the
-// reverse accumulation of alpha2weight_backward.
+// Backward of the composite chain for one ray (warp per ray), chunks of 32
+// kept samples from the last to the first. The transmittance before sample i
+// is recovered from the saved forward weight, T_i = w_i / alpha_i (alpha_i >
+// fast_color_thres > 0), so no per-sample transmittance is stored and no
+// serial pass is needed. back_i = grad_last*T_last + sum_{j>i} gw_j*w_j
+// (alpha2weight_backward, render_utils_kernel.cu:665-673) is an exclusive
+// suffix sum: a warp shuffle scan inside the chunk plus the carry of the later
+// chunks.
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_bwd(GridView gd, int R, MarchP P, MarchW W, const float* __restrict__ grad_w,
-                const float* __restrict__ grad_last, uint32_t* keys, int max_chunks) {
-  extern __shared__ float chunkT_all[];
+                const float* __restrict__ grad_last, uint32_t* keys) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
-  float* chunkT = chunkT_all + warp * max_chunks;
   const int nk = int(W.n_kept[r]);
   if (nk == 0) return;
   const int64_t sbase = int64_t(r) * P.cap;
   const int64_t kb = W.kept_off[r];
   const int nchunks = (nk + 31) >> 5;
-  // pass 1: chunk-start transmittance
-  {
-    float T = 1.f;
-    for (int c = 0; c < nchunks; ++c) {
-      const int i = c * 32 + lane;
-      const float a = i < nk ? W.k_alpha[sbase + i] : 0.f;
-      if (lane == 0) chunkT[c] = T;
-      const int nv = min(32, nk - c * 32);
-      for (int l = 0; l < nv; ++l) T = trans_step(T, __shfl_sync(0xffffffffu, a, l));
-    }
-  }
-  __syncwarp();
   RaySetup rs;
   load_setup(W, r, rs);
-  float back = (grad_last ? grad_last[r] : 0.f) * W.T_last[r];
+  float carry = (grad_last ? grad_last[r] : 0.f) * W.T_last[r];
   for (int c = nchunks - 1; c >= 0; --c) {
     const int i = c * 32 + lane;
     const bool valid = i < nk;
-    const int nv = min(32, nk - c * 32);
-    float a = 0.f, gw = 0.f;
+    float a = 1.f, w = 0.f, gw = 0.f;
     int32_t st = 0, row = -1;
     if (valid) {
       a = W.k_alpha[sbase + i];
+      w = W.k_w[sbase + i];
       st = W.k_step[sbase + i];
       row = W.k_row[sbase + i];
       if (row >= 0 && grad_w) gw = grad_w[row];
     }
-    // T_i and w_i within the chunk
-    float Ti = 0.f, wi = 0.f;
-    {
-      float T = chunkT[c];
-      for (int l = 0; l < nv; ++l) {
-        const float al = __shfl_sync(0xffffffffu, a, l);
-        if (lane == l) {
-          Ti = T;
-          wi = T * al;
-        }
-        T = trans_step(T, al);
-      }
+    // inclusive suffix sum of gw*w over lanes >= lane
+    const float term = __fmul_rn(gw, w);
+    float suf = term;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float v = __shfl_down_sync(0xffffffffu, suf, o);
+      if (lane + o < 32) suf += v;
     }
-    // reverse accumulation (render_utils_kernel.cu:669-673)
-    float ga = 0.f;
-    for (int l = nv - 1; l >= 0; --l) {
-      const float gwl = __shfl_sync(0xffffffffu, gw, l);
-      const float Tl = __shfl_sync(0xffffffffu, Ti, l);
-      const float al = __shfl_sync(0xffffffffu, a, l);
-      const float wl = __shfl_sync(0xffffffffu, wi, l);
-      const float g = alpha_grad(gwl, Tl, back, al);
-      if (lane == l) ga = g;
-      back = __fmaf_rn(gwl, wl, back);
-    }
+    const float back = carry + (suf - term);
+    carry += __shfl_sync(0xffffffffu, suf, 0);
     if (valid) {
+      const float Ti = __fdiv_rn(w, a);
+      const float ga = alpha_grad(gw, Ti, back, a);
       const int32_t k = st & 0x7fffffff;
       float p[3], idx[3];
       ray_point(rs, P.stepdist, k, p);
@@ -476,11 +455,9 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   const int64_t nmax = m->slots * 8;
   int rc = scratch_reserve(m->red, nmax);
   if (rc) return rc;
-  const int max_chunks = (m->cap + 31) / 32;
-  const size_t smem = size_t(kMarchWarps) * max_chunks * 4;
   const int nb = ceil_div(R, kMarchWarps);
-  k_march_bwd<<<nb, kMarchThreads, smem, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
-                                               m->red.keys[0], max_chunks);
+  k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
+                                            m->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
   int buf = 0;

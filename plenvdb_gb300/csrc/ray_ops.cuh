@@ -42,8 +42,7 @@ __device__ __forceinline__ void ray_setup(const float o[3], const float d[3], co
   const float rn = ray_norm(d[0], d[1], d[2]);
   // n_samples = max(ceil((t_max-t_min)*|d|/stepdist), 1.)  (:52)
   const float q = __fdiv_rn(__fmul_rn(r.t_max - r.t_min, rn), stepdist);
-  const double ns = fmax((double)ceilf(q), 1.0);
-  r.n_steps = (int64_t)ns;
+  r.n_steps = (int64_t)fmaxf(ceilf(q), 1.f);
   for (int a = 0; a < 3; ++a) {
     r.start[a] = __fmaf_rn(d[a], r.t_min, o[a]);  // (:71-73)
     r.dir[a] = __fdiv_rn(d[a], rn);               // (:74-76)
@@ -88,21 +87,26 @@ __device__ __forceinline__ float raw2alpha(float sigma, float shift, float inter
   return 1.f - powf(1.f + e, -interval);
 }
 
-// raw2alpha_backward (:514): min(e,1e10) is a double, so the product is formed in
-// double and rounded once.
+// raw2alpha_backward (:514): min(e,1e10) * (1+e)^(-interval-1) * interval * g.
+// The reference forms the product in double (min() of a double literal); here
+// it is three FP32 products, within a few ulps of that.
 __device__ __forceinline__ float raw2alpha_grad(float e, float interval, float g) {
-  const double a = fmin((double)e, 1e10);
-  return (float)(a * (double)powf(1.f + e, -interval - 1.f) * (double)interval * (double)g);
+  return __fmul_rn(__fmul_rn(__fmul_rn(fminf(e, 1e10f), powf(1.f + e, -interval - 1.f)), interval), g);
 }
 
-// T_cum *= (1. - alpha) with the double literal (:593): exact product, one rounding.
+// T_cum *= (1. - alpha) (:593). The reference promotes to double because of
+// the literal: it rounds the exact product T*(1-alpha) to double, then to
+// float. One fmaf rounds the same exact product T - T*alpha straight to
+// float; the two agree except when the double rounding lands on a float tie
+// (about one step in 2^29), and no FP64 unit is used.
 __device__ __forceinline__ float trans_step(float T, float alpha) {
-  return (float)((double)T * (1.0 - (double)alpha));
+  return __fmaf_rn(-T, alpha, T);
 }
 
-// grad = gw*T - back_cum / (1-alpha + 1e-10) (:671): (1-alpha) in float, the rest in double.
+// grad = gw*T - back_cum / (1-alpha + 1e-10) (:671), in FP32 (the reference
+// adds the double literal and divides in double).
 __device__ __forceinline__ float alpha_grad(float gw, float T, float back_cum, float alpha) {
-  return (float)((double)(gw * T) - (double)back_cum / ((double)(1.f - alpha) + 1e-10));
+  return __fmul_rn(gw, T) - __fdiv_rn(back_cum, (1.f - alpha) + 1e-10f);
 }
 
 }  // namespace pvdb

@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--render-frames", type=int, default=20)
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the fused step eagerly instead of replaying a CUDA graph")
     return ap.parse_args()
 
 
@@ -160,6 +162,7 @@ def run_ours(args):
     lib = L.load()
     scfg, cfg, cam, ro, rd, vd, tgt = make_problem(device_seed=rank)
     cfg.precision = 1 if args.precision == "bf16" else 0
+    cfg.use_graph = not args.no_graph
     dg, kg = build_grids(scfg)
     tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), cfg, max_rays=RAYS)
     nb = ro.shape[0] // RAYS
@@ -175,7 +178,6 @@ def run_ours(args):
            for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
-    L.call("pvdb_profile_begin", args.steps)
     launches0 = lib.pvdb_launch_count()
     if ws_ > 1:
         dist.barrier()
@@ -189,9 +191,6 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     launches = lib.pvdb_launch_count() - launches0
-    marks = (__import__("ctypes").c_float * 16)()
-    ncalls = __import__("ctypes").c_int32()
-    L.call("pvdb_profile_end", marks, 16, __import__("ctypes").byref(ncalls))
     clk = clocks.stop()
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
     if ws_ > 1:
@@ -200,10 +199,7 @@ def run_ours(args):
         step_ms = float(t.item())
     ms_per_step = step_ms / args.steps
     value = ws_ * args.steps / (step_ms / 1e3)
-    stage_names = {1: "march_fwd", 2: "k0_gather", 3: "rgbnet_fwd", 4: "composite_loss",
-                   5: "rgbnet_bwd", 6: "march_bwd", 7: "radix_sort", 8: "segment_reduce",
-                   9: "tv", 10: "voxel_adam", 11: "rgbnet_adam"}
-    stage_ms = {stage_names[i]: marks[i] / max(1, ncalls.value) for i in stage_names}
+    stage_ms = stage_profile(tr, dev, nb, flush, args)
     # ---------------- end to end through the public API with host buffers
     e2e = run_e2e(tr, ro, rd, vd, tgt, args, flush)
     # ---------------- roofline of the dominant stage
@@ -224,7 +220,8 @@ def run_ours(args):
                                    f"{args.precision}",
                        "rays": RAYS, "reso": RESO, "l2": "512 MB buffer written between "
                                                          "timed steps, outside the step events",
-                       "parallelism": "replicas" if ws_ > 1 else "single GPU"},
+                       "parallelism": "replicas" if ws_ > 1 else "single GPU",
+                       "launch": "eager" if args.no_graph else "CUDA graph replay of the fused step"},
             "wall_s": t_wall, "clocks": clk, "gpu_launches": int(launches),
             "stage_ms": stage_ms, "roofline": roof, "e2e": e2e,
         }
@@ -236,6 +233,31 @@ def run_ours(args):
     if ws_ > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def stage_profile(tr, dev, nb, flush, args):
+    """Per-stage device time from events between the stages of eagerly launched
+    steps (a graph replay has no stage boundaries); a separate, shorter pass
+    after the timed region."""
+    import ctypes
+    import torch
+    from plenvdb_gb300 import _lib as L
+    n = max(5, min(args.steps, 20))
+    use_graph = tr.tc.use_graph
+    tr.tc.use_graph = 0
+    L.call("pvdb_profile_begin", n)
+    for i in range(n):
+        flush_l2(flush)
+        tr.step(*dev[i % nb])
+    torch.cuda.synchronize()
+    marks = (ctypes.c_float * 16)()
+    ncalls = ctypes.c_int32()
+    L.call("pvdb_profile_end", marks, 16, ctypes.byref(ncalls))
+    tr.tc.use_graph = use_graph
+    stage_names = {1: "march_fwd", 2: "k0_gather", 3: "rgbnet_fwd", 4: "composite_loss",
+                   5: "rgbnet_bwd", 6: "march_bwd", 7: "radix_sort", 8: "segment_reduce",
+                   9: "tv", 10: "voxel_adam", 11: "rgbnet_adam"}
+    return {stage_names[i]: marks[i] / max(1, ncalls.value) for i in stage_names}
 
 
 def run_e2e(tr, ro, rd, vd, tgt, args, flush):

@@ -402,6 +402,7 @@ typedef struct pvdb_train_config {
   float lr_decay_factor;                 /* applied after the step (run.py:592-598) */
   float rgbnet_lr, rgbnet_beta1, rgbnet_beta2, rgbnet_eps;
   int32_t precision;                     /* 0 FP32, 1 BF16 rgbnet */
+  int32_t use_graph;                     /* 1: replay the step as a captured CUDA graph */
 } pvdb_train_config;
 
 typedef struct pvdb_rgbnet_state {

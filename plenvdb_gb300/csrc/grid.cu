@@ -190,29 +190,56 @@ __device__ __forceinline__ float value_c(const GridView& g, int i, int j, int k,
   return s < 0 ? g.background : g.data[int64_t(s) * g.C + ch];
 }
 
-// TV gradient (total_variation_kernel.cu:13-35) on the leaf store. One thread per
-// (slot, channel); neighbours inside [0,reso) only; values through the leaf table.
-__global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode) {
-  int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (t >= int64_t(g.nleaf) * kLeafVox * g.C) return;
-  const int64_t n = t / g.C;
-  const int ch = int(t % g.C);
-  const int leaf = int(n >> 9), vox = int(n & 511);
-  if (!is_active(g, leaf, vox)) return;
-  const float gcur = g.grad[t];
-  if (!dense_mode && gcur == 0.f) return;
-  int x, y, z;
-  slot_coord(g, leaf, vox, x, y, z);
-  if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) return;
-  const float p = g.data[t];
-  float add = 0.f;
-  add += (z == 0 ? 0.f : wz * tv_clamp(p - value_c(g, x, y, z - 1, ch)));
-  add += (z == g.reso[2] - 1 ? 0.f : wz * tv_clamp(p - value_c(g, x, y, z + 1, ch)));
-  add += (y == 0 ? 0.f : wy * tv_clamp(p - value_c(g, x, y - 1, z, ch)));
-  add += (y == g.reso[1] - 1 ? 0.f : wy * tv_clamp(p - value_c(g, x, y + 1, z, ch)));
-  add += (x == 0 ? 0.f : wx * tv_clamp(p - value_c(g, x - 1, y, z, ch)));
-  add += (x == g.reso[0] - 1 ? 0.f : wx * tv_clamp(p - value_c(g, x + 1, y, z, ch)));
-  g.grad[t] = gcur + add;
+// TV gradient (total_variation_kernel.cu:13-35) on the leaf store, for the
+// voxels of the listed leaves (list = NULL: all leaves). One thread per voxel:
+// the six neighbour slots are looked up once and shared by the channels;
+// neighbours inside [0,reso) only, values through the leaf table (background
+// outside allocated leaves). Per channel the sum is formed in the reference's
+// order z-, z+, y-, y+, x-, x+.
+__global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
+                     const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+  const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list ? list[i >> 9] : int(i >> 9);
+    const int vox = int(i & 511);
+    if (!is_active(g, leaf, vox)) continue;
+    int x, y, z;
+    slot_coord(g, leaf, vox, x, y, z);
+    if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) continue;
+    // neighbour slots; -2 = outside [0,reso) (no term), -1 = no leaf (background)
+    int nb[6];
+    nb[0] = z == 0 ? -2 : slot_of(g, x, y, z - 1);
+    nb[1] = z == g.reso[2] - 1 ? -2 : slot_of(g, x, y, z + 1);
+    nb[2] = y == 0 ? -2 : slot_of(g, x, y - 1, z);
+    nb[3] = y == g.reso[1] - 1 ? -2 : slot_of(g, x, y + 1, z);
+    nb[4] = x == 0 ? -2 : slot_of(g, x - 1, y, z);
+    nb[5] = x == g.reso[0] - 1 ? -2 : slot_of(g, x + 1, y, z);
+    const float wt[6] = {wz, wz, wy, wy, wx, wx};
+    const int64_t t0 = (int64_t(leaf) * kLeafVox + vox) * g.C;
+    for (int ch = 0; ch < g.C; ++ch) {
+      const float gcur = g.grad[t0 + ch];
+      if (!dense_mode && gcur == 0.f) continue;
+      const float p = g.data[t0 + ch];
+      float add = 0.f;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (nb[q] == -2) {
+          add += 0.f;
+        } else {
+          const float vn = nb[q] < 0 ? g.background : g.data[int64_t(nb[q]) * g.C + ch];
+          add += wt[q] * tv_clamp(p - vn);
+        }
+      }
+      g.grad[t0 + ch] = gcur + add;
+    }
+  }
+}
+
+__global__ void k_touched_compact(const uint8_t* __restrict__ touched, int nleaf, int32_t* list,
+                                  uint32_t* count) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l < nleaf && touched[l]) list[atomicAdd(count, 1u)] = l;
 }
 
 // ---------------------------------------------------------------- helpers
@@ -270,7 +297,9 @@ static int build_grid(const int reso[3], int C, float bg,
       (rc = dev_alloc((void**)&g->d_mask, std::max<size_t>(1, g->h_mask.size()) * 8)) ||
       (rc = dev_alloc((void**)&g->d_data, std::max<size_t>(1, nval) * 4)) ||
       (rc = dev_alloc((void**)&g->d_grad, std::max<size_t>(1, nval) * 4)) ||
-      (rc = dev_alloc((void**)&g->d_touched, std::max(1, g->nleaf)))) {
+      (rc = dev_alloc((void**)&g->d_touched, std::max(1, g->nleaf))) ||
+      (rc = dev_alloc((void**)&g->d_tlist, std::max<size_t>(1, g->nleaf) * 4)) ||
+      (rc = dev_alloc((void**)&g->d_tcount, 16))) {
     pvdb_grid_destroy(g);
     return rc;
   }
@@ -300,6 +329,18 @@ static int build_grid(const int reso[3], int C, float bg,
 // Host staging: copy `n` host bytes into the grid's device stage at `offset`.
 static int stage_reserve(pvdb_grid_s* g, size_t bytes) {
   return dev_reserve(&g->d_stage, &g->stage_cap, bytes);
+}
+
+int touched_list(pvdb_grid_s* g, cudaStream_t st) {
+  if (g->tlist_valid) return PVDB_OK;
+  PVDB_CHECK_CUDA(cudaMemsetAsync(g->d_tcount, 0, 4, st));
+  if (g->nleaf) {
+    k_touched_compact<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf, g->d_tlist,
+                                                              g->d_tcount);
+    PVDB_CHECK_LAUNCH("k_touched_compact");
+  }
+  g->tlist_valid = true;
+  return PVDB_OK;
 }
 
 }  // namespace pvdb
@@ -426,6 +467,8 @@ int pvdb_grid_destroy(pvdb_grid g) {
   dev_free(g->d_data);
   dev_free(g->d_grad);
   dev_free(g->d_touched);
+  dev_free(g->d_tlist);
+  dev_free(g->d_tcount);
   dev_free(g->d_stage);
   free_scratch(g->red);
   delete g;
@@ -605,13 +648,21 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
   wy /= 6.f;
   wz /= 6.f;
   if (mimic_axis_bug) wx = wz;
-  const int64_t nt = g->nslots() * g->C;
-  if (nt)
-    k_tv<<<ceil_div(nt, 256), 256, 0, as_stream(s)>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0);
+  cudaStream_t st = as_stream(s);
+  if (g->nslots() == 0) return PVDB_OK;
+  // without dense mode only voxels with a nonzero gradient change: the touched leaves
+  const bool use_list = !dense_mode && !g->all_touched;
+  if (use_list) {
+    int rc = touched_list(g, st);
+    if (rc) return rc;
+  }
+  k_tv<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
+                                      use_list ? g->d_tlist : nullptr, g->d_tcount);
   PVDB_CHECK_LAUNCH("k_tv");
   if (dense_mode) g->all_touched = true;
   return PVDB_OK;
 }
+
 
 int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
   clear_error();
@@ -626,6 +677,7 @@ int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
     PVDB_CHECK_LAUNCH("k_clear_touched");
   }
   g->all_touched = false;
+  g->tlist_valid = false;
   return PVDB_OK;
 }
 

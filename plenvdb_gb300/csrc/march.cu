@@ -15,10 +15,10 @@
 //
 // Backward (k_march_bwd) recovers transmittance from the saved alphas and
 // weights, runs alpha2weight_backward (:653-677) as a suffix scan and
-// raw2alpha_backward (:506-517),
-// and emits the 8 corner keys of every kept sample; a stable radix sort by
-// voxel slot and a sequential per-slot sum (reduce.cuh) then add the density
-// and k0 gradients deterministically.
+// raw2alpha_backward (:506-517), and keys every kept sample by its trilinear
+// cell; a stable radix sort by cell, per-cell partial sums and a per-voxel
+// gather over the touched leaves then add the density and k0 gradients
+// deterministically (see the reduction below).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -226,7 +226,9 @@ __global__ void __launch_bounds__(kMarchThreads)
 // chunks.
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_bwd(GridView gd, int R, MarchP P, MarchW W, const float* __restrict__ grad_w,
-                const float* __restrict__ grad_last, uint32_t* keys) {
+                const float* __restrict__ grad_last, const float* __restrict__ grad_k0, int C,
+                uint32_t* keys) {
+  const int nq = (C + 3) >> 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -272,47 +274,213 @@ __global__ void __launch_bounds__(kMarchThreads)
       (void)raw2alpha(sigma, P.shift, P.interval, e);
       const float gs = raw2alpha_grad(e, P.interval, ga);
       const int64_t s = kb + i;
-      W.b_pos[s * 3 + 0] = idx[0];
-      W.b_pos[s * 3 + 1] = idx[1];
-      W.b_pos[s * 3 + 2] = idx[2];
-      W.b_gsig[s] = gs;
-      W.b_row[s] = row;
-      emit_corner_keys(gd, idx[0], idx[1], idx[2], keys, s);
+      float4* rec = W.b_rec + s * (1 + nq);
+      rec[0] = make_float4(idx[0], idx[1], idx[2], gs);
+      for (int b = 0; b < nq; ++b) {
+        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row >= 0 && grad_k0) {
+          const float* gr = grad_k0 + int64_t(row) * C + 4 * b;
+          g4.x = gr[0];
+          g4.y = 4 * b + 1 < C ? gr[1] : 0.f;
+          g4.z = 4 * b + 2 < C ? gr[2] : 0.f;
+          g4.w = 4 * b + 3 < C ? gr[3] : 0.f;
+        }
+        rec[1 + b] = g4;
+      }
+      keys[s] = cell_key(gd.ldim, ifloor(idx[0]), ifloor(idx[1]), ifloor(idx[2]));
     }
   }
 }
 
-// Keys of the k0 grid (when its topology differs from the density grid's).
-__global__ void k_march_keys_k0(GridView gk, MarchW W, uint32_t* keys) {
-  const int64_t n = W.totals[0];
-  for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
-       s += int64_t(gridDim.x) * blockDim.x) {
-    if (W.b_row[s] >= 0) {
-      emit_corner_keys(gk, W.b_pos[s * 3], W.b_pos[s * 3 + 1], W.b_pos[s * 3 + 2], keys, s);
-    } else {
+// Deterministic reduction of the sample gradients into voxel gradients.
+//
+// Each kept sample s sits in the trilinear cell whose low corner is
+// floor(idx); its 8 corners receive w_c * gs (density) and w_c * gk0[row]
+// (k0). The samples are stably radix-sorted by cell key, a leaf-major code of
+// the cell's low corner, so each cell's samples form one segment in ascending
+// sample order, and the first sorted index of each cell goes into a dense cell
+// map. Then, in two passes:
+//   1. per (cell, corner c): the segment's contributions to corner c are summed
+//      in sample order into the cell's partial P[cell][c] (1 + C floats), and
+//      the corner voxel's leaf is flagged as touched;
+//   2. per voxel of the touched leaves: grad += sum over c' = 0..7, in that
+//      order, of P[v - delta(c')][c'] for the cells present in the map.
+// Every sum has an order fixed by the data, so the result is bitwise
+// reproducible without atomics. Corners in no allocated leaf are dropped
+// (densityvdb.cu:23).
+__device__ __forceinline__ void cell_decode(const int ld[3], uint32_t key, int& i, int& j, int& k) {
+  const int leaf = int(key >> 9), off = int(key & 511u);
+  const int lk = leaf % ld[2];
+  const int lj = (leaf / ld[2]) % ld[1];
+  const int li = leaf / (ld[2] * ld[1]);
+  i = (li << 3) | (off >> 6);
+  j = (lj << 3) | ((off >> 3) & 7);
+  k = (lk << 3) | (off & 7);
+}
+
+__device__ __forceinline__ bool seg_head(const uint32_t* __restrict__ skeys, int64_t i) {
+  const uint32_t key = skeys[i];
+  return key != kInvalidKey && (i == 0 || skeys[i - 1] != key);
+}
+
+__global__ void k_cell_map_set(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
+                               int32_t* map, int clear) {
+  const int64_t n = *n_dev;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    if (seg_head(skeys, i)) map[skeys[i]] = clear ? -1 : int32_t(i);
+}
+
+// Corner weight c of the multi-channel formula, ((a*b)*c) (colorvdb.cu:100-107).
+__device__ __forceinline__ float corner_scale(float u, float v, float w, int c) {
+  int di, dj, dk;
+  corner_delta(c, di, dj, dk);
+  const float a = di ? u : 1.f - u, b = dj ? v : 1.f - v, cc = dk ? w : 1.f - w;
+  return __fmul_rn(__fmul_rn(a, b), cc);
+}
+
+// Pass 1: thread per (sorted index j, corner c); segment heads only. NQ = the
+// number of float4 chunks of the k0 gradient (0 = density only).
+template <int NQ>
+__global__ void __launch_bounds__(256)
+    k_cell_partials(GridView gd, GridView gc, const uint32_t* __restrict__ skeys,
+                    const uint32_t* __restrict__ svals, const uint32_t* n_dev,
+                    const float4* __restrict__ rec, float* __restrict__ pd,
+                    float4* __restrict__ pk, uint8_t* touched_d, uint8_t* touched_c) {
+  const int64_t n = *n_dev;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n * 8;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t h = t >> 3;
+    const int c = int(t & 7);
+    if (!seg_head(skeys, h)) continue;
+    const uint32_t key = skeys[h];
+    int ci, cj, ck, di, dj, dk;
+    cell_decode(gd.ldim, key, ci, cj, ck);
+    corner_delta(c, di, dj, dk);
+    const int sd = slot_of(gd, ci + di, cj + dj, ck + dk);
+    const int sc = NQ ? slot_of(gc, ci + di, cj + dj, ck + dk) : -1;
+    if (sd < 0 && sc < 0) continue;
+    float sum_d = 0.f;
+    float4 acc[NQ > 0 ? NQ : 1];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) keys[s * 8 + c] = kInvalidKey;
+    for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t j = h; j < n && skeys[j] == key; ++j) {
+      const float4* r = rec + int64_t(svals[j]) * (1 + NQ);
+      const float4 p = r[0];
+      const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
+                  w = p.z - float(ifloor(p.z));
+      if (p.w != 0.f) sum_d = __fadd_rn(sum_d, density_corner_term(p.w, u, v, w, c));
+      if (NQ) {
+        const float sce = corner_scale(u, v, w, c);
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) {
+          const float4 g = r[1 + b];
+          acc[b].x = __fadd_rn(acc[b].x, __fmul_rn(g.x, sce));
+          acc[b].y = __fadd_rn(acc[b].y, __fmul_rn(g.y, sce));
+          acc[b].z = __fadd_rn(acc[b].z, __fmul_rn(g.z, sce));
+          acc[b].w = __fadd_rn(acc[b].w, __fmul_rn(g.w, sce));
+        }
+      }
+    }
+    const int64_t e = int64_t(key) * 8 + c;
+    pd[e] = sum_d;
+#pragma unroll
+    for (int b = 0; b < NQ; ++b) pk[e * NQ + b] = acc[b];
+    if (sd >= 0) touched_d[sd >> 9] = 1;
+    if (NQ && sc >= 0) touched_c[sc >> 9] = 1;
+  }
+}
+
+// Pass 2: thread per voxel of the listed (touched) leaves of grid g; adds the
+// density partials to grad_d and/or the k0 partials to grad_c (C channels).
+template <int NQ>
+__global__ void __launch_bounds__(256)
+    k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
+                   const int32_t* __restrict__ map, const float* __restrict__ pd,
+                   const float4* __restrict__ pk, float* grad_d, float* grad_c, int C) {
+  const int64_t nv = int64_t(*count) * kLeafVox;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list[i >> 9];
+    const int vox = int(i & 511);
+    const int vi = g.origin[leaf * 3] + (vox >> 6), vj = g.origin[leaf * 3 + 1] + ((vox >> 3) & 7),
+              vk = g.origin[leaf * 3 + 2] + (vox & 7);
+    // the up to 8 cells that have this voxel as corner c, in corner order
+    int64_t ent[8];
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      int di, dj, dk;
+      corner_delta(c, di, dj, dk);
+      const uint32_t key = cell_key(g.ldim, vi - di, vj - dj, vk - dk);
+      ent[c] = (key != kInvalidKey && __ldg(map + key) >= 0) ? int64_t(key) * 8 + c : -1;
+      any = any || ent[c] >= 0;
+    }
+    if (!any) continue;
+    const int64_t slot = int64_t(leaf) * kLeafVox + vox;
+    if (grad_d) {
+      float sum_d = 0.f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (ent[c] >= 0) sum_d = __fadd_rn(sum_d, pd[ent[c]]);
+      grad_d[slot] = __fadd_rn(grad_d[slot], sum_d);
+    }
+    if (NQ && grad_c) {
+      float4 acc[NQ > 0 ? NQ : 1];
+#pragma unroll
+      for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        if (ent[c] < 0) continue;
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) {
+          const float4 q = pk[ent[c] * NQ + b];
+          acc[b].x = __fadd_rn(acc[b].x, q.x);
+          acc[b].y = __fadd_rn(acc[b].y, q.y);
+          acc[b].z = __fadd_rn(acc[b].z, q.z);
+          acc[b].w = __fadd_rn(acc[b].w, q.w);
+        }
+      }
+      float* dst = grad_c + slot * C;
+#pragma unroll
+      for (int b = 0; b < NQ; ++b) {
+        const float a4[4] = {acc[b].x, acc[b].y, acc[b].z, acc[b].w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (4 * b + q < C) dst[4 * b + q] = __fadd_rn(dst[4 * b + q], a4[q]);
+      }
     }
   }
 }
 
-struct MarchSrc {
-  const float* xyz;
-  const float* gsig;
-  const int32_t* row;
-  const float* gk0;
-  int C;
-  __device__ __forceinline__ void pos(int64_t s, float& x, float& y, float& z) const {
-    x = xyz[s * 3];
-    y = xyz[s * 3 + 1];
-    z = xyz[s * 3 + 2];
+template <int NQ>
+static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0,
+                              const uint32_t* skeys, const uint32_t* svals, cudaStream_t st) {
+  const int grid = stride_grid();
+  const GridView gv = density->view();
+  const GridView kv = NQ ? k0->view() : gv;
+  k_cell_partials<NQ><<<grid * 2, 256, 0, st>>>(gv, kv, skeys, svals, m->w.totals + 0, m->w.b_rec,
+                                                m->cell_pd, m->cell_pk, density->d_touched,
+                                                NQ ? k0->d_touched : density->d_touched);
+  PVDB_CHECK_LAUNCH("k_cell_partials");
+  density->tlist_valid = false;
+  if (NQ) k0->tlist_valid = false;
+  int rc = touched_list(density, st);
+  if (rc) return rc;
+  const bool same = NQ && k0->h_table == density->h_table;
+  const int C = NQ ? k0->C : 0;
+  k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_map,
+                                           m->cell_pd, m->cell_pk, density->d_grad,
+                                           same ? k0->d_grad : nullptr, C);
+  PVDB_CHECK_LAUNCH("k_voxel_gather");
+  if (NQ && !same) {
+    if ((rc = touched_list(k0, st))) return rc;
+    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_map,
+                                             m->cell_pd, m->cell_pk, nullptr, k0->d_grad, C);
+    PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
-  __device__ __forceinline__ float gd(int64_t s) const { return gsig ? gsig[s] : 0.f; }
-  __device__ __forceinline__ bool has_c(int64_t s) const { return gk0 && row[s] >= 0; }
-  __device__ __forceinline__ float gc(int64_t s, int ch) const {
-    return gk0[int64_t(row[s]) * C + ch];
-  }
-};
+  return PVDB_OK;
+}
 
 // --------------------------------------------------------------- composite
 __global__ void __launch_bounds__(kMarchThreads)
@@ -401,8 +569,10 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st) {
   if (k0) {
-    for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a) {
       PVDB_REQUIRE(k0->reso[a] == density->reso[a], "k0 and density grids need the same resolution");
+      PVDB_REQUIRE(k0->ldim[a] == density->ldim[a], "k0 and density grids need the same leaf lattice");
+    }
     if (m->k0_channels < k0->C) {
       dev_free(m->w.r_k0);
       m->w.r_k0 = nullptr;
@@ -439,56 +609,56 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   return PVDB_OK;
 }
 
-static bool same_topology(const pvdb_grid_s* a, const pvdb_grid_s* b) {
-  if (a->nleaf != b->nleaf) return false;
-  for (int q = 0; q < 3; ++q)
-    if (a->ldim[q] != b->ldim[q]) return false;
-  return a->h_table == b->h_table;
-}
-
 int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_last,
                         const float* grad_k0, cudaStream_t st) {
   pvdb_grid_s* density = m->density;
   pvdb_grid_s* k0 = m->k0;
   const int R = m->n_rays;
   if (R == 0) return PVDB_OK;
-  const int64_t nmax = m->slots * 8;
+  const int64_t nmax = m->slots;
   int rc = scratch_reserve(m->red, nmax);
   if (rc) return rc;
+  const int64_t ncells = int64_t(density->ldim[0]) * density->ldim[1] * density->ldim[2] * kLeafVox;
+  if (m->cell_map_cap < size_t(ncells)) {
+    dev_free(m->cell_map);
+    m->cell_map = nullptr;
+    m->cell_map_cap = 0;
+    if ((rc = dev_alloc((void**)&m->cell_map, size_t(ncells) * 4))) return rc;
+    PVDB_CHECK_CUDA(cudaMemsetAsync(m->cell_map, 0xFF, size_t(ncells) * 4, st));
+    m->cell_map_cap = size_t(ncells);
+  }
+  const bool use_k0 = k0 && grad_k0;
+  const int C = use_k0 ? k0->C : 0;
+  PVDB_REQUIRE(C <= 16, "the march backward takes at most 16 k0 channels");
+  const int nq = (C + 3) / 4;
+  if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)) ||
+      (rc = dev_reserve((void**)&m->cell_pd, &m->cell_pd_cap, size_t(ncells) * 8 * 4)) ||
+      (nq && (rc = dev_reserve((void**)&m->cell_pk, &m->cell_pk_cap, size_t(ncells) * 8 * nq * 16))))
+    return rc;
   const int nb = ceil_div(R, kMarchWarps);
   k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
-                                            m->red.keys[0]);
+                                            use_k0 ? grad_k0 : nullptr, C, m->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
   int buf = 0;
-  rc = radix_sort_pairs_dev(m->red, nmax, m->w.totals + 2, slot_key_bits(density->nslots()), true,
-                            &buf, st);
+  rc = radix_sort_pairs_dev(m->red, nmax, m->w.totals + 0, slot_key_bits(ncells), true, &buf, st);
   if (rc) return rc;
   if (m->prof) prof_mark(st, 7);
-  const bool use_k0 = k0 && grad_k0;
-  const bool shared = use_k0 && same_topology(density, k0);
-  MarchSrc src{m->w.b_pos, m->w.b_gsig, m->w.b_row, shared ? grad_k0 : nullptr,
-               k0 ? k0->C : 0};
-  const int grid = num_sms() * 16;
-  k_segment_reduce<MarchSrc><<<grid, 256, 0, st>>>(
-      m->red.keys[buf], m->red.vals[buf], nmax, m->w.totals + 2, src, density->d_grad,
-      shared ? k0->d_grad : nullptr, k0 ? k0->C : 0, density->d_touched,
-      shared ? k0->d_touched : nullptr);
-  PVDB_CHECK_LAUNCH("k_segment_reduce(march)");
-  if (use_k0 && !shared) {
-    rc = scratch_reserve(m->red2, nmax);
-    if (rc) return rc;
-    k_march_keys_k0<<<grid, 256, 0, st>>>(k0->view(), m->w, m->red2.keys[0]);
-    PVDB_CHECK_LAUNCH("k_march_keys_k0");
-    rc = radix_sort_pairs_dev(m->red2, nmax, m->w.totals + 2, slot_key_bits(k0->nslots()), true,
-                              &buf, st);
-    if (rc) return rc;
-    MarchSrc src2{m->w.b_pos, nullptr, m->w.b_row, grad_k0, k0->C};
-    k_segment_reduce<MarchSrc><<<grid, 256, 0, st>>>(m->red2.keys[buf], m->red2.vals[buf], nmax,
-                                                     m->w.totals + 2, src2, nullptr, k0->d_grad,
-                                                     k0->C, nullptr, k0->d_touched);
-    PVDB_CHECK_LAUNCH("k_segment_reduce(k0)");
+  const uint32_t* skeys = m->red.keys[buf];
+  const uint32_t* svals = m->red.vals[buf];
+  const int grid = stride_grid();
+  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 0);
+  PVDB_CHECK_LAUNCH("k_cell_map_set");
+  switch (nq) {
+    case 0: rc = cell_reduce_launch<0>(m, density, k0, skeys, svals, st); break;
+    case 1: rc = cell_reduce_launch<1>(m, density, k0, skeys, svals, st); break;
+    case 2: rc = cell_reduce_launch<2>(m, density, k0, skeys, svals, st); break;
+    case 3: rc = cell_reduce_launch<3>(m, density, k0, skeys, svals, st); break;
+    default: rc = cell_reduce_launch<4>(m, density, k0, skeys, svals, st); break;
   }
+  if (rc) return rc;
+  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 1);
+  PVDB_CHECK_LAUNCH("k_cell_map_set(clear)");
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
 }
@@ -550,8 +720,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
       (rc = dev_alloc((void**)&w.k_step, S * 4)) || (rc = dev_alloc((void**)&w.k_row, S * 4)) ||
       (rc = dev_alloc((void**)&w.r_w, S * 4)) || (rc = dev_alloc((void**)&w.r_alpha, S * 4)) ||
       (rc = dev_alloc((void**)&w.r_ray, S * 4)) || (rc = dev_alloc((void**)&w.r_step, S * 4)) ||
-      (rc = dev_alloc((void**)&w.b_pos, S * 12)) || (rc = dev_alloc((void**)&w.b_gsig, S * 4)) ||
-      (rc = dev_alloc((void**)&w.b_row, S * 4)) || (rc = dev_alloc((void**)&w.totals, 64))) {
+      (rc = dev_alloc((void**)&w.totals, 64))) {
     pvdb_march_destroy(m);
     return rc;
   }
@@ -568,13 +737,15 @@ int pvdb_march_destroy(pvdb_march m) {
   if (!m) return PVDB_OK;
   MarchW& w = m->w;
   void* ptrs[] = {w.ray_sd, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
-                  w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_pos,
-                  w.b_gsig, w.b_row, w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed,
+                  w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec,
+                  w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,
                   m->t_loss_part, m->t_rgb_marched};
   for (void* p : ptrs) dev_free(p);
   free_scratch(m->red);
-  free_scratch(m->red2);
+  dev_free(m->cell_map);
+  dev_free(m->cell_pd);
+  dev_free(m->cell_pk);
   delete m;
   return PVDB_OK;
 }

@@ -39,10 +39,10 @@ struct MarchW {
   float* r_alpha;
   int32_t* r_ray;
   int32_t* r_step;
-  // per kept sample (global kept index), backward
-  float* b_pos;
-  float* b_gsig;
-  int32_t* b_row;
+  // per kept sample (global kept index), backward: record of 1 + nq float4,
+  // (x, y, z, dL/dsigma) then the k0 gradient of the sample's colour row
+  // (zeros for a sample without one), nq = ceil(C/4)
+  float4* b_rec;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   uint32_t* totals;
 };
@@ -55,8 +55,14 @@ struct pvdb_march_s {
   int64_t slots = 0;  // max_rays * cap
   int k0_channels = 0;
   pvdb::MarchW w{};
-  pvdb::ReduceScratch red;   // contributions (8 per kept sample)
-  pvdb::ReduceScratch red2;  // second reduction when k0 has its own topology
+  pvdb::ReduceScratch red;   // kept samples sorted by cell key
+  int32_t* cell_map = nullptr;  // [cells of the leaf lattice] first sorted index, -1 = none
+  size_t cell_map_cap = 0;      // elements
+  float* cell_pd = nullptr;     // [cells][8 corners] density partial sums
+  size_t cell_pd_cap = 0;       // bytes
+  float4* cell_pk = nullptr;    // [cells][8 corners][nq] k0 partial sums
+  size_t cell_pk_cap = 0;       // bytes
+  size_t b_rec_cap = 0;         // bytes of w.b_rec
   uint32_t* scan_partial = nullptr;
   size_t scan_partial_cap = 0;
   // state of the last forward
@@ -82,4 +88,14 @@ struct pvdb_march_s {
   float* t_loss_part = nullptr;  // [max_rays]
   float* t_rgb_marched = nullptr;  // [max_rays,3]
   size_t t_cap_rows = 0;
+  // CUDA graph of the fused train step (train.cu)
+  cudaGraph_t g_graph = nullptr;
+  cudaGraphExec_t g_exec = nullptr;
+  cudaStream_t g_stream = nullptr;  // capture stream
+  float* g_in = nullptr;            // staged rays_o, rays_d, viewdirs, target [4][R][3]
+  size_t g_in_cap = 0;
+  float* g_scal = nullptr;          // [0..2] Adam step sizes, [4] loss
+  std::vector<uint8_t> g_key;       // what the graph was captured for
+  std::vector<uint8_t> g_pending;   // key of the last eager step (capture on a repeat)
+  uint64_t g_launches = 0;          // library launches per replay
 };

@@ -35,31 +35,44 @@ struct MlpArgs {
 // [w0 (128 x din), b0 (128), w1 (128 x 128), b1 (128), w2 (3 x 128), b2 (3)].
 __host__ __device__ inline int64_t mlp_param_count(int din) { return int64_t(kW) * din + kW + kW * kW + kW + 3 * kW + 3; }
 
-// PE of a unit view direction: [d, sin(d*2^i) (i-major per axis), cos(...)]
-// (dvgo.py:354-355).
-__device__ __forceinline__ void view_pe(const float d[3], int npe, float* out) {
-  out[0] = d[0]; out[1] = d[1]; out[2] = d[2];
-  for (int a = 0; a < 3; ++a)
-    for (int i = 0; i < npe; ++i) {
-      const float x = d[a] * float(1 << i);
-      out[3 + a * npe + i] = sinf(x);
-      out[3 + 3 * npe + a * npe + i] = cosf(x);
-    }
-}
-
+// PE of a unit view direction (dvgo.py:354-355): [d, sin(d*2^i), cos(d*2^i)]
+// with the frequencies innermost per axis: sin at 3 + a*npe + i, cos at
+// 3 + 3*npe + a*npe + i.
 // Per ray: pe[r][0:dpe] and hpe[r][n] = b0[n] + sum_q w0[n][c0+q] * pe[r][q].
-__global__ void k_pe_hpe(const float* __restrict__ viewdirs, int R, int npe, MlpArgs a,
-                         float* pe_out, float* hpe) {
-  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (t >= int64_t(R) * kW) return;
-  const int r = int(t / kW), n = int(t % kW);
-  const float d[3] = {viewdirs[r * 3], viewdirs[r * 3 + 1], viewdirs[r * 3 + 2]};
-  float pe[kMaxPe];
-  view_pe(d, npe, pe);
-  float s = 0.f;
-  for (int q = 0; q < a.dpe; ++q) s = fmaf(a.w0[n * a.din + a.c0 + q], pe[q], s);
-  hpe[t] = a.b0[n] + s;
-  if (n < a.dpe) pe_out[int64_t(r) * kMaxPe + n] = pe[n];
+// A 128-thread block takes kPeRays rays: the PE part of W0 is staged
+// transposed in shared memory (coalesced), each PE component is evaluated
+// once, then thread n forms hpe[r][n] for the block's rays.
+constexpr int kPeRays = 32;
+__global__ void __launch_bounds__(128)
+    k_pe_hpe(const float* __restrict__ viewdirs, int R, int npe, MlpArgs a, float* pe_out,
+             float* hpe) {
+  __shared__ float wt[kMaxPe][kW];       // wt[q][n] = w0[n][c0+q]
+  __shared__ float pe_s[kPeRays][kMaxPe];
+  const int n = threadIdx.x;
+  const int r0 = blockIdx.x * kPeRays;
+  for (int q = 0; q < a.dpe; ++q) wt[q][n] = a.w0[n * a.din + a.c0 + q];
+  for (int e = n; e < kPeRays * a.dpe; e += kW) {
+    const int rr = e / a.dpe, q = e % a.dpe, r = r0 + rr;
+    if (r >= R) continue;
+    float v;
+    if (q < 3) {
+      v = viewdirs[r * 3 + q];
+    } else {
+      const int qq = q - 3, sc = qq / (3 * npe), rem = qq % (3 * npe), ax = rem / npe,
+                i = rem % npe;
+      const float x = viewdirs[r * 3 + ax] * float(1 << i);
+      v = sc ? cosf(x) : sinf(x);
+    }
+    pe_s[rr][q] = v;
+    pe_out[int64_t(r) * kMaxPe + q] = v;
+  }
+  __syncthreads();
+  const float b = a.b0[n];
+  for (int rr = 0; rr < kPeRays && r0 + rr < R; ++rr) {
+    float s = 0.f;
+    for (int q = 0; q < a.dpe; ++q) s = fmaf(wt[q][n], pe_s[rr][q], s);
+    hpe[int64_t(r0 + rr) * kW + n] = b + s;
+  }
 }
 
 struct MlpSmem {
@@ -416,14 +429,13 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
   if (rc) return rc;
   float* hpe = m->hpe;
   float* pe = m->hpe + size_t(m->max_rays) * kW;
-  k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
                                m->w.r_ray, hpe, m->w.totals, rgb, 0, &m->mlp_packed,
                                &m->mlp_packed_cap, m->w.totals + 3, st);
-  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(sizeof(MlpSmem))));
+  PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
       a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_f32");
@@ -439,13 +451,12 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
   if (R <= 0) return PVDB_OK;
   float* hpe = hpe_buf;
   float* pe = hpe_buf + size_t(R) * kW;
-  k_pe_hpe<<<ceil_div(int64_t(R) * kW, 256), 256, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, hpe,
                                totals, out, out_logits, blob, blob_cap, err, st);
-  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(sizeof(MlpSmem))));
+  PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
                                                                   out, out_logits);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_f32(rows)");
@@ -482,8 +493,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
     PVDB_CHECK_LAUNCH("k_wgrad_reduce");
     return PVDB_OK;
   }
-  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(sizeof(MlpBwdSmem))));
+  PVDB_SMEM_ATTR(k_mlp_bwd_f32, int(sizeof(MlpBwdSmem)));
   k_mlp_bwd_f32<<<G, kMlpThreads, sizeof(MlpBwdSmem), st>>>(
       a, k0rows, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
       grad_rgb, grad_k0, m->wpart);
@@ -540,7 +550,7 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   // backward does not rely on a preceding forward call of the same weights.
   rc = mlp_reserve(m, a.din);
   if (rc) return rc;
-  k_pe_hpe<<<ceil_div(int64_t(m->n_rays) * kW, 256), 256, 0, st>>>(
+  k_pe_hpe<<<ceil_div(m->n_rays, kPeRays), kW, 0, st>>>(
       viewdirs, m->n_rays, (a.dpe - 3) / 6, a, m->hpe + size_t(m->max_rays) * kW, m->hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   const int64_t P = mlp_param_count(a.din);

@@ -694,8 +694,7 @@ int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 0);
   PVDB_CHECK_LAUNCH("k_pack");
-  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(kSmFwdBytes)));
+  PVDB_SMEM_ATTR(k_mlp_fwd_tc, int(kSmFwdBytes));
   k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
       a, static_cast<const uint8_t*>(*blob), k0rows, ray, hpe, totals, out, out_logits, err);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_tc");
@@ -717,8 +716,7 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 1);
   PVDB_CHECK_LAUNCH("k_pack");
-  PVDB_CHECK_CUDA(cudaFuncSetAttribute(k_mlp_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(kSmBwdBytes)));
+  PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
   k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob), k0rows,
                                                       ray, hpe, pe, pe_stride, totals, rgb, grad_rgb,
                                                       grad_k0, wpart, err);

@@ -119,5 +119,6 @@ extern "C" int pvdb_grid_sample_backward_noalloc(pvdb_grid g, const float* xs, c
       rs.keys[buf], rs.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
       g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched);
   PVDB_CHECK_LAUNCH("k_segment_reduce(noalloc)");
+  g->tlist_valid = false;  // new touched leaves
   return PVDB_OK;
 }

@@ -24,37 +24,45 @@ float adam_step_size(float lr, float beta_m, float beta_v, int step) {
 
 // One thread per (slot, group); a group is 1 channel for scalar grids and a
 // 3-channel Vec3 for multi-channel grids (the reference skips a Vec3 only when
-// all three gradient components are zero, colorvdb.cu:318).
+// all three gradient components are zero, colorvdb.cu:318). With a leaf list
+// only the listed leaves are visited (grid-stride; the count is on the device).
 __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict__ v,
-                           const float* __restrict__ perlr, float stepsz, float eps, float b0,
-                           float b1, int mode, int zero_after,
-                           const uint8_t* __restrict__ touched) {
+                           const float* __restrict__ perlr, float stepsz,
+                           const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
+                           int mode, int zero_after, const int32_t* __restrict__ list,
+                           const uint32_t* __restrict__ count) {
   const int G = g.C == 1 ? 1 : 3;
   const int ngroups = g.C / G;
-  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (t >= int64_t(g.nleaf) * kLeafVox * ngroups) return;
-  const int64_t slot = t / ngroups;
-  const int grp = int(t % ngroups);
-  const int leaf = int(slot >> 9), vox = int(slot & 511);
-  if (touched && !touched[leaf]) return;
-  if (!((__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull)) return;
-  const int64_t base = slot * g.C + int64_t(grp) * G;
-  float gr[3];
-  bool allzero = true;
-  for (int q = 0; q < G; ++q) {
-    gr[q] = g.grad[base + q];
-    allzero = allzero && (gr[q] == 0.f);
-  }
-  if (mode == 1 && allzero) return;
-  const float lrf = mode == 2 ? perlr[slot] : 1.f;
-  for (int q = 0; q < G; ++q) {
-    const float mn = b0 * m[base + q] + (1 - b0) * gr[q];
-    const float vn = b1 * v[base + q] + (1 - b1) * gr[q] * gr[q];
-    m[base + q] = mn;
-    v[base + q] = vn;
-    const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
-    g.data[base + q] = g.data[base + q] - num / (eps + sqrtf(vn));
-    if (zero_after) g.grad[base + q] = 0.f;
+  const int64_t per = int64_t(kLeafVox) * ngroups;
+  const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
+  if (stepsz_dev) stepsz = *stepsz_dev;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * per;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t li = i / per;
+    const int leaf = list ? list[li] : int(li);
+    const int64_t rem = i - li * per;
+    const int vox = int(rem / ngroups);
+    const int grp = int(rem % ngroups);
+    const int64_t slot = int64_t(leaf) * kLeafVox + vox;
+    if (!((__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull)) continue;
+    const int64_t base = slot * g.C + int64_t(grp) * G;
+    float gr[3];
+    bool allzero = true;
+    for (int q = 0; q < G; ++q) {
+      gr[q] = g.grad[base + q];
+      allzero = allzero && (gr[q] == 0.f);
+    }
+    if (mode == 1 && allzero) continue;
+    const float lrf = mode == 2 ? perlr[slot] : 1.f;
+    for (int q = 0; q < G; ++q) {
+      const float mn = b0 * m[base + q] + (1 - b0) * gr[q];
+      const float vn = b1 * v[base + q] + (1 - b1) * gr[q] * gr[q];
+      m[base + q] = mn;
+      v[base + q] = vn;
+      const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
+      g.data[base + q] = g.data[base + q] - num / (eps + sqrtf(vn));
+      if (zero_after) g.grad[base + q] = 0.f;
+    }
   }
 }
 
@@ -69,12 +77,13 @@ __global__ void k_clear_u8(uint8_t* t, int n) {
 template <int MODE>
 __global__ void k_adam_dense(float* __restrict__ p, const float* __restrict__ g,
                              float* __restrict__ m, float* __restrict__ v,
-                             const float* __restrict__ perlr, int64_t n, float stepsz, float b1,
-                             float b2, float eps) {
+                             const float* __restrict__ perlr, int64_t n, float stepsz,
+                             const float* __restrict__ stepsz_dev, float b1, float b2, float eps) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
   if (MODE == 1 && gi == 0.f) return;
+  if (stepsz_dev) stepsz = *stepsz_dev;
   const float mn = b1 * m[i] + (1 - b1) * gi;
   const float vn = b2 * v[i] + (1 - b2) * gi * gi;
   m[i] = mn;
@@ -87,43 +96,63 @@ __global__ void k_adam_dense(float* __restrict__ p, const float* __restrict__ g,
 
 int adam_dense_launch(float* param, const float* grad, float* m, float* v, const float* perlr,
                       int64_t n, float stepsz, float b1, float b2, float eps, int mode,
-                      cudaStream_t st) {
+                      cudaStream_t st, const float* stepsz_dev) {
   if (n <= 0) return PVDB_OK;
   const int nb = ceil_div(n, 256);
+  const float* sd = stepsz_dev;
   if (mode == 1)
-    k_adam_dense<1><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+    k_adam_dense<1><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   else if (mode == 2)
-    k_adam_dense<2><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+    k_adam_dense<2><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   else
-    k_adam_dense<0><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, b1, b2, eps);
+    k_adam_dense<0><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   PVDB_CHECK_LAUNCH("k_adam_dense");
   return PVDB_OK;
 }
 
+int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
+               cudaStream_t st);
+
+// Advances the step counter and returns this step's Adam step size.
+float opt_next_stepsz(pvdb_opt_s* o) {
+  o->step++;
+  return adam_step_size(o->lr, o->beta0, o->beta1, o->step);
+}
+
 // Runs one voxel-Adam step (used by the C ABI and the fused train step).
 int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st) {
+  return opt_launch(o, mode, zero_after, opt_next_stepsz(o), nullptr, st);
+}
+
+// The launches of one voxel-Adam step; the step size is stepsz, or
+// *stepsz_dev when that is given (a captured graph reads it each replay).
+int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
+               cudaStream_t st) {
   pvdb_grid_s* g = o->params;
-  o->step++;
-  const float stepsz = adam_step_size(o->lr, o->beta0, o->beta1, o->step);
-  const int G = g->C == 1 ? 1 : 3;
-  const int64_t nt = g->nslots() * (g->C / G);
-  const uint8_t* touched = (mode == 1 && !g->all_touched) ? g->d_touched : nullptr;
-  if (nt) {
-    k_vdb_adam<<<ceil_div(nt, 256), 256, 0, st>>>(
+  // mode 1 skips voxels whose gradient is zero: only the touched leaves matter
+  const bool use_list = mode == 1 && !g->all_touched;
+  if (g->nslots()) {
+    if (use_list) {
+      int rc = touched_list(g, st);
+      if (rc) return rc;
+    }
+    k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
         g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
-        mode == 2 ? o->per_lr->d_data : nullptr, stepsz, o->eps, o->beta0, o->beta1, mode,
-        zero_after, touched);
+        mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0, o->beta1,
+        mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
     PVDB_CHECK_LAUNCH("k_vdb_adam");
   }
   if (zero_after && g->nleaf) {
     k_clear_u8<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf);
     PVDB_CHECK_LAUNCH("k_clear_u8");
     g->all_touched = false;
+    g->tlist_valid = false;
   }
   return PVDB_OK;
 }
 
 pvdb_grid_s* opt_params(pvdb_opt_s* o) { return o->params; }
+pvdb_grid_s* opt_moment(pvdb_opt_s* o, int which) { return which ? o->exp_avg_sq : o->exp_avg; }
 float opt_lr_scale(pvdb_opt_s* o, float factor) {
   o->lr *= factor;
   return o->lr;

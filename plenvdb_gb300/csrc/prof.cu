@@ -12,6 +12,7 @@ namespace pvdb {
 
 static std::atomic<unsigned long long> g_launches{0};
 void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+uint64_t launch_counter() { return g_launches.load(); }
 
 namespace {
 struct Prof {

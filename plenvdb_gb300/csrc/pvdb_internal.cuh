@@ -47,6 +47,18 @@ void count_launches(int n);
   } while (0)
 #define PVDB_CHECK_LAUNCH(what) PVDB_CHECK_LAUNCHES(what, 1)
 
+// Opt a kernel into more than 48 KB of dynamic shared memory, once per
+// process (so a stream capture never issues the call).
+#define PVDB_SMEM_ATTR(kernel, bytes)                                                    \
+  do {                                                                                  \
+    static bool _done = false;                                                          \
+    if (!_done) {                                                                       \
+      PVDB_CHECK_CUDA(                                                                  \
+          cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); \
+      _done = true;                                                                     \
+    }                                                                                   \
+  } while (0)
+
 #define PVDB_REQUIRE(cond, msg)                                         \
   do {                                                                   \
     if (!(cond)) return ::pvdb::set_error(PVDB_ERR_ARG, msg);            \
@@ -104,6 +116,9 @@ struct pvdb_grid_s {
   float* d_grad = nullptr;
   uint8_t* d_touched = nullptr;  // [nleaf] leaves whose gradient may be nonzero
   bool all_touched = true;       // every leaf must be treated as touched
+  int32_t* d_tlist = nullptr;    // [nleaf] compacted ids of the touched leaves
+  uint32_t* d_tcount = nullptr;  // number of entries in d_tlist (device)
+  bool tlist_valid = false;      // d_tlist reflects d_touched
   std::vector<int32_t> h_table;
   std::vector<int32_t> h_origin;
   std::vector<uint64_t> h_mask;
@@ -248,7 +263,16 @@ void prof_mark(cudaStream_t st, int id);
 float adam_step_size(float lr, float beta_m, float beta_v, int step);
 int adam_dense_launch(float* param, const float* grad, float* m, float* v, const float* perlr,
                       int64_t n, float stepsz, float b1, float b2, float eps, int mode,
-                      cudaStream_t st);
+                      cudaStream_t st, const float* stepsz_dev = nullptr);
+// Launch-counter value (every library kernel launch adds one).
+uint64_t launch_counter();
+
+// Compacts the touched flags of g into g->d_tlist / d_tcount unless the list
+// is still valid (device work on st, no host synchronisation).
+int touched_list(pvdb_grid_s* g, cudaStream_t st);
+
+// Fixed grid for grid-stride kernels whose work size lives on the device.
+inline int stride_grid() { return num_sms() * 8; }
 
 // Number of key bits needed so that all slots and the invalid key sort apart.
 int slot_key_bits(int64_t nslots);

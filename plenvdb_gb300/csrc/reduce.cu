@@ -119,6 +119,43 @@ __global__ void k_scan_apply(const uint32_t* __restrict__ in, uint32_t* out, int
   }
 }
 
+// Single-block scan for short inputs: 1024 threads walk the input in chunks
+// of 16384 with a running carry (one launch instead of three).
+constexpr int kScan1Threads = 1024;
+constexpr int kScan1Items = 16;
+constexpr int64_t kScan1Max = 262144;  // inputs up to this length take the one-block path
+
+__global__ void __launch_bounds__(kScan1Threads)
+    k_scan_single(const uint32_t* __restrict__ in, uint32_t* out, int64_t n_max,
+                  const uint32_t* n_dev, uint32_t* total) {
+  __shared__ uint32_t carry_s;
+  const int64_t n = eff_size(n_max, n_dev);
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  constexpr int64_t kChunk = int64_t(kScan1Threads) * kScan1Items;
+  for (int64_t c0 = 0; c0 < n; c0 += kChunk) {
+    const int64_t base = c0 + int64_t(threadIdx.x) * kScan1Items;
+    uint32_t v[kScan1Items];
+    uint32_t s = 0;
+#pragma unroll
+    for (int q = 0; q < kScan1Items; ++q) {
+      v[q] = base + q < n ? in[base + q] : 0u;
+      s += v[q];
+    }
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan(s, &tot) + carry_s;
+#pragma unroll
+    for (int q = 0; q < kScan1Items; ++q) {
+      if (base + q < n) out[base + q] = run;
+      run += v[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total) *total = carry_s;
+}
+
 int scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total,
                        uint32_t** partial, size_t* partial_cap, cudaStream_t st) {
   return scan_exclusive_u32_dev(in, out, n, nullptr, total, partial, partial_cap, st);
@@ -129,6 +166,11 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
                            size_t* partial_cap, cudaStream_t st) {
   if (n_max <= 0) {
     if (total) PVDB_CHECK_CUDA(cudaMemsetAsync(total, 0, 4, st));
+    return PVDB_OK;
+  }
+  if (n_max <= kScan1Max) {
+    k_scan_single<<<1, kScan1Threads, 0, st>>>(in, out, n_max, n_dev, total);
+    PVDB_CHECK_LAUNCH("k_scan_single");
     return PVDB_OK;
   }
   const int64_t nb = (n_max + kScanTile - 1) / kScanTile;
@@ -259,9 +301,18 @@ int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev
   for (int shift = 0; shift < key_bits; shift += 8) {
     k_rs_upsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur], sizes, shift, rs.hist);
     PVDB_CHECK_LAUNCH("k_rs_upsweep");
-    rc = scan_exclusive_u32_dev(rs.hist, rs.hist, ntiles_max * kRsBins, sizes + 1, nullptr,
-                                &rs.partial, &rs.partial_cap, st);
-    if (rc) return rc;
+    // the histogram length is on the device; its host-side maximum assumes
+    // every slot is used, so a one-block scan over the actual length is the
+    // faster choice unless even the maximum is very long
+    if (ntiles_max * kRsBins <= (int64_t(1) << 23)) {
+      k_scan_single<<<1, kScan1Threads, 0, st>>>(rs.hist, rs.hist, ntiles_max * kRsBins,
+                                                 sizes + 1, nullptr);
+      PVDB_CHECK_LAUNCH("k_scan_single(hist)");
+    } else {
+      rc = scan_exclusive_u32_dev(rs.hist, rs.hist, ntiles_max * kRsBins, sizes + 1, nullptr,
+                                  &rs.partial, &rs.partial_cap, st);
+      if (rc) return rc;
+    }
     k_rs_downsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
                                                 (first && iota_vals) ? nullptr : rs.vals[cur],
                                                 sizes, shift, rs.hist, rs.keys[cur ^ 1],
@@ -372,6 +423,7 @@ extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const flo
       g->red.keys[buf], g->red.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
       g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched);
   PVDB_CHECK_LAUNCH("k_segment_reduce");
+  g->tlist_valid = false;
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
   return PVDB_OK;
 }

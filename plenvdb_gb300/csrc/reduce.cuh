@@ -29,6 +29,16 @@ __device__ __forceinline__ void emit_corner_keys(const GridView& g, float x, flo
   }
 }
 
+// Leaf-major key of the trilinear cell (or voxel) (i,j,k) over the dense leaf
+// lattice [0, 8*ldim): dense leaf index * 512 + NanoVDB voxel offset; defined
+// whether or not the leaf is allocated. kInvalidKey outside the lattice.
+__device__ __forceinline__ uint32_t cell_key(const int ld[3], int i, int j, int k) {
+  if ((unsigned)i >= (unsigned)(ld[0] << 3) || (unsigned)j >= (unsigned)(ld[1] << 3) ||
+      (unsigned)k >= (unsigned)(ld[2] << 3))
+    return kInvalidKey;
+  return (uint32_t(((i >> 3) * ld[1] + (j >> 3)) * ld[2] + (k >> 3)) << 9) | uint32_t(vox_offset(i, j, k));
+}
+
 // Source of contributions for the segmented reduce:
 //   pos(s)       -> index-space position of sample s
 //   gd(s)        -> density gradient of sample s (scalar grid)

@@ -30,8 +30,11 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
                         const float* grad_k0, cudaStream_t st);
 int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
                            cudaStream_t st);
-int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st);
+float opt_next_stepsz(pvdb_opt_s* o);
+int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
+               cudaStream_t st);
 pvdb_grid_s* opt_params(pvdb_opt_s* o);
+pvdb_grid_s* opt_moment(pvdb_opt_s* o, int which);
 float opt_lr_scale(pvdb_opt_s* o, float factor);
 
 struct LossW {
@@ -118,6 +121,207 @@ static int train_reserve(pvdb_march_s* m, int C) {
   return PVDB_OK;
 }
 
+// Writes the step sizes a captured train step reads.
+__global__ void k_set_step_scalars(float* scal, float ss_d, float ss_k, float ss_n) {
+  scal[0] = ss_d;
+  scal[1] = ss_k;
+  scal[2] = ss_n;
+}
+
+struct TrainArgs {
+  pvdb_march_s* m;
+  pvdb_opt_s* dopt;
+  pvdb_opt_s* kopt;
+  pvdb_rgbnet_state* net;
+  const float *ro, *rd, *vd, *tgt;
+  int R;
+  const pvdb_train_config* cfg;
+  float* loss;
+  float ss[3];             // Adam step sizes (density, k0, rgbnet)
+  const float* ss_dev;     // or read from the device ([0..2]) when captured
+  bool prof;
+};
+
+// All device work of one train step: launches only, no host state changes
+// (so it can be captured into a graph and replayed).
+static int train_launches(const TrainArgs& t, cudaStream_t st) {
+  pvdb_march_s* m = t.m;
+  pvdb_rgbnet_state* net = t.net;
+  const pvdb_train_config* cfg = t.cfg;
+  pvdb_grid_s* dg = opt_params(t.dopt);
+  pvdb_grid_s* kg = opt_params(t.kopt);
+  const int n_rays = t.R;
+  pvdb_stream s = reinterpret_cast<pvdb_stream>(st);
+  // parameters in the flat layout [w0,b0,w1,b1,w2,b2]
+  MlpArgs a;
+  a.c0 = net->c0;
+  a.dpe = 3 + 6 * net->pe;
+  a.din = a.c0 + a.dpe;
+  const int W = 128;
+  a.w0 = net->params;
+  a.b0 = a.w0 + W * a.din;
+  a.w1 = a.b0 + W;
+  a.b1 = a.w1 + W * W;
+  a.w2 = a.b1 + W;
+  a.b2 = a.w2 + 3 * W;
+  const int64_t P = int64_t(W) * a.din + W + W * W + W + 3 * W + 3;
+
+  if (t.prof) {
+    prof_begin_call();
+    prof_mark(st, 0);
+  }
+  struct ProfGuard {
+    pvdb_march_s* m;
+    ~ProfGuard() { m->prof = false; }
+  } guard{m};
+  m->prof = t.prof;
+  int rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st);
+  if (rc) return rc;
+  rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st);
+  if (rc) return rc;
+  if (t.prof) prof_mark(st, 3);
+  rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
+  if (rc) return rc;
+  LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
+  k_loss<<<ceil_div(n_rays, 8), 256, 0, st>>>(m->w, m->t_rgb, m->t_rgb_marched, t.tgt, n_rays, L,
+                                              m->t_grad_rgb, m->t_grad_w, m->t_grad_last,
+                                              m->t_loss_part);
+  PVDB_CHECK_LAUNCH("k_loss");
+  k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, t.loss);
+  PVDB_CHECK_LAUNCH("k_loss_sum");
+  if (t.prof) prof_mark(st, 4);
+  rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads,
+                         cfg->precision, st);
+  if (rc) return rc;
+  if (t.prof) prof_mark(st, 5);
+  rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);
+  if (rc) return rc;
+  // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
+  const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
+  if (cfg->tv_weight_density > 0.f) {
+    const float w = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
+    rc = pvdb_grid_tv_add_grad(dg, w, w, w, cfg->tv_dense_mode, 0, s);
+    if (rc) return rc;
+  }
+  if (cfg->tv_weight_k0 > 0.f) {
+    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
+    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0, s);
+    if (rc) return rc;
+  }
+  if (t.prof) prof_mark(st, 9);
+  rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st);
+  if (rc) return rc;
+  rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, st);
+  if (rc) return rc;
+  if (t.prof) prof_mark(st, 10);
+  rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
+                         t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0, st,
+                         t.ss_dev ? t.ss_dev + 2 : nullptr);
+  if (rc) return rc;
+  if (t.prof) prof_mark(st, 11);
+  return PVDB_OK;
+}
+
+static void graph_reset(pvdb_march_s* m) {
+  if (m->g_exec) cudaGraphExecDestroy(m->g_exec);
+  if (m->g_graph) cudaGraphDestroy(m->g_graph);
+  m->g_exec = nullptr;
+  m->g_graph = nullptr;
+  m->g_key.clear();
+}
+
+template <class T>
+static void key_put(std::vector<uint8_t>& k, const T& v) {
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+  k.insert(k.end(), p, p + sizeof(T));
+}
+
+static void grid_key(std::vector<uint8_t>& k, const pvdb_grid_s* g) {
+  key_put(k, g);
+  key_put(k, g->d_data);
+  key_put(k, g->d_grad);
+  key_put(k, g->d_mask);
+  key_put(k, g->d_table);
+  key_put(k, g->d_touched);
+  key_put(k, g->nleaf);
+}
+
+// Everything a captured step has baked in: sizes, configuration, and the
+// device pointers of every buffer it touches.
+static std::vector<uint8_t> graph_key(const TrainArgs& t) {
+  std::vector<uint8_t> k;
+  const pvdb_march_s* m = t.m;
+  key_put(k, t.R);
+  key_put(k, *t.cfg);
+  key_put(k, t.dopt);
+  key_put(k, t.kopt);
+  for (pvdb_opt_s* o : {t.dopt, t.kopt}) {
+    grid_key(k, opt_params(o));
+    grid_key(k, opt_moment(o, 0));
+    grid_key(k, opt_moment(o, 1));
+  }
+  key_put(k, t.net->params);
+  key_put(k, t.net->grads);
+  key_put(k, t.net->exp_avg);
+  key_put(k, t.net->exp_avg_sq);
+  key_put(k, t.net->c0);
+  key_put(k, t.net->pe);
+  key_put(k, m->w);
+  key_put(k, m->hpe);
+  key_put(k, m->wpart);
+  key_put(k, m->mlp_packed);
+  key_put(k, m->red.keys[0]);
+  key_put(k, m->red.keys[1]);
+  key_put(k, m->red.vals[0]);
+  key_put(k, m->red.vals[1]);
+  key_put(k, m->red.hist);
+  key_put(k, m->red.partial);
+  key_put(k, m->scan_partial);
+  key_put(k, m->cell_map);
+  key_put(k, m->cell_pd);
+  key_put(k, m->cell_pk);
+  key_put(k, m->t_rgb);
+  key_put(k, m->t_grad_k0);
+  key_put(k, m->g_in);
+  key_put(k, m->g_scal);
+  return k;
+}
+
+static int graph_capture(TrainArgs t, const std::vector<uint8_t>& key) {
+  pvdb_march_s* m = t.m;
+  graph_reset(m);
+  if (!m->g_stream) PVDB_CHECK_CUDA(cudaStreamCreateWithFlags(&m->g_stream, cudaStreamNonBlocking));
+  const size_t R3 = size_t(t.R) * 3;
+  t.ro = m->g_in;
+  t.rd = m->g_in + R3;
+  t.vd = m->g_in + 2 * R3;
+  t.tgt = m->g_in + 3 * R3;
+  t.loss = m->g_scal + 4;
+  t.ss_dev = m->g_scal;
+  t.prof = false;
+  const uint64_t before = launch_counter();
+  PVDB_CHECK_CUDA(cudaStreamBeginCapture(m->g_stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = train_launches(t, m->g_stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(m->g_stream, &g);
+  const uint64_t n = launch_counter() - before;
+  count_launches(-int(n));  // nothing ran yet; each replay counts them
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc) return rc;
+    return cuda_error(e, "cudaStreamEndCapture");
+  }
+  m->g_graph = g;
+  const cudaError_t ei = cudaGraphInstantiate(&m->g_exec, g, 0);
+  if (ei != cudaSuccess) {
+    graph_reset(m);
+    return cuda_error(ei, "cudaGraphInstantiate");
+  }
+  m->g_launches = n;
+  m->g_key = key;
+  return PVDB_OK;
+}
+
 }  // namespace pvdb
 
 using namespace pvdb;
@@ -135,78 +339,56 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
                "null rgbnet state");
   PVDB_REQUIRE(net->width == 128 && net->c0 > 0 && net->c0 <= 16 && net->pe >= 0 && net->pe <= 4,
                "unsupported rgbnet shape");
+  PVDB_REQUIRE(cfg->precision == 0 || cfg->precision == 1, "precision must be 0 or 1");
   pvdb_grid_s* dg = opt_params(density_opt);
   pvdb_grid_s* kg = opt_params(k0_opt);
   PVDB_REQUIRE(dg->C == 1 && kg->C == net->c0, "grid channels do not match the rgbnet");
   cudaStream_t st = as_stream(s);
   int rc = train_reserve(m, kg->C);
   if (rc) return rc;
-  // parameters in the flat layout [w0,b0,w1,b1,w2,b2]
-  MlpArgs a;
-  a.c0 = net->c0;
-  a.dpe = 3 + 6 * net->pe;
-  a.din = a.c0 + a.dpe;
-  const int W = 128;
-  a.w0 = net->params;
-  a.b0 = a.w0 + W * a.din;
-  a.w1 = a.b0 + W;
-  a.b1 = a.w1 + W * W;
-  a.w2 = a.b1 + W;
-  a.b2 = a.w2 + 3 * W;
-  const int64_t P = int64_t(W) * a.din + W + W * W + W + 3 * W + 3;
-
-  prof_begin_call();
-  prof_mark(st, 0);
-  struct ProfGuard {
-    pvdb_march_s* m;
-    ~ProfGuard() { m->prof = false; }
-  } guard{m};
-  m->prof = true;
-  rc = march_forward_impl(m, dg, kg, rays_o, rays_d, n_rays, &cfg->march, nullptr, nullptr, st);
-  if (rc) return rc;
-  rc = mlp_forward_impl(m, a, m->w.r_k0, viewdirs, m->t_rgb, cfg->precision, st);
-  if (rc) return rc;
-  prof_mark(st, 3);
-  rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
-  if (rc) return rc;
-  LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
-  k_loss<<<ceil_div(n_rays, 8), 256, 0, st>>>(m->w, m->t_rgb, m->t_rgb_marched, target, n_rays, L,
-                                              m->t_grad_rgb, m->t_grad_w, m->t_grad_last,
-                                              m->t_loss_part);
-  PVDB_CHECK_LAUNCH("k_loss");
-  k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, loss_out);
-  PVDB_CHECK_LAUNCH("k_loss_sum");
-  prof_mark(st, 4);
-  rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads,
-                         cfg->precision, st);
-  if (rc) return rc;
-  prof_mark(st, 5);
-  rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);
-  if (rc) return rc;
-  // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
-  const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
-  if (cfg->tv_weight_density > 0.f) {
-    const float w = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
-    rc = pvdb_grid_tv_add_grad(dg, w, w, w, cfg->tv_dense_mode, 0, s);
-    if (rc) return rc;
+  // a graph replays the step whose gradients start at zero on tracked leaves;
+  // right after the grids were written from outside, step eagerly once
+  bool graph_ok = cfg->use_graph && !dg->all_touched && !kg->all_touched;
+  TrainArgs t{m, density_opt, k0_opt, net, rays_o, rays_d, viewdirs, target, n_rays, cfg,
+              loss_out, {0.f, 0.f, 0.f}, nullptr, !graph_ok};
+  if (graph_ok) {
+    const size_t R3 = size_t(n_rays) * 3;
+    if ((rc = dev_reserve((void**)&m->g_in, &m->g_in_cap, 4 * R3 * 4))) return rc;
+    if (!m->g_scal && (rc = dev_alloc((void**)&m->g_scal, 64))) return rc;
+    // capture once the same key was seen on the previous call, i.e. after an
+    // eager step allocated every buffer the step needs
+    std::vector<uint8_t> key = graph_key(t);
+    if (!m->g_exec || key != m->g_key) {
+      if (key == m->g_pending) {
+        rc = graph_capture(t, key);
+        if (rc) return rc;
+      } else {
+        graph_reset(m);
+        m->g_pending = key;
+        graph_ok = false;
+        t.prof = true;
+      }
+    }
   }
-  if (cfg->tv_weight_k0 > 0.f) {
-    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
-    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0, s);
-    if (rc) return rc;
-  }
-  prof_mark(st, 9);
-  rc = opt_step_launch(density_opt, 1, 1, st);
-  if (rc) return rc;
-  rc = opt_step_launch(k0_opt, 1, 1, st);
-  if (rc) return rc;
-  prof_mark(st, 10);
+  // host-side optimiser state (run.py:592-598 order: step, then lr decay)
+  t.ss[0] = opt_next_stepsz(density_opt);
+  t.ss[1] = opt_next_stepsz(k0_opt);
   *net->step += 1;
-  const float stepsz = adam_step_size(*net->lr, cfg->rgbnet_beta1, cfg->rgbnet_beta2, *net->step);
-  rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P, stepsz,
-                         cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0, st);
-  if (rc) return rc;
-  prof_mark(st, 11);
+  t.ss[2] = adam_step_size(*net->lr, cfg->rgbnet_beta1, cfg->rgbnet_beta2, *net->step);
+  if (graph_ok) {
+    const size_t R3 = size_t(n_rays) * 3;
+    k_set_step_scalars<<<1, 1, 0, st>>>(m->g_scal, t.ss[0], t.ss[1], t.ss[2]);
+    PVDB_CHECK_LAUNCH("k_set_step_scalars");
+    const float* src[4] = {rays_o, rays_d, viewdirs, target};
+    for (int q = 0; q < 4; ++q)
+      PVDB_CHECK_CUDA(cudaMemcpyAsync(m->g_in + q * R3, src[q], R3 * 4, cudaMemcpyDeviceToDevice, st));
+    PVDB_CHECK_CUDA(cudaGraphLaunch(m->g_exec, st));
+    count_launches(int(m->g_launches));
+    PVDB_CHECK_CUDA(cudaMemcpyAsync(loss_out, m->g_scal + 4, 4, cudaMemcpyDeviceToDevice, st));
+  } else {
+    rc = train_launches(t, st);
+    if (rc) return rc;
+  }
   *net->lr *= cfg->lr_decay_factor;
   opt_lr_scale(density_opt, cfg->lr_decay_factor);
   opt_lr_scale(k0_opt, cfg->lr_decay_factor);

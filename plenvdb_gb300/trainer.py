@@ -44,6 +44,7 @@ class FineStageConfig:
     tv_weight: float = 1e-4
     tv_dense_mode: bool = False
     precision: int = 0              # 0 FP32 SIMT rgbnet, 1 BF16 tensor cores
+    use_graph: bool = True          # replay the fused step as a captured CUDA graph
 
     @property
     def voxel_size(self) -> float:
@@ -94,6 +95,7 @@ class FineStageTrainer:
         self.tc.rgbnet_beta1, self.tc.rgbnet_beta2 = cfg.betas
         self.tc.rgbnet_eps = cfg.eps
         self.tc.precision = cfg.precision
+        self.tc.use_graph = int(cfg.use_graph)
         self.loss = torch.zeros(1, device="cuda")
         # gradients start clean
         density.zero_grad()

@@ -227,3 +227,36 @@ def test_fused_train_loss_decreases_and_is_deterministic(setup):
     assert runs[0][0] == runs[1][0]
     assert np.array_equal(runs[0][1], runs[1][1])
     assert np.array_equal(runs[0][2], runs[1][2])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_eager_steps(setup, precision):
+    """The CUDA-graph replay of the fused step gives bitwise the same losses,
+    grids, moments and rgbnet weights as eager launches, across steps with
+    changing ray batches (the batch is staged into the graph's inputs)."""
+    import copy
+    import torch
+    from plenvdb_gb300.scene import build_grids, rgbnet_init
+    from plenvdb_gb300.trainer import FineStageTrainer
+    s = setup
+    ro, rd, vd = (torch.from_numpy(a).cuda() for a in (s["ro"], s["rd"], s["vd"]))
+    R = ro.shape[0]
+    g = torch.Generator().manual_seed(9)
+    batches = []
+    for b in range(4):
+        perm = torch.randperm(R, generator=g).cuda()
+        tgt = torch.rand(R, 3, generator=g).cuda()
+        batches.append((ro[perm].contiguous(), rd[perm].contiguous(), vd[perm].contiguous(), tgt))
+    runs = []
+    for use_graph in (False, True):
+        cfg = copy.copy(s["cfg"])
+        cfg.precision, cfg.use_graph = precision, use_graph
+        dg, kg = build_grids(s["scfg"])
+        tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), cfg, max_rays=1024)
+        losses = [float(tr.step(*batches[i % 4])) for i in range(12)]
+        runs.append((losses, dg.get_dense_grid(), kg.get_dense_grid(), tr.params.cpu().numpy(),
+                     tr.exp_avg_sq.cpu().numpy(), tr._lr.value, tr._step.value))
+    eager, graph = runs
+    assert eager[0] == graph[0]
+    for a, b in zip(eager[1:], graph[1:]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))

@@ -141,7 +141,7 @@ int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys, con
  * memory budget, and callers that cannot afford the device-wide
  * synchronisation of cudaMalloc/cudaFree. No counterpart in the reference.
  * The call allocates nothing: its scratch is one fixed file-scope device array
- * (about 4.3 MB, held on every GPU that loads the library until exit) that
+ * (about 5.3 MB, held on every GPU that loads the library until exit) that
  * limits a call to n <= 32768 points (PVDB_ERR_ARG beyond that). The first
  * call on a device looks up that array's address (cudaGetSymbolAddress); make
  * it before any stream capture. All calls share the array, so calls that

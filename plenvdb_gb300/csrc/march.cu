@@ -641,7 +641,8 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
   int buf = 0;
-  rc = radix_sort_pairs_dev(m->red, nmax, m->w.totals + 0, slot_key_bits(ncells), true, &buf, st);
+  rc = radix_sort_pairs_dev(m->red, nmax, m->w.totals + 0, slot_key_bits(ncells), true, &buf, st,
+                            m->w.totals + 3);
   if (rc) return rc;
   if (m->prof) prof_mark(st, 7);
   const uint32_t* skeys = m->red.keys[buf];
@@ -792,6 +793,7 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
   if (total_rows) *total_rows = t[1];
   if (t[3] & 1u) return set_error(PVDB_ERR_STATE, "a ray had more samples than samples_cap");
   if (t[3] & 2u) return set_error(PVDB_ERR_TIMEOUT, "a tensor-core MMA wait timed out");
+  if (t[3] & 4u) return set_error(PVDB_ERR_TIMEOUT, "a radix-sort look-back wait timed out");
   return PVDB_OK;
 }
 

@@ -417,8 +417,8 @@ static int mlp_reserve(pvdb_march_s* m, int din) {
 
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
-                        const int32_t* ray, const float* hpe, const uint32_t* totals, float* out,
-                        int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
+                        const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
+                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
                         cudaStream_t st);
 
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
@@ -433,7 +433,7 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
-                               m->w.r_ray, hpe, m->w.totals, rgb, 0, &m->mlp_packed,
+                               m->w.r_ray, pe, kMaxPe, m->w.totals, rgb, 0, &m->mlp_packed,
                                &m->mlp_packed_cap, m->w.totals + 3, st);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
@@ -454,8 +454,8 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
   k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
-    return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, hpe,
-                               totals, out, out_logits, blob, blob_cap, err, st);
+    return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
+                               kMaxPe, totals, out, out_logits, blob, blob_cap, err, st);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
                                                                   out, out_logits);
@@ -465,7 +465,7 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
 
 int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                          const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
-                         const int32_t* ray, const float* hpe, const float* pe, int pe_stride,
+                         const int32_t* ray, const float* pe, int pe_stride,
                          const uint32_t* totals, const float* rgb, const float* grad_rgb,
                          float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
                          uint32_t* err, cudaStream_t st);
@@ -485,7 +485,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
   const int G = mlp_grid();
   if (precision == 1) {
     rc = mlp_tc_backward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, m->w.r_ray,
-                              m->hpe, m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, rgb,
+                              m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, rgb,
                               grad_rgb, grad_k0, m->wpart, G, &m->mlp_packed, &m->mlp_packed_cap,
                               m->w.totals + 3, st);
     if (rc) return rc;

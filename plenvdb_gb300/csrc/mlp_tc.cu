@@ -2,18 +2,20 @@
 // accumulation in TMEM — the BF16 path of the colour MLP (dvgo.py:99-107,
 // :354-362; renderer.cu:83-119).
 //
-// Forward, per 128-row tile (one CTA, 8 warps, persistent over tiles, 2 CTAs
-// per SM, 256 TMEM columns each):
-//   L0  Z0 = X[128x16] . W0k^T          one MMA (K=16; k0's 12 channels padded)
-//       H0 = relu(Z0 + hpe[ray])         epilogue (hpe = W0[:,k0:]·PE + b0 per ray)
-//   L1  Z1 = H0[128x128] . W1^T          8 MMAs (K=128 in steps of 16)
-//       H1 = relu(Z1 + b1)               epilogue, written over H0
-//   L2  Z2 = H1 . W2p^T                  8 MMAs, N=16 (3 outputs padded)
-//       rgb = sigmoid(Z2 + b2)           epilogue (or the raw logits)
-// One thread issues the MMAs; completion is signalled through an mbarrier
-// (tcgen05.commit). Epilogues read TMEM with tcgen05.ld (warp w reads lanes
-// 32*(w%4).., columns 64*(w/4)..), apply bias/activation in FP32 and store
-// BF16 into shared memory in the canonical layout the next MMA reads.
+// Rows are processed in tiles of 128 (TMEM lane = tile row). Each row's input
+// is X = [k0 (c0) | PE (dpe) | 1 | 0...], 48 BF16 columns, so layer 0 is one
+// K=48 GEMM against W0f = [W0 | b0 | 0] (the bias rides on the ones column).
+//
+// Forward (k_mlp_fwd_tc: persistent CTAs, 8 warps, 2 CTAs per SM, 256 TMEM
+// columns each):
+//   L0  Z0 = X . W0f^T            3 MMAs (K=48)        H0 = relu(Z0)
+//   L1  Z1 = H0 . W1^T            8 MMAs (K=128)       H1 = relu(Z1 + b1)
+//   L2  Z2 = H1 . W2p^T           8 MMAs, N=16         rgb = sigmoid(Z2 + b2)
+// The next tile's X is loaded into registers while the current tile's MMAs
+// run. One thread issues the MMAs; completion is signalled through an
+// mbarrier (tcgen05.commit). Epilogues read TMEM with tcgen05.ld (warp w reads
+// lanes 32*(w%4).., columns 64*(w/4)..), apply bias/activation in FP32 and
+// store BF16 into shared memory in the canonical layout the next MMA reads.
 #include <algorithm>
 
 #include "march.cuh"
@@ -25,24 +27,26 @@ namespace {
 
 constexpr int kW = 128;
 constexpr int kTcThreads = 256;
-// packed weight blob (bytes): W0k [128x16] | W1 [128x128] | W2p [16x128]
-constexpr uint32_t kOffW0 = 0;
-constexpr uint32_t kOffW1 = kOffW0 + 128 * 16 * 2;    // 4096
-constexpr uint32_t kOffW2 = kOffW1 + 128 * 128 * 2;   // 36864
-constexpr uint32_t kPackFwdBytes = kOffW2 + 16 * 128 * 2;  // 40960
-constexpr uint32_t kOffW1T = kPackFwdBytes;                // W1T [128x128]
-constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16x128]
-constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T [128x16]
-constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 81920
+constexpr int kXK = 48;  // input columns of a row: k0 | PE | 1 | 0
+// packed weight blob (bytes, canonical K-major BF16 tiles)
+constexpr uint32_t kOffW0 = 0;                             // W0f  [128 n][48 q]
+constexpr uint32_t kOffW1 = kOffW0 + 128 * kXK * 2;        // W1   [128 n][128 k]   12288
+constexpr uint32_t kOffW2 = kOffW1 + 128 * 128 * 2;        // W2p  [16 c][128 k]    45056
+constexpr uint32_t kPackFwdBytes = kOffW2 + 16 * 128 * 2;  // 49152
+constexpr uint32_t kOffW1T = kPackFwdBytes;                // W1T  [128 k][128 n]
+constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16 q][128 n]    81920
+constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T  [128 n][16 c]    86016
+constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 90112
 // shared-memory layout of the forward kernel
-constexpr uint32_t kSmX = kPackFwdBytes;              // X tile [128x16] bf16
-constexpr uint32_t kSmH = kSmX + 128 * 16 * 2;        // H tile [128x128] bf16
+constexpr uint32_t kSmX = kPackFwdBytes;              // X tile [128 x 48] bf16
+constexpr uint32_t kSmH = kSmX + 128 * kXK * 2;       // H tile [128 x 128] bf16
 constexpr uint32_t kSmB1 = kSmH + 128 * 128 * 2;      // b1 f32[128]
 constexpr uint32_t kSmB2 = kSmB1 + 128 * 4;           // b2 f32[16]
 constexpr uint32_t kSmBar = kSmB2 + 16 * 4;           // mbarrier (8 B)
 constexpr uint32_t kSmTmem = kSmBar + 8;              // TMEM base address (4 B)
 constexpr uint32_t kSmFlag = kSmTmem + 4;             // timeout flag (4 B)
 constexpr uint32_t kSmFwdBytes = kSmFlag + 16;
+static_assert(2 * kSmFwdBytes <= 228 * 1024, "two forward CTAs must fit on an SM");
 constexpr uint32_t kTmemCols = 256;
 constexpr uint32_t kWaitIters = 1u << 22;
 
@@ -61,9 +65,10 @@ __global__ void k_pack(MlpArgsTc a, uint8_t* blob, int with_bwd) {
   __nv_bfloat16* w0 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0);
   __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1);
   __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW2);
-  if (t < 128 * 16) {  // W0k[n][k] = w0[n][k] for k < c0, 0 otherwise
-    const int n = t / 16, k = t % 16;
-    w0[tc::kmaj(n, k, 16) / 2] = __float2bfloat16_rn(k < a.c0 ? a.w0[n * a.din + k] : 0.f);
+  if (t < 128 * kXK) {  // W0f[n][q] = w0[n][q] (q < din), b0[n] (q == din), 0
+    const int n = t / kXK, q = t % kXK;
+    const float v = q < a.din ? a.w0[n * a.din + q] : q == a.din ? a.b0[n] : 0.f;
+    w0[tc::kmaj(n, q, kXK) / 2] = __float2bfloat16_rn(v);
   }
   if (t < 128 * 128) {
     const int n = t / 128, k = t % 128;
@@ -101,9 +106,72 @@ __device__ __forceinline__ bool wait_or_flag(uint64_t* bar, uint32_t parity, uin
   return *((volatile uint32_t*)flag) == 0;
 }
 
+// The X chunks of one tile held by one thread: chunk tid + 256*i (i < 3) is
+// row (chunk / 6), columns 8*(chunk % 6) .. +7.
+struct XRegs {
+  float v[3][8];
+};
+
+__device__ __forceinline__ void x_load(const MlpArgsTc& a, const float* __restrict__ k0,
+                                       const int32_t* __restrict__ ray,
+                                       const float* __restrict__ pe, int pe_stride, int64_t row0,
+                                       int64_t M, XRegs& x) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int c = threadIdx.x + kTcThreads * i;
+    const int r = c / 6, qb = (c % 6) * 8;
+    const int64_t m = row0 + r;
+    if (m < M) {
+      const int64_t rr = __ldg(ray + m);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int qq = qb + e;
+        x.v[i][e] = qq < a.c0 ? __ldg(k0 + m * a.c0 + qq)
+                    : qq < a.din ? __ldg(pe + rr * pe_stride + (qq - a.c0))
+                    : qq == a.din ? 1.f : 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x.v[i][e] = 0.f;
+    }
+  }
+}
+
+__device__ __forceinline__ void x_store(uint8_t* xs, const XRegs& x) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int c = threadIdx.x + kTcThreads * i;
+    const int r = c / 6, qb = (c % 6) * 8;
+    uint4 pk;
+    pk.x = tc::pack_bf16(x.v[i][0], x.v[i][1]);
+    pk.y = tc::pack_bf16(x.v[i][2], x.v[i][3]);
+    pk.z = tc::pack_bf16(x.v[i][4], x.v[i][5]);
+    pk.w = tc::pack_bf16(x.v[i][6], x.v[i][7]);
+    *reinterpret_cast<uint4*>(xs + tc::kmaj(r, qb, kXK)) = pk;
+  }
+}
+
+// 32 FP32 values (+ bias, relu) -> 4 x 8 BF16 into a K-major tile (ktot columns).
+__device__ __forceinline__ void store_relu32(uint8_t* tile, int row, int col0, int ktot,
+                                             const float* v, const float* bias) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int o = 8 * c;
+    float h[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[o + e] + (bias ? bias[col0 + o + e] : 0.f), 0.f);
+    uint4 pk;
+    pk.x = tc::pack_bf16(h[0], h[1]);
+    pk.y = tc::pack_bf16(h[2], h[3]);
+    pk.z = tc::pack_bf16(h[4], h[5]);
+    pk.w = tc::pack_bf16(h[6], h[7]);
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(row, col0 + o, ktot)) = pk;
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 2)
     k_mlp_fwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const float* __restrict__ k0,
-                 const int32_t* __restrict__ ray, const float* __restrict__ hpe,
+                 const int32_t* __restrict__ ray, const float* __restrict__ pe, int pe_stride,
                  const uint32_t* __restrict__ totals, float* out, int out_logits, uint32_t* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
@@ -115,7 +183,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kSmFlag);
   float* b1s = reinterpret_cast<float*>(sm + kSmB1);
   float* b2s = reinterpret_cast<float*>(sm + kSmB2);
-  // weights: 16-byte copies of the packed blob
   {
     const int4* src = reinterpret_cast<const int4*>(blob);
     int4* dst = reinterpret_cast<int4*>(sm);
@@ -143,93 +210,33 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const uint32_t t_lane = tmem + (uint32_t(32 * q) << 16);
   uint32_t phase = 0;
   bool ok = true;
+  XRegs xr;
+  x_load(a, k0, ray, pe, pe_stride, int64_t(blockIdx.x) * 128, M, xr);
   for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     const int64_t row0 = t * 128;
-    // ---- X tile: row = tid/2, k = 8*(tid&1) .. +7
-    {
-      const int r = tid >> 1, kb = (tid & 1) * 8;
-      const int64_t m = row0 + r;
-      float v[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = (m < M && kb + i < a.c0) ? k0[m * a.c0 + kb + i] : 0.f;
-      uint4 pk;
-      pk.x = tc::pack_bf16(v[0], v[1]);
-      pk.y = tc::pack_bf16(v[2], v[3]);
-      pk.z = tc::pack_bf16(v[4], v[5]);
-      pk.w = tc::pack_bf16(v[6], v[7]);
-      *reinterpret_cast<uint4*>(sm + kSmX + tc::kmaj(r, kb, 16)) = pk;
-    }
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      tc::mma_bf16(tmem, tc::make_desc(sbase + kSmX, 128, 256), tc::make_desc(sbase + kOffW0, 128, 256),
-                   id_n128, 0);
-      tc::mma_commit(bar);
-    }
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
-    if (!ok) break;
-    tc::fence_after();
-    // ---- epilogue 0: H0 = relu(Z0 + hpe[ray])
-    {
-      const int64_t m = row0 + row;
-      const bool valid = m < M;
-      const float* hp = hpe + int64_t(valid ? ray[m] : 0) * kW + 64 * half;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        float v[16];
-        tc::tmem_ld16(t_lane + uint32_t(64 * half + 16 * j), v);
-        float hv[16];
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 h4 = valid ? __ldg(reinterpret_cast<const float4*>(hp + 16 * j + i))
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-          hv[i] = h4.x; hv[i + 1] = h4.y; hv[i + 2] = h4.z; hv[i + 3] = h4.w;
-        }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          uint4 pk;
-          const int o = 8 * c;
-          pk.x = tc::pack_bf16(fmaxf(v[o] + hv[o], 0.f), fmaxf(v[o + 1] + hv[o + 1], 0.f));
-          pk.y = tc::pack_bf16(fmaxf(v[o + 2] + hv[o + 2], 0.f), fmaxf(v[o + 3] + hv[o + 3], 0.f));
-          pk.z = tc::pack_bf16(fmaxf(v[o + 4] + hv[o + 4], 0.f), fmaxf(v[o + 5] + hv[o + 5], 0.f));
-          pk.w = tc::pack_bf16(fmaxf(v[o + 6] + hv[o + 6], 0.f), fmaxf(v[o + 7] + hv[o + 7], 0.f));
-          *reinterpret_cast<uint4*>(sm + kSmH + tc::kmaj(row, 64 * half + 16 * j + o, 128)) = pk;
-        }
-      }
-    }
-    tc::fence_before();
+    x_store(sm + kSmX, xr);
     tc::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc::fence_after();
 #pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem, tc::make_desc(sbase + kSmH + 256 * s, 128, 2048),
-                     tc::make_desc(sbase + kOffW1 + 256 * s, 128, 2048), id_n128, s > 0);
+      for (int s = 0; s < 3; ++s)
+        tc::mma_bf16(tmem, tc::make_desc(sbase + kSmX + 256 * s, 128, 768),
+                     tc::make_desc(sbase + kOffW0 + 256 * s, 128, 768), id_n128, s > 0);
       tc::mma_commit(bar);
     }
+    // the next tile's inputs travel while this tile computes
+    if (t + gridDim.x < ntiles) x_load(a, k0, ray, pe, pe_stride, (t + gridDim.x) * 128, M, xr);
     ok = wait_or_flag(bar, phase, flag, err);
     phase ^= 1;
     if (!ok) break;
     tc::fence_after();
-    // ---- epilogue 1: H1 = relu(Z1 + b1), over H0
+    // ---- H0 = relu(Z0)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      float v[16];
-      tc::tmem_ld16(t_lane + uint32_t(64 * half + 16 * j), v);
-      const int cb = 64 * half + 16 * j;
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        uint4 pk;
-        const int o = 8 * c;
-        pk.x = tc::pack_bf16(fmaxf(v[o] + b1s[cb + o], 0.f), fmaxf(v[o + 1] + b1s[cb + o + 1], 0.f));
-        pk.y = tc::pack_bf16(fmaxf(v[o + 2] + b1s[cb + o + 2], 0.f), fmaxf(v[o + 3] + b1s[cb + o + 3], 0.f));
-        pk.z = tc::pack_bf16(fmaxf(v[o + 4] + b1s[cb + o + 4], 0.f), fmaxf(v[o + 5] + b1s[cb + o + 5], 0.f));
-        pk.w = tc::pack_bf16(fmaxf(v[o + 6] + b1s[cb + o + 6], 0.f), fmaxf(v[o + 7] + b1s[cb + o + 7], 0.f));
-        *reinterpret_cast<uint4*>(sm + kSmH + tc::kmaj(row, cb + o, 128)) = pk;
-      }
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      tc::tmem_ld32(t_lane + uint32_t(64 * half + 32 * j), v);
+      store_relu32(sm + kSmH, row, 64 * half + 32 * j, 128, v, nullptr);
     }
     tc::fence_before();
     tc::fence_async_smem();
@@ -239,6 +246,28 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 #pragma unroll
       for (int s = 0; s < 8; ++s)
         tc::mma_bf16(tmem + 128, tc::make_desc(sbase + kSmH + 256 * s, 128, 2048),
+                     tc::make_desc(sbase + kOffW1 + 256 * s, 128, 2048), id_n128, s > 0);
+      tc::mma_commit(bar);
+    }
+    ok = wait_or_flag(bar, phase, flag, err);
+    phase ^= 1;
+    if (!ok) break;
+    tc::fence_after();
+    // ---- H1 = relu(Z1 + b1), over H0
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      tc::tmem_ld32(t_lane + 128u + uint32_t(64 * half + 32 * j), v);
+      store_relu32(sm + kSmH, row, 64 * half + 32 * j, 128, v, b1s);
+    }
+    tc::fence_before();
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(tmem, tc::make_desc(sbase + kSmH + 256 * s, 128, 2048),
                      tc::make_desc(sbase + kOffW2 + 256 * s, 128, 2048), id_n16, s > 0);
       tc::mma_commit(bar);
     }
@@ -246,10 +275,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     phase ^= 1;
     if (!ok) break;
     tc::fence_after();
-    // ---- epilogue 2: logits (warps 0-3 hold all 16 columns of their rows)
+    // ---- logits (warps 0-3 hold all 16 columns of their rows)
     if (half == 0) {
       float v[16];
-      tc::tmem_ld16(t_lane + 128u, v);
+      tc::tmem_ld16(t_lane, v);
       const int64_t m = row0 + row;
       if (m < M) {
 #pragma unroll
@@ -271,15 +300,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-
 // ---------------------------------------------------------------- backward
 // Per 128-row tile (one CTA per SM, persistent, all 512 TMEM columns):
-//   recompute  Z0 = X.W0k^T -> H0 = relu(Z0 + hpe);  Z1 = H0.W1^T -> H1 = relu(Z1 + b1)
+//   recompute  Z0 = X.W0f^T -> H0 = relu(Z0);  Z1 = H0.W1^T -> H1 = relu(Z1 + b1)
 //   dl   = grad_rgb * y (1 - y)                       [128 x 3] (sigmoid backward)
 //   dZ1  = (dl . W2) * [H1 > 0]                       MMA K=16 (W2T)
 //   dZ0  = (dZ1 . W1) * [H0 > 0]                      MMA K=128 (W1T)
 //   gk0  = dZ0 . W0k                                  MMA N=16 (W0kT)
-//   dW2 += H1^T . dl      dW1|db1 += dZ1^T . [H0|1]   dW0|db0 += dZ0^T . [k0|PE|1]
+//   dW2 += H1^T . dl      dW1|db1 += dZ1^T . [H0|1]   dW0|db0 += dZ0^T . X
 // The three weight-gradient accumulators stay in TMEM across all tiles of the
 // CTA (a ones column in H0 and in X turns the bias sums into one more MMA
 // column); the transposed operands are the same shared-memory tiles read
@@ -288,16 +316,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 // are summed over CTAs in a fixed order, so the result is deterministic.
 //
 // Shared memory (bytes). The tiles read through MN-major descriptors come
-// first and the weights (77824 B) last.
+// first and the weights (86016 B) last. dZ0 reuses H1's buffer: H1's last
+// readers (the dW2 MMA and the dZ1 mask) are done before dZ0 is written.
 constexpr uint32_t kBdZ1 = 0;                        // dZ1 [128 r][128 n]
-constexpr uint32_t kBdZ0 = kBdZ1 + 128 * 128 * 2;    // dZ0 [128 r][128 n]
-constexpr uint32_t kBH1 = kBdZ0 + 128 * 128 * 2;     // H1  [128 r][128 n]
+constexpr uint32_t kBH1 = kBdZ1 + 128 * 128 * 2;     // H1, later dZ0 [128 r][128 n]
+constexpr uint32_t kBdZ0 = kBH1;
 constexpr uint32_t kBH0 = kBH1 + 128 * 128 * 2;      // H0  [128 r][144 k], col 128 = 1
 constexpr uint32_t kBX = kBH0 + 128 * 144 * 2;       // X   [128 r][48 q]: k0 | PE | 1 | 0
-constexpr uint32_t kBDl = kBX + 128 * 48 * 2;        // dl  [128 r][16 c]
+constexpr uint32_t kBDl = kBX + 128 * kXK * 2;       // dl  [128 r][16 c]
 constexpr uint32_t kBW = kBDl + 128 * 16 * 2;        // weights
-constexpr uint32_t kBW0k = kBW;                      // W0k  [128 n][16 q]
-constexpr uint32_t kBW1 = kBW0k + 128 * 16 * 2;      // W1   [128 n][128 k]
+constexpr uint32_t kBW0f = kBW;                      // W0f  [128 n][48 q]
+constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;     // W1   [128 n][128 k]
 constexpr uint32_t kBW1T = kBW1 + 128 * 128 * 2;     // W1T  [128 k][128 n]
 constexpr uint32_t kBW0T = kBW1T + 128 * 128 * 2;    // W0kT [16 q][128 n]
 constexpr uint32_t kBW2T = kBW0T + 16 * 128 * 2;     // W2T  [128 n][16 c]
@@ -307,6 +336,8 @@ constexpr uint32_t kBTmem = kBBar + 8;
 constexpr uint32_t kBFlag = kBTmem + 4;
 constexpr uint32_t kSmBwdBytes = kBFlag + 12;
 static_assert(kSmBwdBytes <= 232448, "backward tile exceeds 227 KB of shared memory");
+static_assert(kBW2T + 128 * 16 * 2 - kBW == (kOffW2 - kOffW0) + (kPackAllBytes - kOffW1T),
+              "backward weight region must hold W0f, W1, W1T, W0kT, W2T");
 // TMEM columns
 constexpr uint32_t kTA = 0;      // Z0, then dZ1 (pre-mask)
 constexpr uint32_t kTB = 128;    // Z1, then dH0
@@ -337,10 +368,9 @@ __device__ __forceinline__ uint4 mask_pack(const float* v, uint4 h) {
 
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_mlp_bwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const float* __restrict__ k0,
-                 const int32_t* __restrict__ ray, const float* __restrict__ hpe,
-                 const float* __restrict__ pe, int pe_stride, const uint32_t* __restrict__ totals,
-                 const float* __restrict__ rgb, const float* __restrict__ grad_rgb,
-                 float* grad_k0, float* wpart, uint32_t* err) {
+                 const int32_t* __restrict__ ray, const float* __restrict__ pe, int pe_stride,
+                 const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
+                 const float* __restrict__ grad_rgb, float* grad_k0, float* wpart, uint32_t* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
   const int64_t ntiles = (M + 127) / 128;
@@ -363,7 +393,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   {
     const int4* src = reinterpret_cast<const int4*>(blob);
     int4* dst = reinterpret_cast<int4*>(sm + kBW);
-    // W0k, W1 (blob 0..36864) and W1T, W0kT, W2T (blob 40960..81920)
+    // W0f, W1 (blob 0..45056) and W1T, W0kT, W2T (blob 49152..90112)
     for (int i = tid; i < int(kOffW2 / 16); i += kTcThreads) dst[i] = __ldg(src + i);
     for (int i = tid; i < int((kPackAllBytes - kOffW1T) / 16); i += kTcThreads)
       dst[kOffW2 / 16 + i] = __ldg(src + kOffW1T / 16 + i);
@@ -399,74 +429,42 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   float db2[3] = {0.f, 0.f, 0.f};
   uint32_t phase = 0;
   bool ok = true, first = true;
+  XRegs xr;
+  x_load(a, k0, ray, pe, pe_stride, int64_t(blockIdx.x) * 128, M, xr);
   for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     const int64_t row0 = t * 128;
-    // ---- X tile [k0 | PE | 1 | 0]: 6 chunks of 8 columns per row
-    for (int c = tid; c < 128 * 6; c += kTcThreads) {
-      const int r = c / 6, qb = (c % 6) * 8;
-      const int64_t m = row0 + r;
-      float v[8];
-      if (m < M) {
-        const int64_t rr = ray[m];
+    const int64_t mrow = row0 + row;
+    // sigmoid inputs of this thread's row (warps 0-3), read early
+    float yv[3] = {0.f, 0.f, 0.f}, gv[3] = {0.f, 0.f, 0.f};
+    if (half == 0 && mrow < M) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int qq = qb + i;
-          v[i] = qq < a.c0 ? k0[m * a.c0 + qq]
-                 : qq < a.din ? pe[rr * pe_stride + (qq - a.c0)]
-                 : qq == a.din ? 1.f : 0.f;
-        }
-      } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = 0.f;
+      for (int c = 0; c < 3; ++c) {
+        yv[c] = __ldg(rgb + mrow * 3 + c);
+        gv[c] = __ldg(grad_rgb + mrow * 3 + c);
       }
-      uint4 pk;
-      pk.x = tc::pack_bf16(v[0], v[1]);
-      pk.y = tc::pack_bf16(v[2], v[3]);
-      pk.z = tc::pack_bf16(v[4], v[5]);
-      pk.w = tc::pack_bf16(v[6], v[7]);
-      *reinterpret_cast<uint4*>(sm + kBX + tc::kmaj(r, qb, 48)) = pk;
     }
+    x_store(sm + kBX, xr);
     tc::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc::fence_after();
-      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX, 128, 768),
-                   tc::make_desc(sb + kBW0k, 128, 256), id_r128, 0);
+#pragma unroll
+      for (int s = 0; s < 3; ++s)
+        tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX + 256 * s, 128, 768),
+                     tc::make_desc(sb + kBW0f + 256 * s, 128, 768), id_r128, s > 0);
       tc::mma_commit(bar);
     }
+    if (t + gridDim.x < ntiles) x_load(a, k0, ray, pe, pe_stride, (t + gridDim.x) * 128, M, xr);
     ok = wait_or_flag(bar, phase, flag, err);
     phase ^= 1;
     if (!ok) break;
     tc::fence_after();
-    // ---- H0 = relu(Z0 + hpe[ray])
-    {
-      const int64_t m = row0 + row;
-      const bool valid = m < M;
-      const float* hp = hpe + int64_t(valid ? ray[m] : 0) * kW + 64 * half;
+    // ---- H0 = relu(Z0)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        float v[16];
-        tc::tmem_ld16(t_lane + kTA + uint32_t(64 * half + 16 * j), v);
-#pragma unroll
-        for (int i = 0; i < 16; i += 4) {
-          const float4 h4 = valid ? __ldg(reinterpret_cast<const float4*>(hp + 16 * j + i))
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-          v[i] = fmaxf(v[i] + h4.x, 0.f);
-          v[i + 1] = fmaxf(v[i + 1] + h4.y, 0.f);
-          v[i + 2] = fmaxf(v[i + 2] + h4.z, 0.f);
-          v[i + 3] = fmaxf(v[i + 3] + h4.w, 0.f);
-        }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          const int o = 8 * c;
-          uint4 pk;
-          pk.x = tc::pack_bf16(v[o], v[o + 1]);
-          pk.y = tc::pack_bf16(v[o + 2], v[o + 3]);
-          pk.z = tc::pack_bf16(v[o + 4], v[o + 5]);
-          pk.w = tc::pack_bf16(v[o + 6], v[o + 7]);
-          *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(row, 64 * half + 16 * j + o, 144)) = pk;
-        }
-      }
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      tc::tmem_ld32(t_lane + kTA + uint32_t(64 * half + 32 * j), v);
+      store_relu32(sm + kBH0, row, 64 * half + 32 * j, 144, v, nullptr);
     }
     tc::fence_before();
     tc::fence_async_smem();
@@ -485,31 +483,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc::fence_after();
     // ---- H1 = relu(Z1 + b1); dl = grad_rgb * y * (1 - y)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      float v[16];
-      const int cb = 64 * half + 16 * j;
-      tc::tmem_ld16(t_lane + kTB + uint32_t(cb), v);
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int o = 8 * c;
-        uint4 pk;
-        pk.x = tc::pack_bf16(fmaxf(v[o] + b1s[cb + o], 0.f), fmaxf(v[o + 1] + b1s[cb + o + 1], 0.f));
-        pk.y = tc::pack_bf16(fmaxf(v[o + 2] + b1s[cb + o + 2], 0.f), fmaxf(v[o + 3] + b1s[cb + o + 3], 0.f));
-        pk.z = tc::pack_bf16(fmaxf(v[o + 4] + b1s[cb + o + 4], 0.f), fmaxf(v[o + 5] + b1s[cb + o + 5], 0.f));
-        pk.w = tc::pack_bf16(fmaxf(v[o + 6] + b1s[cb + o + 6], 0.f), fmaxf(v[o + 7] + b1s[cb + o + 7], 0.f));
-        *reinterpret_cast<uint4*>(sm + kBH1 + tc::kmaj(row, cb + o, 128)) = pk;
-      }
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      tc::tmem_ld32(t_lane + kTB + uint32_t(64 * half + 32 * j), v);
+      store_relu32(sm + kBH1, row, 64 * half + 32 * j, 128, v, b1s);
     }
     if (half == 0) {
-      const int64_t m = row0 + row;
-      float d[3] = {0.f, 0.f, 0.f};
-      if (m < M) {
+      float d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float y = rgb[m * 3 + c];
-          d[c] = grad_rgb[m * 3 + c] * (1.f - y) * y;
-          db2[c] += d[c];
-        }
+      for (int c = 0; c < 3; ++c) {
+        d[c] = gv[c] * (1.f - yv[c]) * yv[c];
+        db2[c] += d[c];
       }
       *reinterpret_cast<uint4*>(sm + kBDl + tc::kmaj(row, 0, 16)) =
           make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
@@ -536,12 +520,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc::fence_after();
     // ---- dZ1 = (dl . W2) * [H1 > 0]
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      float v[16];
-      const int cb = 64 * half + 16 * j;
-      tc::tmem_ld16(t_lane + kTA + uint32_t(cb), v);
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      const int cb = 64 * half + 32 * j;
+      tc::tmem_ld32(t_lane + kTA + uint32_t(cb), v);
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
+      for (int c = 0; c < 4; ++c) {
         const uint32_t off = tc::kmaj(row, cb + 8 * c, 128);
         const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH1 + off);
         *reinterpret_cast<uint4*>(sm + kBdZ1 + off) = mask_pack(v + 8 * c, h);
@@ -568,14 +552,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     phase ^= 1;
     if (!ok) break;
     tc::fence_after();
-    // ---- dZ0 = dH0 * [H0 > 0]
+    // ---- dZ0 = dH0 * [H0 > 0]  (into H1's buffer)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      float v[16];
-      const int cb = 64 * half + 16 * j;
-      tc::tmem_ld16(t_lane + kTB + uint32_t(cb), v);
+    for (int j = 0; j < 2; ++j) {
+      float v[32];
+      const int cb = 64 * half + 32 * j;
+      tc::tmem_ld32(t_lane + kTB + uint32_t(cb), v);
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
+      for (int c = 0; c < 4; ++c) {
         const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH0 + tc::kmaj(row, cb + 8 * c, 144));
         *reinterpret_cast<uint4*>(sm + kBdZ0 + tc::kmaj(row, cb + 8 * c, 128)) = mask_pack(v + 8 * c, h);
       }
@@ -604,11 +588,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (half == 0) {
       float v[16];
       tc::tmem_ld16(t_lane + kTG, v);
-      const int64_t m = row0 + row;
-      if (m < M) {
+      if (mrow < M) {
 #pragma unroll
         for (int qq = 0; qq < 16; ++qq)
-          if (qq < a.c0) grad_k0[m * a.c0 + qq] = v[qq];
+          if (qq < a.c0) grad_k0[mrow * a.c0 + qq] = v[qq];
       }
     }
     first = false;
@@ -682,13 +665,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 }  // namespace
 
-// Packs the weights and runs the forward over rows k0rows [M, c0] (M = totals[1]).
+// Packs the weights and runs the forward over rows k0rows [M, c0] (M = totals[1]);
+// pe [rays, pe_stride] holds each ray's view-direction PE.
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
-                        const int32_t* ray, const float* hpe, const uint32_t* totals, float* out,
-                        int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
+                        const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
+                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
                         cudaStream_t st) {
-  if (c0 > 16) return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 channels");
+  if (c0 > 16 || c0 + dpe + 1 > kXK)
+    return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
   if (rc) return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
@@ -696,20 +681,21 @@ int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const
   PVDB_CHECK_LAUNCH("k_pack");
   PVDB_SMEM_ATTR(k_mlp_fwd_tc, int(kSmFwdBytes));
   k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
-      a, static_cast<const uint8_t*>(*blob), k0rows, ray, hpe, totals, out, out_logits, err);
+      a, static_cast<const uint8_t*>(*blob), k0rows, ray, pe, pe_stride, totals, out, out_logits,
+      err);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_tc");
   return PVDB_OK;
 }
 
 // Weight and k0 gradients of the rows k0rows [M, c0] (M = totals[1]); per-CTA
-// partials go to wpart (num_sms() x P floats), the caller sums them.
+// partials go to wpart (grid x P floats), the caller sums them.
 int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                          const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
-                         const int32_t* ray, const float* hpe, const float* pe, int pe_stride,
+                         const int32_t* ray, const float* pe, int pe_stride,
                          const uint32_t* totals, const float* rgb, const float* grad_rgb,
                          float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
                          uint32_t* err, cudaStream_t st) {
-  if (c0 > 16 || c0 + dpe + 1 > 48)
+  if (c0 > 16 || c0 + dpe + 1 > kXK)
     return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
   if (rc) return rc;
@@ -718,7 +704,7 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
   PVDB_CHECK_LAUNCH("k_pack");
   PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
   k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob), k0rows,
-                                                      ray, hpe, pe, pe_stride, totals, rgb, grad_rgb,
+                                                      ray, pe, pe_stride, totals, rgb, grad_rgb,
                                                       grad_k0, wpart, err);
   PVDB_CHECK_LAUNCH("k_mlp_bwd_tc");
   return PVDB_OK;

@@ -9,7 +9,7 @@
 // histograms, scan partials) in one fixed file-scope device array, so the call
 // itself allocates nothing. The caller still passes the points, the gradients
 // and the grid (device memory). The array holds kNoAllocMaxPoints points'
-// worth of scratch (about 4.3 MB) on every GPU that loads the library, until
+// worth of scratch (about 5.3 MB) on every GPU that loads the library, until
 // the process exits.
 #include <mutex>
 
@@ -19,9 +19,10 @@ namespace pvdb {
 
 constexpr int64_t kNoAllocMaxPoints = 32768;
 constexpr int64_t kNoAllocMaxPairs = kNoAllocMaxPoints * 8;
-constexpr int64_t kNoAllocTiles = (kNoAllocMaxPairs + 4095) / 4096;
-// radix histograms (256 per tile) plus the two size words written by the sort
-constexpr int64_t kNoAllocHistWords = kNoAllocTiles * 256 + 16;
+constexpr int64_t kNoAllocTiles = (kNoAllocMaxPairs + kRsTile - 1) / kRsTile;
+// radix sort scratch: tile status words of up to 4 digit passes, the digit
+// histograms, tile counters and a few scalars
+constexpr int64_t kNoAllocHistWords = 4 * kNoAllocTiles * kRsBins + 4 * kRsBins + 16;
 // scan partials of the histogram scan (one per 4096-entry tile)
 constexpr int64_t kNoAllocPartialWords = 64;
 constexpr int64_t kNoAllocWords = 4 * kNoAllocMaxPairs + kNoAllocHistWords + kNoAllocPartialWords;
@@ -108,6 +109,8 @@ extern "C" int pvdb_grid_sample_backward_noalloc(pvdb_grid g, const float* xs, c
   rs.partial = rs.hist + kNoAllocHistWords;
   rs.partial_cap = size_t(kNoAllocPartialWords) * 4;
   const int64_t nc = n * 8;
+  if (radix_sort_words(nc, slot_key_bits(g->nslots())) > kNoAllocHistWords)
+    return set_error(PVDB_ERR_STATE, "no-alloc scratch too small for the sort");
   k_noalloc_keys<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), xs, ys, zs, n, rs.keys[0]);
   PVDB_CHECK_LAUNCH("k_noalloc_keys");
   int buf = 0;

@@ -245,7 +245,9 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
 int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,
                      cudaStream_t st);
 int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
-                         bool iota_vals, int* out_buf, cudaStream_t st);
+                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t* err = nullptr);
+// Scratch words (rs.hist) the sort needs for n_max keys of key_bits bits.
+int radix_sort_words(int64_t n_max, int key_bits);
 
 int scratch_reserve(ReduceScratch& rs, int64_t n);
 void free_scratch(ReduceScratch& rs);

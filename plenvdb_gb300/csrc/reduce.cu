@@ -185,51 +185,102 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
 }
 
 // ------------------------------------------------------------- radix sort
-constexpr int kRsThreads = 256;
+// Stable LSD radix sort, 8-bit digits, one kernel per digit pass ("onesweep"):
+//   k_os_init     zeroes the per-pass tile status words, digit histograms and
+//                 tile counters for the tiles the device-side count needs;
+//   k_os_hist     builds the digit histograms of every pass in one read;
+//   k_os_scatter  per pass: CTAs take 1024-key tiles in order from a counter,
+//                 count the tile's digits, publish them, and find the tile's
+//                 exclusive prefix per digit by looking back over the earlier
+//                 tiles' published counts (decoupled look-back); then scatter
+//                 stably (tile order, and (warp, round, lane) = index order
+//                 inside a tile).
+// A tile publishes its own count before it waits on anyone, and a tile only
+// waits on tiles taken earlier (already running), so every wait ends; each is
+// still bounded, and one that gives up sets an error flag.
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsRounds = 16;                    // keys per lane
-constexpr int kRsTile = kRsThreads * kRsRounds;  // 4096 keys per tile
-constexpr int kRsBins = 256;
+constexpr uint32_t kOsAgg = 0x40000000u;     // status: tile count published
+constexpr uint32_t kOsPrefix = 0x80000000u;  // status: inclusive prefix published
+constexpr uint32_t kOsValue = 0x3FFFFFFFu;
+constexpr uint32_t kOsSpinMax = 1u << 24;
 
-// sizes[0] = n (contributions), sizes[1] = 256 * tiles (histogram length)
-__global__ void k_rs_sizes(int64_t n_max, const uint32_t* n_dev, uint32_t* sizes) {
-  const int64_t n = eff_size(n_max, n_dev);
-  sizes[0] = uint32_t(n);
-  sizes[1] = uint32_t(((n + kRsTile - 1) / kRsTile) * kRsBins);
+// Scratch words after the status array: ghist [npass][256], counters
+// [npass], n, error flag.
+struct OsLayout {
+  int64_t ntiles_max;
+  int npass;
+  int64_t status, ghist, counters, n, err, words;
+};
+static OsLayout os_layout(int64_t n_max, int npass) {
+  OsLayout L;
+  L.ntiles_max = (n_max + kRsTile - 1) / kRsTile;
+  L.npass = npass;
+  L.status = 0;
+  L.ghist = L.status + int64_t(npass) * L.ntiles_max * kRsBins;
+  L.counters = L.ghist + int64_t(npass) * kRsBins;
+  L.n = L.counters + npass;
+  L.err = L.n + 1;
+  L.words = L.err + 1;
+  return L;
 }
 
-__global__ void k_rs_upsweep(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ sizes,
-                             int shift, uint32_t* hist) {
-  __shared__ uint32_t h[kRsBins];
-  const int64_t n = sizes[0];
+__global__ void k_os_init(int64_t n_max, const uint32_t* n_dev, int npass, int64_t ntiles_max,
+                          uint32_t* scratch, OsLayout L) {
+  const int64_t n = eff_size(n_max, n_dev);
   const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const int64_t base = t * kRsTile;
-    for (int q = threadIdx.x; q < kRsTile; q += kRsThreads) {
-      const int64_t i = base + q;
-      if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    hist[int64_t(threadIdx.x) * ntiles + t] = h[threadIdx.x];
-    __syncthreads();
+  const int64_t per = ntiles * kRsBins;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < int64_t(npass) * per;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t p = i / per, r = i - p * per;
+    scratch[L.status + p * ntiles_max * kRsBins + r] = 0u;
+  }
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (t < int64_t(npass) * kRsBins) scratch[L.ghist + t] = 0u;
+  if (t < npass) scratch[L.counters + t] = 0u;
+  if (t == 0) scratch[L.n] = uint32_t(n);
+}
+
+__global__ void __launch_bounds__(kRsThreads)
+    k_os_hist(const uint32_t* __restrict__ keys, int npass, uint32_t* scratch, OsLayout L) {
+  __shared__ uint32_t h[4][kRsBins];
+  const int64_t n = scratch[L.n];
+  for (int q = threadIdx.x; q < 4 * kRsBins; q += blockDim.x) (&h[0][0])[q] = 0u;
+  __syncthreads();
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t k = keys[i];
+    for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int p = 0; p < npass; ++p) {
+    const uint32_t c = h[p][threadIdx.x];
+    if (c) atomicAdd(scratch + L.ghist + p * kRsBins + threadIdx.x, c);
   }
 }
 
-// Stable scatter: within a tile the order is (warp, round, lane) = index order.
-__global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                               const uint32_t* __restrict__ sizes, int shift,
-                               const uint32_t* __restrict__ offsets, uint32_t* kout,
-                               uint32_t* vout) {
+__global__ void __launch_bounds__(kRsThreads)
+    k_os_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, int pass,
+                 uint32_t* scratch, OsLayout L, uint32_t* kout, uint32_t* vout, uint32_t* err) {
   __shared__ uint32_t wh[kRsWarps][kRsBins];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t n = sizes[0];
+  __shared__ uint32_t gbase[kRsBins];
+  __shared__ uint32_t tile_s;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, d = threadIdx.x;
+  const int shift = 8 * pass;
+  const int64_t n = scratch[L.n];
   const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
+  volatile uint32_t* status = scratch + L.status + int64_t(pass) * L.ntiles_max * kRsBins;
   const unsigned lt = lanemask_lt();
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // bucket bases of this pass: exclusive scan of the digit histogram
+  {
+    uint32_t tot;
+    gbase[d] = block_exclusive_scan(scratch[L.ghist + pass * kRsBins + d], &tot);
+  }
+  for (;;) {
+    if (threadIdx.x == 0) tile_s = atomicAdd(scratch + L.counters + pass, 1u);
     for (int q = threadIdx.x; q < kRsWarps * kRsBins; q += kRsThreads) (&wh[0][0])[q] = 0;
     __syncthreads();
+    const int64_t t = tile_s;
+    if (t >= ntiles) break;
     const int64_t wbase = t * kRsTile + int64_t(w) * (kRsRounds * 32);
     uint32_t key[kRsRounds];
 #pragma unroll
@@ -237,20 +288,45 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
       const int64_t i = wbase + r * 32 + lane;
       key[r] = i < n ? kin[i] : 0u;
     }
-    // phase 1: per-warp digit histogram
+    // per-warp digit histogram
 #pragma unroll
     for (int r = 0; r < kRsRounds; ++r) {
       const bool valid = wbase + r * 32 + lane < n;
-      const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
-      if (valid && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+      const uint32_t dg = valid ? ((key[r] >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, dg);
+      if (valid && lane == __ffs(peers) - 1) wh[w][dg] += __popc(peers);
       __syncwarp();
     }
     __syncthreads();
-    // phase 2: per digit, exclusive offsets across warps plus the tile's global base
+    // thread d: tile count, publish, look back, publish the inclusive prefix
     {
-      const int d = threadIdx.x;  // kRsThreads == kRsBins
-      uint32_t run = offsets[int64_t(d) * ntiles + t];
+      uint32_t cnt = 0;
+#pragma unroll
+      for (int q = 0; q < kRsWarps; ++q) cnt += wh[q][d];
+      volatile uint32_t* my = status + t * kRsBins + d;
+      if (t == 0) {
+        *my = kOsPrefix | cnt;
+      } else {
+        *my = kOsAgg | cnt;
+      }
+      uint32_t acc = 0;
+      for (int64_t tt = t - 1; tt >= 0; --tt) {
+        uint32_t v = status[tt * kRsBins + d];
+        for (uint32_t it = 0; v == 0u; ++it) {
+          if (it >= kOsSpinMax) {
+            atomicOr(err, 4u);
+            v = kOsPrefix;  // give up: leave the positions wrong but finish
+            break;
+          }
+          v = status[tt * kRsBins + d];
+        }
+        acc += v & kOsValue;
+        if (v & kOsPrefix) break;
+      }
+      if (t > 0) *my = kOsPrefix | (acc + cnt);
+      // per-warp exclusive offsets of this digit
+      uint32_t run = gbase[d] + acc;
+#pragma unroll
       for (int q = 0; q < kRsWarps; ++q) {
         const uint32_t c = wh[q][d];
         wh[q][d] = run;
@@ -258,17 +334,17 @@ __global__ void k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t*
       }
     }
     __syncthreads();
-    // phase 3: stable ranks and scatter
+    // stable ranks and scatter
 #pragma unroll
     for (int r = 0; r < kRsRounds; ++r) {
       const int64_t i = wbase + r * 32 + lane;
       const bool valid = i < n;
-      const uint32_t d = valid ? ((key[r] >> shift) & 255u) : 256u;
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t dg = valid ? ((key[r] >> shift) & 255u) : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, dg);
       uint32_t pos = 0;
-      if (valid) pos = wh[w][d] + __popc(peers & lt);
+      if (valid) pos = wh[w][dg] + __popc(peers & lt);
       __syncwarp();
-      if (valid && lane == __ffs(peers) - 1) wh[w][d] += __popc(peers);
+      if (valid && lane == __ffs(peers) - 1) wh[w][dg] += __popc(peers);
       __syncwarp();
       if (valid) {
         kout[pos] = key[r];
@@ -286,43 +362,39 @@ int slot_key_bits(int64_t nslots) {
 }
 
 int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
-                         bool iota_vals, int* out_buf, cudaStream_t st) {
+                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t* err) {
   *out_buf = 0;
   if (n_max <= 0) return PVDB_OK;
-  const int64_t ntiles_max = (n_max + kRsTile - 1) / kRsTile;
-  int rc = dev_reserve((void**)&rs.hist, &rs.hist_cap, size_t(ntiles_max) * kRsBins * 4 + 64);
+  const int npass = (key_bits + 7) / 8;
+  if (npass < 1 || npass > 4) return set_error(PVDB_ERR_ARG, "radix sort takes 1..32 key bits");
+  const OsLayout L = os_layout(n_max, npass);
+  int rc = dev_reserve((void**)&rs.hist, &rs.hist_cap, size_t(L.words) * 4);
   if (rc) return rc;
-  uint32_t* sizes = rs.hist + ntiles_max * kRsBins;  // 2 scalars after the histogram
-  k_rs_sizes<<<1, 1, 0, st>>>(n_max, n_dev, sizes);
-  PVDB_CHECK_LAUNCH("k_rs_sizes");
-  const int grid = int(std::min<int64_t>(ntiles_max, int64_t(num_sms()) * 4));
+  uint32_t* sc = rs.hist;
+  uint32_t* errp = err ? err : sc + L.err;
+  const int g_init = int(std::min<int64_t>(
+      std::max<int64_t>(ceil_div(int64_t(npass) * L.ntiles_max * kRsBins, 256), 1),
+      int64_t(num_sms()) * 8));
+  k_os_init<<<g_init, 256, 0, st>>>(n_max, n_dev, npass, L.ntiles_max, sc, L);
+  PVDB_CHECK_LAUNCH("k_os_init");
+  const int g_hist = int(std::min<int64_t>(ceil_div(n_max, kRsThreads), int64_t(num_sms()) * 4));
+  k_os_hist<<<g_hist, kRsThreads, 0, st>>>(rs.keys[0], npass, sc, L);
+  PVDB_CHECK_LAUNCH("k_os_hist");
+  const int grid = int(std::min<int64_t>(L.ntiles_max, int64_t(num_sms()) * 4));
   int cur = 0;
-  bool first = true;
-  for (int shift = 0; shift < key_bits; shift += 8) {
-    k_rs_upsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur], sizes, shift, rs.hist);
-    PVDB_CHECK_LAUNCH("k_rs_upsweep");
-    // the histogram length is on the device; its host-side maximum assumes
-    // every slot is used, so a one-block scan over the actual length is the
-    // faster choice unless even the maximum is very long
-    if (ntiles_max * kRsBins <= (int64_t(1) << 23)) {
-      k_scan_single<<<1, kScan1Threads, 0, st>>>(rs.hist, rs.hist, ntiles_max * kRsBins,
-                                                 sizes + 1, nullptr);
-      PVDB_CHECK_LAUNCH("k_scan_single(hist)");
-    } else {
-      rc = scan_exclusive_u32_dev(rs.hist, rs.hist, ntiles_max * kRsBins, sizes + 1, nullptr,
-                                  &rs.partial, &rs.partial_cap, st);
-      if (rc) return rc;
-    }
-    k_rs_downsweep<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
-                                                (first && iota_vals) ? nullptr : rs.vals[cur],
-                                                sizes, shift, rs.hist, rs.keys[cur ^ 1],
-                                                rs.vals[cur ^ 1]);
-    PVDB_CHECK_LAUNCH("k_rs_downsweep");
-    first = false;
+  for (int p = 0; p < npass; ++p) {
+    k_os_scatter<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
+                                              (p == 0 && iota_vals) ? nullptr : rs.vals[cur], p,
+                                              sc, L, rs.keys[cur ^ 1], rs.vals[cur ^ 1], errp);
+    PVDB_CHECK_LAUNCH("k_os_scatter");
     cur ^= 1;
   }
   *out_buf = cur;
   return PVDB_OK;
+}
+
+int radix_sort_words(int64_t n_max, int key_bits) {
+  return int(os_layout(n_max, (key_bits + 7) / 8).words);
 }
 
 int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,

@@ -16,6 +16,13 @@ namespace pvdb {
 
 constexpr uint32_t kInvalidKey = 0xFFFFFFFFu;
 
+// Radix sort tiling (reduce.cu): keys per tile and bins per 8-bit digit. The
+// sort keeps one histogram of kRsBins words per tile.
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 4;                     // keys per lane
+constexpr int kRsTile = kRsThreads * kRsRounds;  // 1024 keys per tile
+constexpr int kRsBins = 256;
+
 // Writes the 8 corner keys of one sample at keys[s*8 .. s*8+7].
 __device__ __forceinline__ void emit_corner_keys(const GridView& g, float x, float y, float z,
                                                  uint32_t* keys, int64_t s) {

@@ -175,11 +175,13 @@ def _emulated_bf16_backward(k0, rid, vd, params, y, G):
     v = vd.double()
     freq = torch.tensor([1.0, 2.0, 4.0, 8.0], dtype=torch.float64, device="cuda")
     emb = (v.unsqueeze(-1) * freq).flatten(-2)
-    pe = torch.cat([v, emb.sin(), emb.cos()], -1)
-    hpe = (pe @ w0[:, c0:].T + b0)[rid.long()]
-    pe = pe[rid.long()]
+    pe = torch.cat([v, emb.sin(), emb.cos()], -1)[rid.long()]
     x = _bf(k0)
-    h0 = _bf(torch.relu(x @ _bf(w0[:, :c0]).T + hpe))
+    # layer 0 as one GEMM over [k0 | PE | 1] against [W0 | b0], all BF16
+    ones = torch.ones(k0.shape[0], 1, dtype=torch.float64, device="cuda")
+    x1 = _bf(torch.cat([k0.double(), pe, ones], -1))
+    w0f = _bf(torch.cat([w0, b0[:, None]], -1))
+    h0 = _bf(torch.relu(x1 @ w0f.T))
     h1 = _bf(torch.relu(h0 @ _bf(w1).T + b1))
     dl32 = G.double() * (1 - y.double()) * y.double()
     dl = _bf(dl32)

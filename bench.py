@@ -293,9 +293,38 @@ def run_e2e(tr, ro, rd, vd, tgt, args, flush):
             "d2h_bytes_per_step": 4}
 
 
+# Algorithmic work per unit of each train-step stage (the design doc table):
+#   march_fwd       36 B per evaluated sample (8 density corners + the alpha)
+#   k0_gather       8*C*4 + 16 B per colour row (8 k0 corners + row record)
+#   rgbnet_fwd      36,608 FLOP per row + 6,912 per ray (PE part of layer 0)
+#   rgbnet_bwd      122,880 FLOP per row (backward GEMMs + layer 0/1 recompute)
+#   march_bwd       120 B per kept sample (saved alpha/weight/step/row, grad,
+#                   8 density corners, 64 B gradient record, 4 B key)
+#   radix_sort      (8 B read + 8 B write) * passes + 4 B histogram per key
+#   segment_reduce  64 B record + 8 corner partials (1 + C floats) per kept sample
+#   voxel_adam      28 B per visited voxel-channel (p, g, m, v read; p, m, v written)
+RGBNET_FWD_ROW, RGBNET_FWD_RAY, RGBNET_BWD_ROW = 36608.0, 6912.0, 122880.0
+
+
+def stage_work(tr, R):
+    """(bound, algorithmic units per launch) of each stage for the last step."""
+    kept, rows, evaluated = tr.ws.stats()
+    C = 12
+    npass = 3
+    return {
+        "march_fwd": ("hbm", evaluated * 36.0),
+        "k0_gather": ("hbm", rows * (8 * C * 4 + 16.0)),
+        "rgbnet_fwd": ("tensor", rows * RGBNET_FWD_ROW + R * RGBNET_FWD_RAY),
+        "rgbnet_bwd": ("tensor", rows * RGBNET_BWD_ROW),
+        "march_bwd": ("hbm", kept * 120.0),
+        "radix_sort": ("hbm", kept * (16.0 * npass + 4.0)),
+        "segment_reduce": ("hbm", kept * (64.0 + 8 * (1 + C) * 4.0)),
+    }, (kept, rows, evaluated)
+
+
 def roofline(stage_ms, tr, scfg):
-    """HBM roofline of the dominant stage, algorithmic bytes from the workload's
-    counts (one forward of the step's batch provides them)."""
+    """Roofline of the dominant stage: algorithmic bytes (or FLOPs) per launch
+    over the stage's CUDA-event time, against the measured peaks."""
     import json as _json
     peaks = {}
     try:
@@ -303,27 +332,30 @@ def roofline(stage_ms, tr, scfg):
     except Exception:
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    tk, tr_rows = tr.ws.totals()
-    nactive_d = tr.density.info()[3]
+    tflops = float(peaks.get("bf16_tflops", 1900.0))
+    work, (kept, rows, evaluated) = stage_work(tr, RAYS)
+    table = {}
+    for name, ms in stage_ms.items():
+        if name not in work or ms <= 0:
+            continue
+        bound, units = work[name]
+        if bound == "hbm":
+            ach, peak, unit = units / (ms / 1e3) / 1e9, hbm, "GB/s"
+        else:
+            ach, peak, unit = units / (ms / 1e3) / 1e12, tflops, "TFLOP/s"
+        table[name] = {"bound": bound, "achieved": ach, "unit": unit, "frac": ach / peak,
+                       "ms": ms}
     name = max(stage_ms, key=stage_ms.get)
-    ms = stage_ms[name]
-    C = 12
-    # algorithmic bytes per unit: kept sample density fwd 36 B,
-    # colour row k0 gather 8*C*4 B, backward 36 B per kept sample + 8*C*4 per row,
-    # rgbnet rows 4*(C+3+3) B, streaming Adam 28 B per visited voxel-channel.
-    per_stage_bytes = {
-        "march_fwd": tk * 36.0, "k0_gather": tr_rows * (8 * C * 4 + 16),
-        "rgbnet_fwd": tr_rows * (C * 4 + 12), "rgbnet_bwd": tr_rows * (C * 4 + 24 + C * 4),
-        "march_bwd": tk * 36.0, "radix_sort": tk * 8 * 8 * 2 * 3.0,
-        "segment_reduce": tk * 8 * (8 + 4) + tr_rows * C * 4 * 8,
-        "voxel_adam": nactive_d * (1 + C) * 28.0,
-    }
-    bytes_ = per_stage_bytes.get(name)
-    achieved = bytes_ / (ms / 1e3) / 1e9 if bytes_ else None
-    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": (achieved / hbm) if achieved else None, "traffic": None,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
-            "avg_ms": ms, "kept_samples": tk, "color_rows": tr_rows}
+    t = table.get(name)
+    src = "MEASURED_PEAKS.json (of measured)" if peaks else "fallback"
+    out = {"kernel": name, "bound": t["bound"] if t else "hbm",
+           "achieved": t["achieved"] if t else None,
+           "peak": (hbm if (not t or t["bound"] == "hbm") else tflops),
+           "unit": t["unit"] if t else "GB/s", "frac": t["frac"] if t else None,
+           "traffic": None, "peak_source": src, "avg_ms": stage_ms[name],
+           "kept_samples": kept, "color_rows": rows, "evaluated_samples": evaluated,
+           "stages": table}
+    return out
 
 
 def run_render(scfg, cfg, cam, tr, args):

@@ -335,6 +335,11 @@ int pvdb_march_views(pvdb_march m, pvdb_march_views_t* v);
 
 /* Host copy of the totals (synchronises the stream). */
 int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pvdb_stream s);
+/* Counts of the last forward (synchronises s): kept samples, colour rows, and
+ * samples evaluated (in the bbox, up to each ray's early stop). No reference
+ * counterpart: the reference materialises these as tensor sizes. */
+int pvdb_march_stats(pvdb_march m, int64_t* kept, int64_t* rows, int64_t* evaluated,
+                     pvdb_stream s);
 
 /* Backward. grad_weight [M] (per colour row), grad_last [R], grad_k0 [M, C] (may
  * be NULL when k0 is NULL or gets no gradient). Adds into density->grad and

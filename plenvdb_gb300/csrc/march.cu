@@ -63,7 +63,9 @@ __global__ void __launch_bounds__(kMarchThreads)
   const int64_t sbase = int64_t(r) * P.cap;
   float T = 1.f;
   int nk = 0, nc = 0;
+  int64_t nev = 0;  // samples evaluated before the early stop
   for (int64_t base = 0; base < ns; base += 32) {
+    nev += (ns - base < 32) ? (ns - base) : 32;
     const int64_t k = base + lane;
     float alpha = 0.f;
     bool keep = false;
@@ -116,6 +118,7 @@ __global__ void __launch_bounds__(kMarchThreads)
     W.T_last[r] = T;
     W.n_kept[r] = nk;
     W.n_color[r] = nc;
+    atomicAdd(W.totals + 4, uint32_t(nev));
   }
 }
 
@@ -585,7 +588,7 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   m->n_rays = R;
   m->density = density;
   m->k0 = k0;
-  PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals, 0, 16, st));
+  PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals, 0, 32, st));
   if (R > 0) {
     const int nb = ceil_div(R, kMarchWarps);
     k_march_fwd<<<nb, kMarchThreads, 0, st>>>(density->view(), ro, rd, R, m->p, m->w);
@@ -794,6 +797,20 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
   if (t[3] & 1u) return set_error(PVDB_ERR_STATE, "a ray had more samples than samples_cap");
   if (t[3] & 2u) return set_error(PVDB_ERR_TIMEOUT, "a tensor-core MMA wait timed out");
   if (t[3] & 4u) return set_error(PVDB_ERR_TIMEOUT, "a radix-sort look-back wait timed out");
+  return PVDB_OK;
+}
+
+int pvdb_march_stats(pvdb_march m, int64_t* kept, int64_t* rows, int64_t* evaluated,
+                     pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(m, "null argument");
+  uint32_t t[8];
+  cudaStream_t st = as_stream(s);
+  PVDB_CHECK_CUDA(cudaMemcpyAsync(t, m->w.totals, 32, cudaMemcpyDeviceToHost, st));
+  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (kept) *kept = t[0];
+  if (rows) *rows = t[1];
+  if (evaluated) *evaluated = t[4];
   return PVDB_OK;
 }
 

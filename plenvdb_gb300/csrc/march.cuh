@@ -44,6 +44,8 @@ struct MarchW {
   // (zeros for a sample without one), nq = ceil(C/4)
   float4* b_rec;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
+  // (1 samples_cap exceeded, 2 tensor-core wait, 4 sort look-back wait),
+  // [4] samples evaluated
   uint32_t* totals;
 };
 

@@ -77,6 +77,12 @@ class MarchWorkspace:
         L.call("pvdb_march_totals", self.h, C.byref(tk), C.byref(tr), L.stream_of())
         return tk.value, tr.value
 
+    def stats(self):
+        """(kept samples, colour rows, samples evaluated) of the last forward."""
+        k, r, e = C.c_int64(), C.c_int64(), C.c_int64()
+        L.call("pvdb_march_stats", self.h, C.byref(k), C.byref(r), C.byref(e), L.stream_of())
+        return k.value, r.value, e.value
+
     def rows(self, M: int, C0: int):
         """Torch views of the colour rows of the last forward."""
         v = self.views()

@@ -174,9 +174,18 @@ int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s);
 /* Device views of the leaf store (for zero-copy use by a host framework).
  * data/grad: float[nleaf*512*channels] (voxel-major, channel innermost);
  * mask: uint64[nleaf*8]; leaf_table: int32[ldim0*ldim1*ldim2] (-1 = no leaf);
- * leaf_origin: int32[nleaf*3]. Any pointer argument may be NULL. */
+ * leaf_origin: int32[nleaf*3]. Any pointer argument may be NULL. Asking for
+ * `data` (or `grad`) marks the values (gradients) as externally written; a
+ * caller that keeps the pointer and writes through it again after a later
+ * library call must report it with pvdb_grid_mark_written. */
 int pvdb_grid_device_views(pvdb_grid g, void** data, void** grad, void** mask,
                            void** leaf_table, void** leaf_origin, int32_t ldim[3]);
+
+/* Report writes through device views: which = PVDB_WHICH_DATA drops the
+ * values' derived bounds (rebuilt by the next march), PVDB_WHICH_GRAD makes
+ * every leaf count as possibly holding a gradient. No reference counterpart
+ * (the reference copies host arrays in and out on every call). */
+int pvdb_grid_mark_written(pvdb_grid g, int32_t which);
 
 /* save_to / load_from (plenvdb.h:143-148, :126-142, :269-276, :211-240).
  * The file holds the leaf topology, active masks, values and a checksum

@@ -107,6 +107,7 @@ _SIGS = {
     "pvdb_grid_zero_grad": (C.c_int, [vp, vp]),
     "pvdb_grid_device_views": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
                                          C.POINTER(vp), C.POINTER(vp), P_i32]),
+    "pvdb_grid_mark_written": (C.c_int, [vp, i32]),
     "pvdb_grid_save": (C.c_int, [vp, C.c_char_p]),
     "pvdb_grid_load": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
     "pvdb_opt_create": (C.c_int, [vp, f32, f32, f32, f32, C.POINTER(vp)]),

@@ -236,6 +236,25 @@ __global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
   }
 }
 
+// Brick bound from scratch: one thread per brick, the max over the 7^3
+// voxels [4b-1, 4b+5] (background outside allocated leaves).
+__global__ void k_bmax_init(GridView g, uint32_t* bmax) {
+  const int64_t nb = int64_t(g.bdim[0]) * g.bdim[1] * g.bdim[2];
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nb;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int bz = int(t % g.bdim[2]), by = int((t / g.bdim[2]) % g.bdim[1]),
+              bx = int(t / (int64_t(g.bdim[2]) * g.bdim[1]));
+    float m = -INFINITY;
+    for (int x = 4 * bx - 1; x <= 4 * bx + 5; ++x)
+      for (int y = 4 * by - 1; y <= 4 * by + 5; ++y)
+        for (int z = 4 * bz - 1; z <= 4 * bz + 5; ++z) {
+          const float v = value1(g, x, y, z);
+          m = (v > m || v != v) ? v : m;
+        }
+    bmax[t] = fkey(m);
+  }
+}
+
 __global__ void k_touched_compact(const uint8_t* __restrict__ touched, int nleaf, int32_t* list,
                                   uint32_t* count) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,6 +359,22 @@ int touched_list(pvdb_grid_s* g, cudaStream_t st) {
     PVDB_CHECK_LAUNCH("k_touched_compact");
   }
   g->tlist_valid = true;
+  return PVDB_OK;
+}
+
+int bmax_ensure(pvdb_grid_s* g, cudaStream_t st) {
+  if (g->C != 1) return set_error(PVDB_ERR_ARG, "brick bounds are for scalar grids");
+  if (g->bmax_valid) return PVDB_OK;
+  if (!g->d_bmax) {
+    for (int a = 0; a < 3; ++a) g->bdim[a] = (g->reso[a] + 3) / 4;
+    const size_t nb = size_t(g->bdim[0]) * g->bdim[1] * g->bdim[2];
+    int rc = dev_alloc((void**)&g->d_bmax, std::max<size_t>(nb, 1) * 4);
+    if (rc) return rc;
+  }
+  GridView v = g->view();
+  k_bmax_init<<<stride_grid(), 256, 0, st>>>(v, g->d_bmax);
+  PVDB_CHECK_LAUNCH("k_bmax_init");
+  g->bmax_valid = true;
   return PVDB_OK;
 }
 
@@ -469,6 +504,7 @@ int pvdb_grid_destroy(pvdb_grid g) {
   dev_free(g->d_touched);
   dev_free(g->d_tlist);
   dev_free(g->d_tcount);
+  dev_free(g->d_bmax);
   dev_free(g->d_stage);
   free_scratch(g->red);
   delete g;
@@ -520,6 +556,7 @@ int pvdb_grid_copy_from_dense(pvdb_grid g, int32_t which, const float* arr, int6
         g->reso[1], g->reso[2]);
   PVDB_CHECK_LAUNCH("k_copy_from_dense");
   if (which == PVDB_WHICH_GRAD) g->all_touched = true;
+  if (which == PVDB_WHICH_DATA) g->bmax_valid = false;
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
   return PVDB_OK;
 }
@@ -571,6 +608,7 @@ int pvdb_grid_set_values_by_mask(pvdb_grid g, const uint8_t* mask, int64_t n, fl
     k_set_by_mask<<<ceil_div(ns, 256), 256, 0, st>>>(g->view(), m, val, g->reso[0], g->reso[1],
                                                      g->reso[2]);
   PVDB_CHECK_LAUNCH("k_set_by_mask");
+  g->bmax_valid = false;
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
   return PVDB_OK;
 }
@@ -664,6 +702,7 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
 }
 
 
+
 int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
   clear_error();
   PVDB_REQUIRE(g, "null grid");
@@ -681,11 +720,23 @@ int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
   return PVDB_OK;
 }
 
+int pvdb_grid_mark_written(pvdb_grid g, int32_t which) {
+  clear_error();
+  PVDB_REQUIRE(g, "null grid");
+  PVDB_REQUIRE(which == PVDB_WHICH_DATA || which == PVDB_WHICH_GRAD, "bad `which`");
+  if (which == PVDB_WHICH_DATA) g->bmax_valid = false;
+  else g->all_touched = true;
+  return PVDB_OK;
+}
+
 int pvdb_grid_device_views(pvdb_grid g, void** data, void** grad, void** mask, void** leaf_table,
                            void** leaf_origin, int32_t ldim[3]) {
   clear_error();
   PVDB_REQUIRE(g, "null grid");
-  if (data) *data = g->d_data;
+  if (data) {
+    *data = g->d_data;
+    g->bmax_valid = false;  // the caller may write values we cannot track
+  }
   if (grad) {
     *grad = g->d_grad;
     g->all_touched = true;  // the caller may write gradients we cannot track

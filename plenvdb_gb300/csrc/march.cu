@@ -1,17 +1,18 @@
-// Fused training march over ragged per-ray sample counts, one ray per warp.
+// Fused training march over ragged per-ray sample counts.
 //
-// Forward (k_march_fwd) fuses, per ray: sample_pts_on_rays
-// (render_utils_kernel.cu:196-242), the bbox filter and MaskGrid lookup
-// (dvgo.py:290-315), wld2idx (grid.py:77-78), DensityVDB trilinear
-// (densityvdb.cu:101-125), raw2alpha (render_utils_kernel.cu:430-443), the
-// alpha threshold (dvgo.py:319-325) and alpha2weight with its T < 1e-3 early
-// stop (render_utils_kernel.cu:576-605). The transmittance chain is walked in
-// sample order over the kept lanes of each 32-sample chunk with exactly the
-// reference's rounding. Only per-ray alpha / step lists are kept for the
+// Forward (k_march_setup / k_march_alpha / k_march_chain) covers, per ray:
+// sample_pts_on_rays (render_utils_kernel.cu:196-242), the bbox filter and
+// MaskGrid lookup (dvgo.py:290-315), wld2idx (grid.py:77-78), DensityVDB
+// trilinear (densityvdb.cu:101-125), raw2alpha (render_utils_kernel.cu:430-443),
+// the alpha threshold (dvgo.py:319-325) and alpha2weight with its T < 1e-3
+// early stop (render_utils_kernel.cu:576-605). Samples in bricks whose density
+// bound keeps alpha below the threshold skip the trilinear (they would be
+// dropped anyway). The transmittance chain is walked in sample order over the
+// kept samples. Only per-ray alpha / weight / step lists are kept for the
 // backward.
 //
-// k_march_gather compacts the colour samples (weight > thres, dvgo.py:329-335)
-// into dense rows and samples the k0 grid there (colorvdb.cu:81-111).
+// k_march_rows lays the colour samples (weight > thres, dvgo.py:329-335) out as
+// dense rows and samples the k0 grid there (colorvdb.cu:81-111).
 //
 // Backward (k_march_bwd) recovers transmittance from the saved alphas and
 // weights, runs alpha2weight_backward (:653-677) as a suffix scan and
@@ -40,11 +41,21 @@ __device__ __forceinline__ void load_ray(const float* __restrict__ ro, const flo
   }
 }
 
-__global__ void __launch_bounds__(kMarchThreads)
-    k_march_fwd(GridView gd, const float* __restrict__ ro, const float* __restrict__ rd, int R,
-                MarchP P, MarchW W) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kMarchWarps + warp;
+// Forward, in three passes:
+//  k_march_setup (thread per ray): slab test, sample count, start point and
+//    unit direction;
+//  k_march_alpha (thread per (ray, sample)): position, brick-bound skip,
+//    density trilinear and raw2alpha; writes alpha (0 for a sample that is not
+//    kept) into the ray's slots — independent work, so the gathers of all
+//    samples are in flight together;
+//  k_march_chain (warp per ray): the transmittance chain over the kept
+//    samples in order, the T < t_stop early stop, and the in-place compaction
+//    of the kept samples (a kept sample moves to a slot at or before its own,
+//    after the whole chunk has been read).
+__global__ void __launch_bounds__(256)
+    k_march_setup(const float* __restrict__ ro, const float* __restrict__ rd, int R, MarchP P,
+                  MarchW W) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
   float o[3], d[3];
   load_ray(ro, rd, r, o, d);
@@ -52,73 +63,188 @@ __global__ void __launch_bounds__(kMarchThreads)
   ray_setup(o, d, P.mn, P.mx, P.near_, P.far_, P.stepdist, rs);
   int64_t ns = rs.n_steps;
   if (ns > P.cap) {
-    if (lane == 0) atomicOr(W.totals + 3, 1u);
+    atomicOr(W.totals + 3, 1u);
     ns = P.cap;
   }
-  if (lane < 3) {
-    W.ray_sd[r * 6 + lane] = rs.start[lane];
-    W.ray_sd[r * 6 + 3 + lane] = rs.dir[lane];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    W.ray_sd[r * 6 + a] = rs.start[a];
+    W.ray_sd[r * 6 + 3 + a] = rs.dir[a];
   }
+  W.ray_ns[r] = int32_t(ns);
+  atomicAdd(W.totals + 4, uint32_t(ns));
+}
+
+__global__ void __launch_bounds__(256)
+    k_march_alpha(GridView gd, int R, MarchP P, MarchW W) {
+  const int64_t total = int64_t(R) * P.cap;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int r = int(t / P.cap);
+    const int k = int(t - int64_t(r) * P.cap);
+    if (k >= W.ray_ns[r]) continue;
+    RaySetup rs;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      rs.start[a] = W.ray_sd[r * 6 + a];
+      rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+    }
+    float p[3];
+    ray_point(rs, P.stepdist, k, p);
+    float alpha = 0.f;
+    bool skip = false;
+    if (gd.bmax) {
+      // brick of the (approximate) cell; its bound covers the cells next to it
+      int b[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
+      const uint32_t key = __ldg(gd.bmax + (int64_t(b[0]) * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
+      skip = fkey_inv(key) < P.sigma_skip;
+    }
+    if (!skip && !out_of_bbox(p, P.mn, P.mx) &&
+        (!P.mask || mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift))) {
+      float idx[3];
+      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+      const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
+      float e;
+      const float a = raw2alpha(sigma, P.shift, P.interval, e);
+      if (a > P.thr) alpha = a;
+    }
+    W.k_alpha[t] = alpha;
+  }
+}
+
+constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
+
+__global__ void __launch_bounds__(kMarchThreads)
+    k_march_chain(int R, MarchP P, MarchW W) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * kMarchWarps + warp;
+  if (r >= R) return;
+  const int ns = W.ray_ns[r];
   const unsigned lt = lanemask_lt();
   const int64_t sbase = int64_t(r) * P.cap;
   float T = 1.f;
   int nk = 0, nc = 0;
-  int64_t nev = 0;  // samples evaluated before the early stop
-  for (int64_t base = 0; base < ns; base += 32) {
-    nev += (ns - base < 32) ? (ns - base) : 32;
-    const int64_t k = base + lane;
-    float alpha = 0.f;
-    bool keep = false;
-    if (k < ns) {
-      float p[3];
-      ray_point(rs, P.stepdist, k, p);
-      if (!out_of_bbox(p, P.mn, P.mx) &&
-          (!P.mask || mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift))) {
-        float idx[3];
-        world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-        const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
-        float e;
-        alpha = raw2alpha(sigma, P.shift, P.interval, e);
-        keep = alpha > P.thr;
+  bool stop = false;
+  for (int b0 = 0; b0 < ns && !stop; b0 += 32 * kChainBatch) {
+    // the batch's alphas, loaded before any of them is used
+    float al[kChainBatch];
+#pragma unroll
+    for (int j = 0; j < kChainBatch; ++j) {
+      const int k = b0 + 32 * j + lane;
+      al[j] = k < ns ? W.k_alpha[sbase + k] : 0.f;
+    }
+    __syncwarp();  // every lane has read its alphas before the compaction writes
+#pragma unroll
+    for (int j = 0; j < kChainBatch; ++j) {
+      if (stop) continue;
+      const int k = b0 + 32 * j + lane;
+      unsigned km = __ballot_sync(0xffffffffu, al[j] > P.thr);
+      // alpha2weight over the kept lanes, in sample order (uniform across the warp)
+      float w = 0.f;
+      unsigned rem = km;
+      while (rem) {
+        const int l = __ffs(rem) - 1;
+        rem &= rem - 1;
+        const float a = __shfl_sync(0xffffffffu, al[j], l);
+        const float wl = T * a;
+        if (lane == l) w = wl;
+        T = trans_step(T, a);
+        if (T < P.t_stop) {
+          km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
+          stop = true;
+          break;
+        }
       }
-    }
-    unsigned km = __ballot_sync(0xffffffffu, keep);
-    // alpha2weight over the kept lanes, in sample order (uniform across the warp)
-    float w = 0.f;
-    bool stop = false;
-    unsigned rem = km;
-    while (rem) {
-      const int l = __ffs(rem) - 1;
-      rem &= rem - 1;
-      const float a = __shfl_sync(0xffffffffu, alpha, l);
-      const float wl = T * a;
-      if (lane == l) w = wl;
-      T = trans_step(T, a);
-      if (T < P.t_stop) {
-        km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
-        stop = true;
-        break;
+      const bool kept = (km >> lane) & 1u;
+      const bool col = kept && (w > P.thr);
+      const unsigned cm = __ballot_sync(0xffffffffu, col);
+      if (kept) {
+        const int64_t pos = sbase + nk + __popc(km & lt);
+        W.k_alpha[pos] = al[j];
+        W.k_w[pos] = w;
+        W.k_step[pos] = int32_t(k) | (col ? int32_t(0x80000000) : 0);
+        W.k_row[pos] = col ? nc + __popc(cm & lt) : -1;  // rank among the ray's colour rows
       }
+      nk += __popc(km);
+      nc += __popc(cm);
     }
-    const bool kept = (km >> lane) & 1u;
-    const bool col = kept && (w > P.thr);
-    const unsigned cm = __ballot_sync(0xffffffffu, col);
-    if (kept) {
-      const int64_t pos = sbase + nk + __popc(km & lt);
-      W.k_alpha[pos] = alpha;
-      W.k_w[pos] = w;
-      W.k_step[pos] = int32_t(k) | (col ? int32_t(0x80000000) : 0);
-      W.k_row[pos] = -1;
-    }
-    nk += __popc(km);
-    nc += __popc(cm);
-    if (stop) break;
   }
   if (lane == 0) {
     W.T_last[r] = T;
     W.n_kept[r] = nk;
     W.n_color[r] = nc;
-    atomicAdd(W.totals + 4, uint32_t(nev));
+  }
+}
+
+// Per-ray offsets of the kept samples and colour rows (exclusive prefix sums
+// of n_kept and n_color, in ray order) and the totals, in one block: both
+// counts ride in one 64-bit word (colour count in the high half).
+__device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t* total) {
+  __shared__ uint64_t ws[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t s = lane < nw ? ws[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) ws[lane] = s;
+  }
+  __syncthreads();
+  const uint64_t r = (wid ? ws[wid - 1] : 0ull) + x - v;
+  *total = ws[nw - 1];
+  __syncthreads();
+  return r;
+}
+
+constexpr int kOffThreads = 1024;
+constexpr int kOffItems = 4;
+
+__global__ void __launch_bounds__(kOffThreads) k_march_offsets(MarchW W, int R) {
+  __shared__ uint64_t buf[kOffThreads * kOffItems];
+  uint64_t carry = 0;
+  for (int c0 = 0; c0 < R; c0 += kOffThreads * kOffItems) {
+#pragma unroll
+    for (int q = 0; q < kOffItems; ++q) {  // coalesced loads
+      const int i = c0 + q * kOffThreads + threadIdx.x;
+      buf[q * kOffThreads + threadIdx.x] =
+          i < R ? (uint64_t(W.n_color[i]) << 32) | uint64_t(W.n_kept[i]) : 0ull;
+    }
+    __syncthreads();
+    uint64_t v[kOffItems], s = 0;
+#pragma unroll
+    for (int q = 0; q < kOffItems; ++q) {
+      v[q] = buf[threadIdx.x * kOffItems + q];
+      s += v[q];
+    }
+    uint64_t tot;
+    uint64_t run = block_excl_scan64(s, &tot) + carry;
+#pragma unroll
+    for (int q = 0; q < kOffItems; ++q) {
+      const int i = c0 + threadIdx.x * kOffItems + q;
+      if (i < R) {
+        W.kept_off[i] = uint32_t(run);
+        W.color_off[i] = uint32_t(run >> 32);
+      }
+      run += v[q];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0) {
+    W.totals[0] = uint32_t(carry);
+    W.totals[1] = uint32_t(carry >> 32);
   }
 }
 
@@ -128,10 +254,6 @@ __device__ __forceinline__ void load_setup(const MarchW& W, int r, RaySetup& rs)
     rs.start[a] = W.ray_sd[r * 6 + a];
     rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
   }
-}
-
-__global__ void k_march_totals(MarchW W) {
-  W.totals[2] = W.totals[0] * 8u;
 }
 
 // Multi-channel trilinear of k0 at one point (colorvdb.cu:97-108 ordering).
@@ -181,41 +303,32 @@ __device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[
   }
 }
 
-__global__ void __launch_bounds__(kMarchThreads)
-    k_march_gather(GridView gk, int R, MarchP P, MarchW W) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kMarchWarps + warp;
-  if (r >= R) return;
-  const int nk = int(W.n_kept[r]);
-  if (nk == 0) return;
-  RaySetup rs;
-  load_setup(W, r, rs);
-  const unsigned lt = lanemask_lt();
-  const int64_t sbase = int64_t(r) * P.cap;
-  int64_t row = W.color_off[r];
-  for (int base = 0; base < nk; base += 32) {
-    const int i = base + lane;
-    int32_t st = 0;
-    bool col = false;
-    if (i < nk) {
-      st = W.k_step[sbase + i];
-      col = st < 0;
-    }
-    const unsigned cm = __ballot_sync(0xffffffffu, col);
-    if (col) {
-      const int64_t m = row + __popc(cm & lt);
-      const int32_t k = st & 0x7fffffff;
-      float p[3], idx[3];
-      ray_point(rs, P.stepdist, k, p);
-      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-      if (gk.C > 0) k0_trilinear(gk, idx, W.r_k0 + m * gk.C);
-      W.r_w[m] = W.k_w[sbase + i];
-      W.r_alpha[m] = W.k_alpha[sbase + i];
-      W.r_ray[m] = r;
-      W.r_step[m] = k;
-      W.k_row[sbase + i] = int32_t(m);
-    }
-    row += __popc(cm);
+// Colour rows, one thread per kept-sample slot (r, i): a colour sample gets
+// its global row m = color_off[r] + its rank in the ray, the k0 trilinear at
+// its position (colorvdb.cu:81-111) and the row record; k_row becomes m.
+__global__ void __launch_bounds__(256)
+    k_march_rows(GridView gk, int R, MarchP P, MarchW W) {
+  const int64_t total = int64_t(R) * P.cap;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int r = int(t / P.cap);
+    const int i = int(t - int64_t(r) * P.cap);
+    if (i >= int(W.n_kept[r])) continue;
+    const int32_t rank = W.k_row[t];
+    if (rank < 0) continue;
+    const int64_t m = int64_t(W.color_off[r]) + rank;
+    const int32_t k = W.k_step[t] & 0x7fffffff;
+    RaySetup rs;
+    load_setup(W, r, rs);
+    float p[3], idx[3];
+    ray_point(rs, P.stepdist, k, p);
+    world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+    if (gk.C > 0) k0_trilinear(gk, idx, W.r_k0 + m * gk.C);
+    W.r_w[m] = W.k_w[t];
+    W.r_alpha[m] = W.k_alpha[t];
+    W.r_ray[m] = r;
+    W.r_step[m] = k;
+    W.k_row[t] = int32_t(m);
   }
 }
 
@@ -566,6 +679,16 @@ static void fill_params(const pvdb_march_params* in, const pvdb_grid_s* gd, cons
     P.mshift[a] = mask ? (-P.mn[a]) * P.mscale[a] : 0.f;
   }
   P.cap = cap;
+  // alpha > thr  <=>  sigma > log((1 - thr)^(-1/interval) - 1) - shift; the
+  // margin covers the float evaluation of the trilinear and of raw2alpha
+  P.sigma_skip = -INFINITY;
+  if (in->fast_color_thres > 0.f && in->fast_color_thres < 1.f && in->interval > 0.f) {
+    const double t = std::log(std::pow(1.0 - double(in->fast_color_thres),
+                                       -1.0 / double(in->interval)) - 1.0) -
+                     double(in->act_shift);
+    P.sigma_skip = float(t - 1e-3 * (std::fabs(t) + 1.0));
+  }
+  for (int a = 0; a < 3; ++a) P.binv[a] = P.wsm1[a] / P.ext[a] * 0.25f;
 }
 
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
@@ -584,6 +707,10 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
       m->k0_channels = k0->C;
     }
   }
+  if (density->C == 1) {
+    int rc = bmax_ensure(density, st);
+    if (rc) return rc;
+  }
   fill_params(prm, density, mask, mshape, m->cap, m->p);
   m->n_rays = R;
   m->density = density;
@@ -591,21 +718,21 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals, 0, 32, st));
   if (R > 0) {
     const int nb = ceil_div(R, kMarchWarps);
-    k_march_fwd<<<nb, kMarchThreads, 0, st>>>(density->view(), ro, rd, R, m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_fwd");
-    int rc = scan_exclusive_u32(m->w.n_kept, m->w.kept_off, R, m->w.totals + 0, &m->scan_partial,
-                                &m->scan_partial_cap, st);
-    if (rc) return rc;
-    rc = scan_exclusive_u32(m->w.n_color, m->w.color_off, R, m->w.totals + 1, &m->scan_partial,
-                            &m->scan_partial_cap, st);
-    if (rc) return rc;
-    k_march_totals<<<1, 1, 0, st>>>(m->w);
-    PVDB_CHECK_LAUNCH("k_march_totals");
+    k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_setup");
+    k_march_alpha<<<int(std::min<int64_t>(ceil_div(int64_t(R) * m->cap, 256), int64_t(num_sms()) * 32)),
+                    256, 0, st>>>(density->view(), R, m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_alpha");
+    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_chain");
+    k_march_offsets<<<1, kOffThreads, 0, st>>>(m->w, R);
+    PVDB_CHECK_LAUNCH("k_march_offsets");
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
     if (k0) gk = k0->view();
-    k_march_gather<<<nb, kMarchThreads, 0, st>>>(gk, R, m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_gather");
+    k_march_rows<<<int(std::min<int64_t>(ceil_div(int64_t(R) * m->cap, 256), int64_t(num_sms()) * 16)),
+                   256, 0, st>>>(gk, R, m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_rows");
     if (m->prof) prof_mark(st, 2);
   }
   m->has_fwd = true;
@@ -715,7 +842,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
   MarchW& w = m->w;
   const size_t R = max_rays, S = size_t(m->slots);
   int rc;
-  if ((rc = dev_alloc((void**)&w.ray_sd, R * 24)) ||
+  if ((rc = dev_alloc((void**)&w.ray_sd, R * 24)) || (rc = dev_alloc((void**)&w.ray_ns, R * 4)) ||
       (rc = dev_alloc((void**)&w.T_last, R * 4)) || (rc = dev_alloc((void**)&w.n_kept, R * 4)) ||
       (rc = dev_alloc((void**)&w.n_color, R * 4)) ||
       (rc = dev_alloc((void**)&w.kept_off, R * 4)) ||
@@ -740,7 +867,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
 int pvdb_march_destroy(pvdb_march m) {
   if (!m) return PVDB_OK;
   MarchW& w = m->w;
-  void* ptrs[] = {w.ray_sd, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
+  void* ptrs[] = {w.ray_sd, w.ray_ns, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
                   w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec,
                   w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,

@@ -17,12 +17,17 @@ struct MarchP {
   int mshape[3];
   float mscale[3], mshift[3];
   int cap;
+  // empty-space skipping: a sample whose brick bound is below sigma_skip has
+  // alpha <= thr for certain (raw2alpha is increasing in sigma)
+  float sigma_skip;
+  float binv[3];  // approximate world -> brick scale: wsm1 / ext / 4
 };
 
 // Device pointers of the workspace, passed by value to kernels.
 struct MarchW {
   // per ray
   float* ray_sd;  // [R*6] sample origin (rays_o + rays_d*t_min) and unit direction
+  int32_t* ray_ns;  // [R] samples in the bbox (clamped to cap)
   float* T_last;
   uint32_t* n_kept;
   uint32_t* n_color;

@@ -60,8 +60,14 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
       m[base + q] = mn;
       v[base + q] = vn;
       const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
-      g.data[base + q] = g.data[base + q] - num / (eps + sqrtf(vn));
+      const float old = g.data[base + q];
+      const float nv = old - num / (eps + sqrtf(vn));
+      g.data[base + q] = nv;
       if (zero_after) g.grad[base + q] = 0.f;
+      // keep the march's brick bound an upper bound (scalar grids only)
+      if (g.bmax && !(nv <= old))
+        bmax_raise(g, g.origin[leaf * 3] + (vox >> 6), g.origin[leaf * 3 + 1] + ((vox >> 3) & 7),
+                   g.origin[leaf * 3 + 2] + (vox & 7), nv);
     }
   }
 }

@@ -86,6 +86,10 @@ struct GridView {
   const uint64_t* __restrict__ mask;
   float* data;
   float* grad;
+  // per-brick upper bound of the values a trilinear sample can interpolate
+  // (scalar grids that a march reads; NULL when not maintained)
+  uint32_t* bmax;
+  int bdim[3];
 };
 
 // Scratch of the deterministic gradient reduction (one per grid topology).
@@ -119,6 +123,14 @@ struct pvdb_grid_s {
   int32_t* d_tlist = nullptr;    // [nleaf] compacted ids of the touched leaves
   uint32_t* d_tcount = nullptr;  // number of entries in d_tlist (device)
   bool tlist_valid = false;      // d_tlist reflects d_touched
+  // Brick bound: for each brick of 4^3 trilinear cells, the largest value of
+  // the voxels [4b-1, 4b+5] per axis (every corner of those cells and of their
+  // neighbours), as order-preserving uint32 keys. Kept an upper bound by the
+  // voxel Adam (atomicMax when a value grows); any other write of the data
+  // invalidates it.
+  uint32_t* d_bmax = nullptr;
+  int bdim[3] = {0, 0, 0};
+  bool bmax_valid = false;
   std::vector<int32_t> h_table;
   std::vector<int32_t> h_origin;
   std::vector<uint64_t> h_mask;
@@ -132,6 +144,8 @@ struct pvdb_grid_s {
     for (int a = 0; a < 3; ++a) { v.reso[a] = reso[a]; v.ldim[a] = ldim[a]; }
     v.C = C; v.nleaf = nleaf; v.background = background;
     v.table = d_table; v.origin = d_origin; v.mask = d_mask; v.data = d_data; v.grad = d_grad;
+    v.bmax = bmax_valid ? d_bmax : nullptr;
+    for (int a = 0; a < 3; ++a) v.bdim[a] = bdim[a];
     return v;
   }
   int64_t nslots() const { return int64_t(nleaf) * pvdb::kLeafVox; }
@@ -222,6 +236,28 @@ __device__ __forceinline__ float density_corner_term(float g, float u, float v, 
   return __fmul_rn(__fmul_rn(__fmul_rn(g, a), b), cc);
 }
 
+// Order-preserving float <-> uint32 keys (for atomicMax on floats).
+__device__ __forceinline__ uint32_t fkey(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// Raises the brick bounds that cover voxel (x,y,z) to at least v: the bricks
+// b with 4b-1 <= x <= 4b+5 per axis.
+__device__ __forceinline__ void bmax_raise(const GridView& g, int x, int y, int z, float v) {
+  const uint32_t key = fkey(v);
+  const int x0 = max((x - 2) >> 2, 0), x1 = min((x + 1) >> 2, g.bdim[0] - 1);
+  const int y0 = max((y - 2) >> 2, 0), y1 = min((y + 1) >> 2, g.bdim[1] - 1);
+  const int z0 = max((z - 2) >> 2, 0), z1 = min((z + 1) >> 2, g.bdim[2] - 1);
+  for (int bx = x0; bx <= x1; ++bx)
+    for (int by = y0; by <= y1; ++by)
+      for (int bz = z0; bz <= z1; ++bz)
+        atomicMax(g.bmax + (int64_t(bx) * g.bdim[1] + by) * g.bdim[2] + bz, key);
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -268,6 +304,9 @@ int adam_dense_launch(float* param, const float* grad, float* m, float* v, const
                       cudaStream_t st, const float* stepsz_dev = nullptr);
 // Launch-counter value (every library kernel launch adds one).
 uint64_t launch_counter();
+
+// Allocates (once) and rebuilds the brick bound of a scalar grid if invalid.
+int bmax_ensure(pvdb_grid_s* g, cudaStream_t st);
 
 // Compacts the touched flags of g into g->d_tlist / d_tcount unless the list
 // is still valid (device work on st, no host synchronisation).

@@ -244,6 +244,8 @@ static void grid_key(std::vector<uint8_t>& k, const pvdb_grid_s* g) {
   key_put(k, g->d_table);
   key_put(k, g->d_touched);
   key_put(k, g->nleaf);
+  key_put(k, g->d_bmax);
+  key_put(k, g->bmax_valid);
 }
 
 // Everything a captured step has baked in: sizes, configuration, and the
@@ -348,7 +350,8 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   if (rc) return rc;
   // a graph replays the step whose gradients start at zero on tracked leaves;
   // right after the grids were written from outside, step eagerly once
-  bool graph_ok = cfg->use_graph && !dg->all_touched && !kg->all_touched;
+  // (and with the density grid's brick bound current: a replay does not rebuild it)
+  bool graph_ok = cfg->use_graph && !dg->all_touched && !kg->all_touched && dg->bmax_valid;
   TrainArgs t{m, density_opt, k0_opt, net, rays_o, rays_d, viewdirs, target, n_rays, cfg,
               loss_out, {0.f, 0.f, 0.f}, nullptr, !graph_ok};
   if (graph_ok) {

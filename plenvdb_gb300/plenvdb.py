@@ -275,6 +275,11 @@ class BaseVDB:
         origin = device_view(o.value, (nleaf, 3), "int32", self)
         return data, grad, mask, table, origin
 
+    def mark_written(self, which: int = L.WHICH_DATA):
+        """Report writes made through views from device_views() after later
+        library calls (the data's brick bounds / the touched-leaf tracking)."""
+        L.call("pvdb_grid_mark_written", self.handle, int(which))
+
 
 class DensityVDB(BaseVDB):
     """DensityVDB(resolution, n=1) (plenvdb.h:432-524)."""

@@ -877,6 +877,15 @@ int pvdb_march_destroy(pvdb_march m) {
   dev_free(m->cell_map);
   dev_free(m->cell_pd);
   dev_free(m->cell_pk);
+  dev_free(m->g_in);
+  dev_free(m->g_scal);
+  if (m->g_exec) cudaGraphExecDestroy(m->g_exec);
+  if (m->g_graph) cudaGraphDestroy(m->g_graph);
+  if (m->g_stream) cudaStreamDestroy(m->g_stream);
+  for (cudaStream_t& x : m->side)
+    if (x) cudaStreamDestroy(x);
+  for (cudaEvent_t& e : m->side_ev)
+    if (e) cudaEventDestroy(e);
   delete m;
   return PVDB_OK;
 }

@@ -104,5 +104,7 @@ struct pvdb_march_s {
   float* g_scal = nullptr;          // [0..2] Adam step sizes, [4] loss
   std::vector<uint8_t> g_key;       // what the graph was captured for
   std::vector<uint8_t> g_pending;   // key of the last eager step (capture on a repeat)
+  cudaStream_t side[2] = {nullptr, nullptr};  // side streams of the train step
+  cudaEvent_t side_ev[3] = {nullptr, nullptr, nullptr};
   uint64_t g_launches = 0;          // library launches per replay
 };

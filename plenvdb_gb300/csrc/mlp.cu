@@ -45,7 +45,7 @@ __host__ __device__ inline int64_t mlp_param_count(int din) { return int64_t(kW)
 constexpr int kPeRays = 32;
 __global__ void __launch_bounds__(128)
     k_pe_hpe(const float* __restrict__ viewdirs, int R, int npe, MlpArgs a, float* pe_out,
-             float* hpe) {
+             float* hpe) {  // hpe == NULL: the PE only
   __shared__ float wt[kMaxPe][kW];       // wt[q][n] = w0[n][c0+q]
   __shared__ float pe_s[kPeRays][kMaxPe];
   const int n = threadIdx.x;
@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(128)
     pe_out[int64_t(r) * kMaxPe + q] = v;
   }
   __syncthreads();
+  if (!hpe) return;
   const float b = a.b0[n];
   for (int rr = 0; rr < kPeRays && r0 + rr < R; ++rr) {
     float s = 0.f;
@@ -415,26 +416,52 @@ static int mlp_reserve(pvdb_march_s* m, int din) {
   return dev_reserve((void**)&m->wpart, &m->wpart_cap, (size_t(mlp_grid()) + 1) * P * 4);
 }
 
+int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* b1,
+                const float* w2, const float* b2, int c0, int dpe, int with_bwd, void** blob,
+                size_t* blob_cap, cudaStream_t st);
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
                         const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
                         float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
-                        cudaStream_t st);
+                        cudaStream_t st, int packed);
 
+// Inputs of the rgbnet that depend only on the rays and the weights: the
+// per-ray PE (FP32 path: and hpe) and, BF16 path, the packed BF16 weight
+// tiles of the forward and the backward. The train step runs this on a side
+// stream while the march runs.
+int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R, int precision,
+                cudaStream_t st) {
+  if (R <= 0) return PVDB_OK;
+  int rc = mlp_reserve(m, a.din);
+  if (rc) return rc;
+  float* pe = m->hpe + size_t(m->max_rays) * kW;
+  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe,
+                                                 precision == 1 ? nullptr : m->hpe);
+  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  if (precision == 1)
+    return mlp_tc_pack(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, 1, &m->mlp_packed,
+                       &m->mlp_packed_cap, st);
+  return PVDB_OK;
+}
+
+// prepared: mlp_prepare already ran for these rays and weights.
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
-                     const float* viewdirs, float* rgb, int precision, cudaStream_t st) {
+                     const float* viewdirs, float* rgb, int precision, cudaStream_t st,
+                     bool prepared) {
   const int R = m->n_rays;
   if (R <= 0) return PVDB_OK;
   int rc = mlp_reserve(m, a.din);
   if (rc) return rc;
   float* hpe = m->hpe;
   float* pe = m->hpe + size_t(m->max_rays) * kW;
-  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
-  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  if (!prepared) {
+    k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+    PVDB_CHECK_LAUNCH("k_pe_hpe");
+  }
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
                                m->w.r_ray, pe, kMaxPe, m->w.totals, rgb, 0, &m->mlp_packed,
-                               &m->mlp_packed_cap, m->w.totals + 3, st);
+                               &m->mlp_packed_cap, m->w.totals + 3, st, prepared ? 1 : 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
       a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
@@ -455,7 +482,7 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
-                               kMaxPe, totals, out, out_logits, blob, blob_cap, err, st);
+                               kMaxPe, totals, out, out_logits, blob, blob_cap, err, st, 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
                                                                   out, out_logits);
@@ -468,12 +495,13 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
                          const int32_t* ray, const float* pe, int pe_stride,
                          const uint32_t* totals, const float* rgb, const float* grad_rgb,
                          float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
-                         uint32_t* err, cudaStream_t st);
+                         uint32_t* err, cudaStream_t st, int packed);
 
-// hpe/pe of the current forward must still be in the workspace.
+// hpe/pe of the current forward must still be in the workspace; prepared: the
+// BF16 backward tiles were packed by mlp_prepare.
 int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
                       const float* grad_rgb, float* grad_k0, float* grad_flat, int precision,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool prepared) {
   const int R = m->n_rays;
   const int64_t P = mlp_param_count(a.din);
   if (R <= 0) {
@@ -487,7 +515,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
     rc = mlp_tc_backward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, m->w.r_ray,
                               m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, rgb,
                               grad_rgb, grad_k0, m->wpart, G, &m->mlp_packed, &m->mlp_packed_cap,
-                              m->w.totals + 3, st);
+                              m->w.totals + 3, st, prepared ? 1 : 0);
     if (rc) return rc;
     k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
     PVDB_CHECK_LAUNCH("k_wgrad_reduce");
@@ -531,7 +559,8 @@ int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   MlpArgs a;
   int rc = mlp_args_from(w, a);
   if (rc) return rc;
-  return mlp_forward_impl(m, a, k0 ? k0 : m->w.r_k0, viewdirs, rgb, precision, as_stream(s));
+  return mlp_forward_impl(m, a, k0 ? k0 : m->w.r_k0, viewdirs, rgb, precision, as_stream(s),
+                          false);
 }
 
 int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
@@ -555,7 +584,8 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   const int64_t P = mlp_param_count(a.din);
   float* flat = m->wpart + int64_t(mlp_grid()) * P;  // spare slot after the partials
-  rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, precision, st);
+  rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, precision, st,
+                         false);
   if (rc) return rc;
   k_scatter_grads<<<ceil_div(P, 256), 256, 0, st>>>(flat, a.din, g->w0, g->b0, g->w1, g->b1, g->w2,
                                                      g->b2);

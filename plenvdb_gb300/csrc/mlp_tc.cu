@@ -665,20 +665,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 }  // namespace
 
-// Packs the weights and runs the forward over rows k0rows [M, c0] (M = totals[1]);
-// pe [rays, pe_stride] holds each ray's view-direction PE.
-int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
-                        const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
-                        const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
-                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
-                        cudaStream_t st) {
+// Packs the FP32 weights into the BF16 tile blob (forward tiles, plus the
+// backward's transposed tiles when with_bwd).
+int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* b1,
+                const float* w2, const float* b2, int c0, int dpe, int with_bwd, void** blob,
+                size_t* blob_cap, cudaStream_t st) {
   if (c0 > 16 || c0 + dpe + 1 > kXK)
     return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
   if (rc) return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
-  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 0);
+  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), with_bwd);
   PVDB_CHECK_LAUNCH("k_pack");
+  return PVDB_OK;
+}
+
+// Runs the forward over rows k0rows [M, c0] (M = totals[1]); pe [rays,
+// pe_stride] holds each ray's view-direction PE. packed: the blob already
+// holds the weights of this call (else they are packed first).
+int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
+                        const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
+                        const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
+                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
+                        cudaStream_t st, int packed) {
+  int rc = PVDB_OK;
+  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 0, blob, blob_cap, st)))
+    return rc;
+  MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_fwd_tc, int(kSmFwdBytes));
   k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
       a, static_cast<const uint8_t*>(*blob), k0rows, ray, pe, pe_stride, totals, out, out_logits,
@@ -694,14 +707,11 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
                          const int32_t* ray, const float* pe, int pe_stride,
                          const uint32_t* totals, const float* rgb, const float* grad_rgb,
                          float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
-                         uint32_t* err, cudaStream_t st) {
-  if (c0 > 16 || c0 + dpe + 1 > kXK)
-    return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
-  int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
-  if (rc) return rc;
+                         uint32_t* err, cudaStream_t st, int packed) {
+  int rc = PVDB_OK;
+  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 1, blob, blob_cap, st)))
+    return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
-  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), 1);
-  PVDB_CHECK_LAUNCH("k_pack");
   PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
   k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob), k0rows,
                                                       ray, pe, pe_stride, totals, rgb, grad_rgb,

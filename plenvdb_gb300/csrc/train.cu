@@ -18,11 +18,14 @@ struct MlpArgs {
   const float* w2; const float* b2;
   int c0, dpe, din;
 };
+int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R, int precision,
+                cudaStream_t st);
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
-                     const float* viewdirs, float* rgb, int precision, cudaStream_t st);
+                     const float* viewdirs, float* rgb, int precision, cudaStream_t st,
+                     bool prepared);
 int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
                       const float* grad_rgb, float* grad_k0, float* grad_flat, int precision,
-                      cudaStream_t st);
+                      cudaStream_t st, bool prepared);
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st);
@@ -142,6 +145,31 @@ struct TrainArgs {
   bool prof;
 };
 
+// Side streams of the train step: independent branches (the rgbnet inputs
+// beside the march, the two grids' TV and Adam, the rgbnet Adam) run
+// concurrently. Fork: the side streams wait for st; join: st waits for them.
+// Inside a stream capture the same calls make parallel graph branches.
+static int side_streams(pvdb_march_s* m) {
+  if (m->side[0]) return PVDB_OK;
+  for (int i = 0; i < 2; ++i)
+    PVDB_CHECK_CUDA(cudaStreamCreateWithFlags(&m->side[i], cudaStreamNonBlocking));
+  for (int i = 0; i < 3; ++i)
+    PVDB_CHECK_CUDA(cudaEventCreateWithFlags(&m->side_ev[i], cudaEventDisableTiming));
+  return PVDB_OK;
+}
+static int fork_side(pvdb_march_s* m, cudaStream_t st, int n) {
+  PVDB_CHECK_CUDA(cudaEventRecord(m->side_ev[0], st));
+  for (int i = 0; i < n; ++i) PVDB_CHECK_CUDA(cudaStreamWaitEvent(m->side[i], m->side_ev[0], 0));
+  return PVDB_OK;
+}
+static int join_side(pvdb_march_s* m, cudaStream_t st, int n) {
+  for (int i = 0; i < n; ++i) {
+    PVDB_CHECK_CUDA(cudaEventRecord(m->side_ev[1 + i], m->side[i]));
+    PVDB_CHECK_CUDA(cudaStreamWaitEvent(st, m->side_ev[1 + i], 0));
+  }
+  return PVDB_OK;
+}
+
 // All device work of one train step: launches only, no host state changes
 // (so it can be captured into a graph and replayed).
 static int train_launches(const TrainArgs& t, cudaStream_t st) {
@@ -175,9 +203,15 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
     ~ProfGuard() { m->prof = false; }
   } guard{m};
   m->prof = t.prof;
-  int rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st);
+  int rc = side_streams(m);
   if (rc) return rc;
-  rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st);
+  // rgbnet inputs (PE, packed weights) beside the march
+  if ((rc = fork_side(m, st, 1))) return rc;
+  if ((rc = mlp_prepare(m, a, t.vd, n_rays, cfg->precision, m->side[0]))) return rc;
+  rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st);
+  if (rc) return rc;
+  if ((rc = join_side(m, st, 1))) return rc;
+  rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st, true);
   if (rc) return rc;
   if (t.prof) prof_mark(st, 3);
   rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
@@ -191,34 +225,42 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   PVDB_CHECK_LAUNCH("k_loss_sum");
   if (t.prof) prof_mark(st, 4);
   rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads,
-                         cfg->precision, st);
+                         cfg->precision, st, true);
   if (rc) return rc;
   if (t.prof) prof_mark(st, 5);
   rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);
   if (rc) return rc;
   // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
+  // TV of the two grids side by side (each grid's own touched list), then the
+  // three Adam updates side by side; the rgbnet Adam needs only the rgbnet
+  // gradients, complete since the MLP backward
   const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
+  if ((rc = fork_side(m, st, 2))) return rc;
+  rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
+                         t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0,
+                         m->side[1], t.ss_dev ? t.ss_dev + 2 : nullptr);
+  if (rc) return rc;
+  if (cfg->tv_weight_k0 > 0.f) {
+    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
+    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0,
+                               reinterpret_cast<pvdb_stream>(m->side[0]));
+    if (rc) return rc;
+  }
+  rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, m->side[0]);
+  if (rc) return rc;
   if (cfg->tv_weight_density > 0.f) {
     const float w = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
     rc = pvdb_grid_tv_add_grad(dg, w, w, w, cfg->tv_dense_mode, 0, s);
     if (rc) return rc;
   }
-  if (cfg->tv_weight_k0 > 0.f) {
-    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
-    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0, s);
-    if (rc) return rc;
-  }
   if (t.prof) prof_mark(st, 9);
   rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st);
   if (rc) return rc;
-  rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, st);
-  if (rc) return rc;
-  if (t.prof) prof_mark(st, 10);
-  rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
-                         t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0, st,
-                         t.ss_dev ? t.ss_dev + 2 : nullptr);
-  if (rc) return rc;
-  if (t.prof) prof_mark(st, 11);
+  if ((rc = join_side(m, st, 2))) return rc;
+  if (t.prof) {
+    prof_mark(st, 10);
+    prof_mark(st, 11);
+  }
   return PVDB_OK;
 }
 

@@ -255,6 +255,79 @@ __global__ void k_bmax_init(GridView g, uint32_t* bmax) {
   }
 }
 
+// k_tv for 12-channel grids: the voxel's and its neighbours' channels in
+// float4 loads; per-channel arithmetic and order as k_tv.
+__global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mode,
+                         const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+  const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list ? list[i >> 9] : int(i >> 9);
+    const int vox = int(i & 511);
+    if (!is_active(g, leaf, vox)) continue;
+    const int64_t t0 = (int64_t(leaf) * kLeafVox + vox) * 12;
+    float4* g4 = reinterpret_cast<float4*>(g.grad + t0);
+    float gc[12];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float4 x = g4[b];
+      gc[4 * b] = x.x; gc[4 * b + 1] = x.y; gc[4 * b + 2] = x.z; gc[4 * b + 3] = x.w;
+    }
+    bool any = dense_mode != 0;
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) any = any || gc[ch] != 0.f;
+    if (!any) continue;
+    int x, y, z;
+    slot_coord(g, leaf, vox, x, y, z);
+    if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) continue;
+    int nb[6];
+    nb[0] = z == 0 ? -2 : slot_of(g, x, y, z - 1);
+    nb[1] = z == g.reso[2] - 1 ? -2 : slot_of(g, x, y, z + 1);
+    nb[2] = y == 0 ? -2 : slot_of(g, x, y - 1, z);
+    nb[3] = y == g.reso[1] - 1 ? -2 : slot_of(g, x, y + 1, z);
+    nb[4] = x == 0 ? -2 : slot_of(g, x - 1, y, z);
+    nb[5] = x == g.reso[0] - 1 ? -2 : slot_of(g, x + 1, y, z);
+    const float wt[6] = {wz, wz, wy, wy, wx, wx};
+    float p[12], add[12];
+    const float4* d4 = reinterpret_cast<const float4*>(g.data + t0);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float4 v = d4[b];
+      p[4 * b] = v.x; p[4 * b + 1] = v.y; p[4 * b + 2] = v.z; p[4 * b + 3] = v.w;
+    }
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) add[ch] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      if (nb[q] == -2) continue;  // (adding 0.f leaves the sum as it is)
+      float vn[12];
+      if (nb[q] < 0) {
+#pragma unroll
+        for (int ch = 0; ch < 12; ++ch) vn[ch] = g.background;
+      } else {
+        const float4* n4 = reinterpret_cast<const float4*>(g.data + int64_t(nb[q]) * 12);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const float4 v = n4[b];
+          vn[4 * b] = v.x; vn[4 * b + 1] = v.y; vn[4 * b + 2] = v.z; vn[4 * b + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int ch = 0; ch < 12; ++ch) add[ch] += wt[q] * tv_clamp(p[ch] - vn[ch]);
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      float o[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int ch = 4 * b + e;
+        o[e] = (!dense_mode && gc[ch] == 0.f) ? gc[ch] : gc[ch] + add[ch];
+      }
+      g4[b] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+  }
+}
+
 __global__ void k_touched_compact(const uint8_t* __restrict__ touched, int nleaf, int32_t* list,
                                   uint32_t* count) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -694,8 +767,12 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
     int rc = touched_list(g, st);
     if (rc) return rc;
   }
-  k_tv<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
-                                      use_list ? g->d_tlist : nullptr, g->d_tcount);
+  if (g->C == 12)
+    k_tv_c12<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
+                                            use_list ? g->d_tlist : nullptr, g->d_tcount);
+  else
+    k_tv<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
+                                        use_list ? g->d_tlist : nullptr, g->d_tcount);
   PVDB_CHECK_LAUNCH("k_tv");
   if (dense_mode) g->all_touched = true;
   return PVDB_OK;

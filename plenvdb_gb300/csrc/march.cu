@@ -439,12 +439,17 @@ __device__ __forceinline__ bool seg_head(const uint32_t* __restrict__ skeys, int
   return key != kInvalidKey && (i == 0 || skeys[i - 1] != key);
 }
 
+// Marks (or, clear, unmarks) the cells present; when marking, also lists the
+// segment heads (in no particular order: each head's work is independent).
 __global__ void k_cell_map_set(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
-                               int32_t* map, int clear) {
+                               int32_t* map, int clear, int32_t* heads, uint32_t* nheads) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
-    if (seg_head(skeys, i)) map[skeys[i]] = clear ? -1 : int32_t(i);
+    if (seg_head(skeys, i)) {
+      map[skeys[i]] = clear ? -1 : int32_t(i);
+      if (!clear) heads[atomicAdd(nheads, 1u)] = int32_t(i);
+    }
 }
 
 // Corner weight c of the multi-channel formula, ((a*b)*c) (colorvdb.cu:100-107).
@@ -461,14 +466,15 @@ template <int NQ>
 __global__ void __launch_bounds__(256)
     k_cell_partials(GridView gd, GridView gc, const uint32_t* __restrict__ skeys,
                     const uint32_t* __restrict__ svals, const uint32_t* n_dev,
+                    const int32_t* __restrict__ heads, const uint32_t* __restrict__ nheads,
                     const float4* __restrict__ rec, float* __restrict__ pd,
                     float4* __restrict__ pk, uint8_t* touched_d, uint8_t* touched_c) {
   const int64_t n = *n_dev;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n * 8;
+  const int64_t nh = *nheads;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nh * 8;
        t += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t h = t >> 3;
+    const int64_t h = heads[t >> 3];
     const int c = int(t & 7);
-    if (!seg_head(skeys, h)) continue;
     const uint32_t key = skeys[h];
     int ci, cj, ck, di, dj, dk;
     cell_decode(gd.ldim, key, ci, cj, ck);
@@ -575,7 +581,8 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const int grid = stride_grid();
   const GridView gv = density->view();
   const GridView kv = NQ ? k0->view() : gv;
-  k_cell_partials<NQ><<<grid * 2, 256, 0, st>>>(gv, kv, skeys, svals, m->w.totals + 0, m->w.b_rec,
+  k_cell_partials<NQ><<<grid * 2, 256, 0, st>>>(gv, kv, skeys, svals, m->w.totals + 0,
+                                                m->cell_heads, m->w.totals + 5, m->w.b_rec,
                                                 m->cell_pd, m->cell_pk, density->d_touched,
                                                 NQ ? k0->d_touched : density->d_touched);
   PVDB_CHECK_LAUNCH("k_cell_partials");
@@ -761,7 +768,8 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   const int C = use_k0 ? k0->C : 0;
   PVDB_REQUIRE(C <= 16, "the march backward takes at most 16 k0 channels");
   const int nq = (C + 3) / 4;
-  if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)) ||
+  if ((rc = dev_reserve((void**)&m->cell_heads, &m->cell_heads_cap, size_t(nmax) * 4)) ||
+      (rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)) ||
       (rc = dev_reserve((void**)&m->cell_pd, &m->cell_pd_cap, size_t(ncells) * 8 * 4)) ||
       (nq && (rc = dev_reserve((void**)&m->cell_pk, &m->cell_pk_cap, size_t(ncells) * 8 * nq * 16))))
     return rc;
@@ -778,7 +786,9 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   const uint32_t* skeys = m->red.keys[buf];
   const uint32_t* svals = m->red.vals[buf];
   const int grid = stride_grid();
-  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 0);
+  PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals + 5, 0, 4, st));
+  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 0, m->cell_heads,
+                                       m->w.totals + 5);
   PVDB_CHECK_LAUNCH("k_cell_map_set");
   switch (nq) {
     case 0: rc = cell_reduce_launch<0>(m, density, k0, skeys, svals, st); break;
@@ -788,7 +798,7 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
     default: rc = cell_reduce_launch<4>(m, density, k0, skeys, svals, st); break;
   }
   if (rc) return rc;
-  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 1);
+  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 1, nullptr, nullptr);
   PVDB_CHECK_LAUNCH("k_cell_map_set(clear)");
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
@@ -877,6 +887,7 @@ int pvdb_march_destroy(pvdb_march m) {
   dev_free(m->cell_map);
   dev_free(m->cell_pd);
   dev_free(m->cell_pk);
+  dev_free(m->cell_heads);
   dev_free(m->g_in);
   dev_free(m->g_scal);
   if (m->g_exec) cudaGraphExecDestroy(m->g_exec);

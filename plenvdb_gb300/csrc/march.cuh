@@ -50,7 +50,7 @@ struct MarchW {
   float4* b_rec;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 sort look-back wait),
-  // [4] samples evaluated
+  // [4] samples evaluated, [5] touched cells (backward)
   uint32_t* totals;
 };
 
@@ -70,6 +70,8 @@ struct pvdb_march_s {
   float4* cell_pk = nullptr;    // [cells][8 corners][nq] k0 partial sums
   size_t cell_pk_cap = 0;       // bytes
   size_t b_rec_cap = 0;         // bytes of w.b_rec
+  int32_t* cell_heads = nullptr;  // sorted index of each touched cell's first sample
+  size_t cell_heads_cap = 0;      // bytes
   uint32_t* scan_partial = nullptr;
   size_t scan_partial_cap = 0;
   // state of the last forward

@@ -72,6 +72,69 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
   }
 }
 
+// The same update for 12-channel grids (k0), one thread per voxel with the
+// channels in float4 loads; the four Vec3 groups keep their own skip rule.
+// Per-channel arithmetic is identical to k_vdb_adam.
+__global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restrict__ v,
+                               const float* __restrict__ perlr, float stepsz,
+                               const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
+                               int mode, int zero_after, const int32_t* __restrict__ list,
+                               const uint32_t* __restrict__ count) {
+  const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
+  if (stepsz_dev) stepsz = *stepsz_dev;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list ? list[i >> 9] : int(i >> 9);
+    const int vox = int(i & 511);
+    if (!((__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull)) continue;
+    const int64_t slot = int64_t(leaf) * kLeafVox + vox;
+    float4* g4 = reinterpret_cast<float4*>(g.grad + slot * 12);
+    float gr[12];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float4 x = g4[b];
+      gr[4 * b] = x.x; gr[4 * b + 1] = x.y; gr[4 * b + 2] = x.z; gr[4 * b + 3] = x.w;
+    }
+    bool live[4];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      live[q] = mode != 1 || gr[3 * q] != 0.f || gr[3 * q + 1] != 0.f || gr[3 * q + 2] != 0.f;
+      any = any || live[q];
+    }
+    if (!any) continue;
+    float4* m4 = reinterpret_cast<float4*>(m + slot * 12);
+    float4* v4 = reinterpret_cast<float4*>(v + slot * 12);
+    float4* d4 = reinterpret_cast<float4*>(g.data + slot * 12);
+    float mm[12], vv[12], dd[12];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float4 a = m4[b], c = v4[b], d = d4[b];
+      mm[4 * b] = a.x; mm[4 * b + 1] = a.y; mm[4 * b + 2] = a.z; mm[4 * b + 3] = a.w;
+      vv[4 * b] = c.x; vv[4 * b + 1] = c.y; vv[4 * b + 2] = c.z; vv[4 * b + 3] = c.w;
+      dd[4 * b] = d.x; dd[4 * b + 1] = d.y; dd[4 * b + 2] = d.z; dd[4 * b + 3] = d.w;
+    }
+    const float lrf = mode == 2 ? perlr[slot] : 1.f;
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) {
+      if (!live[ch / 3]) continue;
+      const float mn = b0 * mm[ch] + (1 - b0) * gr[ch];
+      const float vn = b1 * vv[ch] + (1 - b1) * gr[ch] * gr[ch];
+      mm[ch] = mn;
+      vv[ch] = vn;
+      const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
+      dd[ch] = dd[ch] - num / (eps + sqrtf(vn));
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      m4[b] = make_float4(mm[4 * b], mm[4 * b + 1], mm[4 * b + 2], mm[4 * b + 3]);
+      v4[b] = make_float4(vv[4 * b], vv[4 * b + 1], vv[4 * b + 2], vv[4 * b + 3]);
+      d4[b] = make_float4(dd[4 * b], dd[4 * b + 1], dd[4 * b + 2], dd[4 * b + 3]);
+      if (zero_after) g4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
 // zero_after for voxels the Adam pass skipped (mode 1, all-zero gradient):
 // nothing to do, their gradient is already zero.
 
@@ -142,10 +205,16 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
       int rc = touched_list(g, st);
       if (rc) return rc;
     }
-    k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
-        g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
-        mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0, o->beta1,
-        mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
+    if (g->C == 12)
+      k_vdb_adam_c12<<<stride_grid(), 256, 0, st>>>(
+          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
+          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
+    else
+      k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
+          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
+          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
     PVDB_CHECK_LAUNCH("k_vdb_adam");
   }
   if (zero_after && g->nleaf) {

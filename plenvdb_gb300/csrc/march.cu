@@ -11,8 +11,9 @@
 // kept samples. Only per-ray alpha / weight / step lists are kept for the
 // backward.
 //
-// k_march_rows lays the colour samples (weight > thres, dvgo.py:329-335) out as
-// dense rows and samples the k0 grid there (colorvdb.cu:81-111).
+// k_march_rowmeta / k_march_k0 lay the colour samples (weight > thres,
+// dvgo.py:329-335) out as dense rows and sample the k0 grid there
+// (colorvdb.cu:81-111).
 //
 // Backward (k_march_bwd) recovers transmittance from the saved alphas and
 // weights, runs alpha2weight_backward (:653-677) as a suffix scan and
@@ -75,20 +76,19 @@ __global__ void __launch_bounds__(256)
   atomicAdd(W.totals + 4, uint32_t(ns));
 }
 
+// One block per ray, threads over the ray's samples.
 __global__ void __launch_bounds__(256)
-    k_march_alpha(GridView gd, int R, MarchP P, MarchW W) {
-  const int64_t total = int64_t(R) * P.cap;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int r = int(t / P.cap);
-    const int k = int(t - int64_t(r) * P.cap);
-    if (k >= W.ray_ns[r]) continue;
-    RaySetup rs;
+    k_march_alpha(GridView gd, MarchP P, MarchW W) {
+  const int r = blockIdx.x;
+  const int ns = W.ray_ns[r];
+  RaySetup rs;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      rs.start[a] = W.ray_sd[r * 6 + a];
-      rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
-    }
+  for (int a = 0; a < 3; ++a) {
+    rs.start[a] = W.ray_sd[r * 6 + a];
+    rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+  }
+  const int64_t sbase = int64_t(r) * P.cap;
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
     float p[3];
     ray_point(rs, P.stepdist, k, p);
     float alpha = 0.f;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int a = 0; a < 3; ++a)
         b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
-      const uint32_t key = __ldg(gd.bmax + (int64_t(b[0]) * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
+      const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
       skip = fkey_inv(key) < P.sigma_skip;
     }
     if (!skip && !out_of_bbox(p, P.mn, P.mx) &&
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256)
       const float a = raw2alpha(sigma, P.shift, P.interval, e);
       if (a > P.thr) alpha = a;
     }
-    W.k_alpha[t] = alpha;
+    W.k_alpha[sbase + k] = alpha;
   }
 }
 
@@ -262,12 +262,7 @@ __device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[
   float sc[8];
   corner_scales(idx[0] - float(i), idx[1] - float(j), idx[2] - float(k), sc);
   int slots[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    int di, dj, dk;
-    corner_delta(c, di, dj, dk);
-    slots[c] = slot_of(g, i + di, j + dj, k + dk);
-  }
+  corner_slots(g, i, j, k, slots);
   if (g.C == 12) {
     float acc[12];
 #pragma unroll
@@ -303,32 +298,43 @@ __device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[
   }
 }
 
-// Colour rows, one thread per kept-sample slot (r, i): a colour sample gets
-// its global row m = color_off[r] + its rank in the ray, the k0 trilinear at
-// its position (colorvdb.cu:81-111) and the row record; k_row becomes m.
-__global__ void __launch_bounds__(256)
-    k_march_rows(GridView gk, int R, MarchP P, MarchW W) {
-  const int64_t total = int64_t(R) * P.cap;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < total;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int r = int(t / P.cap);
-    const int i = int(t - int64_t(r) * P.cap);
-    if (i >= int(W.n_kept[r])) continue;
+// Colour rows. k_march_rowmeta (warp per ray): each colour sample gets its
+// global row m = color_off[r] + its rank in the ray and the row record;
+// k_row becomes m. k_march_k0 (thread per row): the k0 trilinear at the row's
+// position (colorvdb.cu:81-111).
+__global__ void __launch_bounds__(kMarchThreads)
+    k_march_rowmeta(int R, MarchP P, MarchW W) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * kMarchWarps + warp;
+  if (r >= R) return;
+  const int nk = int(W.n_kept[r]);
+  const int64_t sbase = int64_t(r) * P.cap;
+  const int64_t coff = W.color_off[r];
+  for (int i = lane; i < nk; i += 32) {
+    const int64_t t = sbase + i;
     const int32_t rank = W.k_row[t];
     if (rank < 0) continue;
-    const int64_t m = int64_t(W.color_off[r]) + rank;
-    const int32_t k = W.k_step[t] & 0x7fffffff;
-    RaySetup rs;
-    load_setup(W, r, rs);
-    float p[3], idx[3];
-    ray_point(rs, P.stepdist, k, p);
-    world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-    if (gk.C > 0) k0_trilinear(gk, idx, W.r_k0 + m * gk.C);
+    const int64_t m = coff + rank;
     W.r_w[m] = W.k_w[t];
     W.r_alpha[m] = W.k_alpha[t];
     W.r_ray[m] = r;
-    W.r_step[m] = k;
+    W.r_step[m] = W.k_step[t] & 0x7fffffff;
     W.k_row[t] = int32_t(m);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_march_k0(GridView gk, MarchP P, MarchW W) {
+  const int64_t M = W.totals[1];
+  for (int64_t m = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; m < M;
+       m += int64_t(gridDim.x) * blockDim.x) {
+    const int r = W.r_ray[m];
+    RaySetup rs;
+    load_setup(W, r, rs);
+    float p[3], idx[3];
+    ray_point(rs, P.stepdist, W.r_step[m], p);
+    world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+    k0_trilinear(gk, idx, W.r_k0 + m * gk.C);
   }
 }
 
@@ -727,8 +733,7 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     const int nb = ceil_div(R, kMarchWarps);
     k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_setup");
-    k_march_alpha<<<int(std::min<int64_t>(ceil_div(int64_t(R) * m->cap, 256), int64_t(num_sms()) * 32)),
-                    256, 0, st>>>(density->view(), R, m->p, m->w);
+    k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_alpha");
     k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_chain");
@@ -737,9 +742,13 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
     if (k0) gk = k0->view();
-    k_march_rows<<<int(std::min<int64_t>(ceil_div(int64_t(R) * m->cap, 256), int64_t(num_sms()) * 16)),
-                   256, 0, st>>>(gk, R, m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_rows");
+    k_march_rowmeta<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_rowmeta");
+    if (k0) {
+      k_march_k0<<<int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16)), 256, 0,
+                   st>>>(gk, m->p, m->w);
+      PVDB_CHECK_LAUNCH("k_march_k0");
+    }
     if (m->prof) prof_mark(st, 2);
   }
   m->has_fwd = true;

@@ -195,21 +195,51 @@ __device__ __forceinline__ void corner_delta(int c, int& di, int& dj, int& dk) {
 // Floor to int as nanovdb::Vec3::floor (Floor(x) = int32(floorf(x))).
 __device__ __forceinline__ int ifloor(float x) { return int(floorf(x)); }
 
+// Slots of the 8 trilinear corners of cell (i,j,k) in the reference's corner
+// order (see corner_delta), -1 where a corner lies in no allocated leaf. When
+// the cell does not cross a leaf face ((i|j|k) & 7 < 7 per axis) all corners
+// share one leaf: one table lookup, and the offsets follow from the voxel
+// layout (+64 x, +8 y, +1 z).
+__device__ __forceinline__ void corner_slots(const GridView& g, int i, int j, int k, int s[8]) {
+  if ((i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7) {
+    const int l = leaf_of(g, i, j, k);
+    const int b = l < 0 ? -1 : ((l << 9) | vox_offset(i, j, k));
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      int di, dj, dk;
+      corner_delta(c, di, dj, dk);
+      s[c] = b < 0 ? -1 : b + (di << 6) + (dj << 3) + dk;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      int di, dj, dk;
+      corner_delta(c, di, dj, dk);
+      s[c] = slot_of(g, i + di, j + dj, k + dk);
+    }
+  }
+}
+
 // Density trilinear with the reference's association: for each corner in order,
 // res += ((v*(1-u))*(1-v))*(1-w) (densityvdb.cu:115-123).
 __device__ __forceinline__ float trilinear1(const GridView& g, float x, float y, float z) {
   const int i = ifloor(x), j = ifloor(y), k = ifloor(z);
   const float u = x - float(i), v = y - float(j), w = z - float(k);
   const float iu = 1.f - u, iv = 1.f - v, iw = 1.f - w;
+  int s[8];
+  corner_slots(g, i, j, k, s);
+  float val[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) val[c] = s[c] < 0 ? g.background : __ldg(g.data + s[c]);
   float r = 0.f;
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j, k), iu), iv), iw));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j, k + 1), iu), iv), w));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j + 1, k + 1), iu), v), w));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i, j + 1, k), iu), v), iw));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j + 1, k), u), v), iw));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j + 1, k + 1), u), v), w));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j, k + 1), u), iv), w));
-  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(value1(g, i + 1, j, k), u), iv), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[0], iu), iv), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[1], iu), iv), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[2], iu), v), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[3], iu), v), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[4], u), v), iw));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[5], u), v), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[6], u), iv), w));
+  r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[7], u), iv), iw));
   return r;
 }
 

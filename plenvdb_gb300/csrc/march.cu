@@ -888,7 +888,7 @@ int pvdb_march_destroy(pvdb_march m) {
   MarchW& w = m->w;
   void* ptrs[] = {w.ray_sd, w.ray_ns, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
                   w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec,
-                  w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed,
+                  w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed, m->mlp_xt,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,
                   m->t_loss_part, m->t_rgb_marched};
   for (void* p : ptrs) dev_free(p);

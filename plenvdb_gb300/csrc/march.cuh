@@ -88,6 +88,8 @@ struct pvdb_march_s {
   size_t wpart_cap = 0;
   void* mlp_packed = nullptr;    // packed BF16 weights for the tensor-core path
   size_t mlp_packed_cap = 0;
+  void* mlp_xt = nullptr;        // BF16 X tiles of the rows (tensor-core path)
+  size_t mlp_xt_cap = 0;
   // train-step scratch (train.cu)
   float* t_rgb = nullptr;        // [M_max,3]
   float* t_grad_rgb = nullptr;   // [M_max,3]

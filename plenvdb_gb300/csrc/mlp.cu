@@ -422,8 +422,9 @@ int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* 
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
                         const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
-                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
-                        cudaStream_t st, int packed);
+                        int64_t max_rows, float* out, int out_logits, void** blob,
+                        size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                        cudaStream_t st, int packed, int x_ready);
 
 // Inputs of the rgbnet that depend only on the rays and the weights: the
 // per-ray PE (FP32 path: and hpe) and, BF16 path, the packed BF16 weight
@@ -460,8 +461,9 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
   }
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
-                               m->w.r_ray, pe, kMaxPe, m->w.totals, rgb, 0, &m->mlp_packed,
-                               &m->mlp_packed_cap, m->w.totals + 3, st, prepared ? 1 : 0);
+                               m->w.r_ray, pe, kMaxPe, m->w.totals, m->slots, rgb, 0,
+                               &m->mlp_packed, &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap,
+                               m->w.totals + 3, st, prepared ? 1 : 0, 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
       a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
@@ -472,9 +474,10 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
 // Rows from any producer (the merged renderer): k0rows [M, c0], ray [M] ->
 // viewdirs [R,3]; M = totals[1]. hpe_buf holds R*(128+32) floats.
 int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
-                     const float* viewdirs, int R, const uint32_t* totals, float* out,
-                     int out_logits, float* hpe_buf, int precision, void** blob,
-                     size_t* blob_cap, uint32_t* err, cudaStream_t st) {
+                     const float* viewdirs, int R, const uint32_t* totals, int64_t max_rows,
+                     float* out, int out_logits, float* hpe_buf, int precision, void** blob,
+                     size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                     cudaStream_t st) {
   if (R <= 0) return PVDB_OK;
   float* hpe = hpe_buf;
   float* pe = hpe_buf + size_t(R) * kW;
@@ -482,7 +485,8 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
-                               kMaxPe, totals, out, out_logits, blob, blob_cap, err, st, 0);
+                               kMaxPe, totals, max_rows, out, out_logits, blob, blob_cap, xt,
+                               xt_cap, err, st, 0, 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
                                                                   out, out_logits);
@@ -493,9 +497,10 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
 int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                          const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
                          const int32_t* ray, const float* pe, int pe_stride,
-                         const uint32_t* totals, const float* rgb, const float* grad_rgb,
-                         float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
-                         uint32_t* err, cudaStream_t st, int packed);
+                         const uint32_t* totals, int64_t max_rows, const float* rgb,
+                         const float* grad_rgb, float* grad_k0, float* wpart, int grid,
+                         void** blob, size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                         cudaStream_t st, int packed, int x_ready);
 
 // hpe/pe of the current forward must still be in the workspace; prepared: the
 // BF16 backward tiles were packed by mlp_prepare.
@@ -513,9 +518,10 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
   const int G = mlp_grid();
   if (precision == 1) {
     rc = mlp_tc_backward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, m->w.r_ray,
-                              m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, rgb,
-                              grad_rgb, grad_k0, m->wpart, G, &m->mlp_packed, &m->mlp_packed_cap,
-                              m->w.totals + 3, st, prepared ? 1 : 0);
+                              m->hpe + size_t(m->max_rays) * kW, kMaxPe, m->w.totals, m->slots,
+                              rgb, grad_rgb, grad_k0, m->wpart, G, &m->mlp_packed,
+                              &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap, m->w.totals + 3, st,
+                              prepared ? 1 : 0, prepared ? 1 : 0);
     if (rc) return rc;
     k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
     PVDB_CHECK_LAUNCH("k_wgrad_reduce");

@@ -11,8 +11,9 @@
 //   L0  Z0 = X . W0f^T            3 MMAs (K=48)        H0 = relu(Z0)
 //   L1  Z1 = H0 . W1^T            8 MMAs (K=128)       H1 = relu(Z1 + b1)
 //   L2  Z2 = H1 . W2p^T           8 MMAs, N=16         rgb = sigmoid(Z2 + b2)
-// The next tile's X is loaded into registers while the current tile's MMAs
-// run. One thread issues the MMAs; completion is signalled through an
+// X tiles are built once per step (k_build_x) and each CTA fetches the next
+// tile's with a bulk copy while the current tile computes. One thread issues
+// the MMAs; completion is signalled through an
 // mbarrier (tcgen05.commit). Epilogues read TMEM with tcgen05.ld (warp w reads
 // lanes 32*(w%4).., columns 64*(w/4)..), apply bias/activation in FP32 and
 // store BF16 into shared memory in the canonical layout the next MMA reads.
@@ -38,12 +39,13 @@ constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16 q][128 n]
 constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T  [128 n][16 c]    86016
 constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 90112
 // shared-memory layout of the forward kernel
-constexpr uint32_t kSmX = kPackFwdBytes;              // X tile [128 x 48] bf16
-constexpr uint32_t kSmH = kSmX + 128 * kXK * 2;       // H tile [128 x 128] bf16
+constexpr uint32_t kXTile = 128 * kXK * 2;             // 12288 B: one X tile
+constexpr uint32_t kSmX = kPackFwdBytes;              // two X tiles [128 x 48] bf16
+constexpr uint32_t kSmH = kSmX + 2 * kXTile;          // H tile [128 x 128] bf16
 constexpr uint32_t kSmB1 = kSmH + 128 * 128 * 2;      // b1 f32[128]
 constexpr uint32_t kSmB2 = kSmB1 + 128 * 4;           // b2 f32[16]
-constexpr uint32_t kSmBar = kSmB2 + 16 * 4;           // mbarrier (8 B)
-constexpr uint32_t kSmTmem = kSmBar + 8;              // TMEM base address (4 B)
+constexpr uint32_t kSmBar = kSmB2 + 16 * 4;           // mbarriers: MMA, X0, X1 (24 B)
+constexpr uint32_t kSmTmem = kSmBar + 24;             // TMEM base address (4 B)
 constexpr uint32_t kSmFlag = kSmTmem + 4;             // timeout flag (4 B)
 constexpr uint32_t kSmFwdBytes = kSmFlag + 16;
 static_assert(2 * kSmFwdBytes <= 228 * 1024, "two forward CTAs must fit on an SM");
@@ -106,49 +108,49 @@ __device__ __forceinline__ bool wait_or_flag(uint64_t* bar, uint32_t parity, uin
   return *((volatile uint32_t*)flag) == 0;
 }
 
-// The X chunks of one tile held by one thread: chunk tid + 256*i (i < 3) is
-// row (chunk / 6), columns 8*(chunk % 6) .. +7.
-struct XRegs {
-  float v[3][8];
-};
-
-__device__ __forceinline__ void x_load(const MlpArgsTc& a, const float* __restrict__ k0,
-                                       const int32_t* __restrict__ ray,
-                                       const float* __restrict__ pe, int pe_stride, int64_t row0,
-                                       int64_t M, XRegs& x) {
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int c = threadIdx.x + kTcThreads * i;
-    const int r = c / 6, qb = (c % 6) * 8;
-    const int64_t m = row0 + r;
+// The rows' X tiles in global memory, tile after tile in the canonical BF16
+// K-major layout the MMAs read (one 16-byte chunk per thread): the MLP
+// kernels fetch a tile with one bulk copy.
+__global__ void __launch_bounds__(256)
+    k_build_x(MlpArgsTc a, const float* __restrict__ k0, const int32_t* __restrict__ ray,
+              const float* __restrict__ pe, int pe_stride, const uint32_t* __restrict__ totals,
+              uint8_t* xt) {
+  const int64_t M = totals[1];
+  const int64_t nchunks = (M + 127) / 128 * (128 * 6);
+  for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < nchunks;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t tile = c / (128 * 6);
+    const int w = int(c - tile * (128 * 6));
+    const int r = w / 6, qb = (w % 6) * 8;
+    const int64_t m = tile * 128 + r;
+    float v[8];
     if (m < M) {
       const int64_t rr = __ldg(ray + m);
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
         const int qq = qb + e;
-        x.v[i][e] = qq < a.c0 ? __ldg(k0 + m * a.c0 + qq)
-                    : qq < a.din ? __ldg(pe + rr * pe_stride + (qq - a.c0))
-                    : qq == a.din ? 1.f : 0.f;
+        v[e] = qq < a.c0 ? __ldg(k0 + m * a.c0 + qq)
+               : qq < a.din ? __ldg(pe + rr * pe_stride + (qq - a.c0))
+               : qq == a.din ? 1.f : 0.f;
       }
     } else {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) x.v[i][e] = 0.f;
+      for (int e = 0; e < 8; ++e) v[e] = 0.f;
     }
+    uint4 pk;
+    pk.x = tc::pack_bf16(v[0], v[1]);
+    pk.y = tc::pack_bf16(v[2], v[3]);
+    pk.z = tc::pack_bf16(v[4], v[5]);
+    pk.w = tc::pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(xt + tile * kXTile + tc::kmaj(r, qb, kXK)) = pk;
   }
 }
 
-__device__ __forceinline__ void x_store(uint8_t* xs, const XRegs& x) {
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int c = threadIdx.x + kTcThreads * i;
-    const int r = c / 6, qb = (c % 6) * 8;
-    uint4 pk;
-    pk.x = tc::pack_bf16(x.v[i][0], x.v[i][1]);
-    pk.y = tc::pack_bf16(x.v[i][2], x.v[i][3]);
-    pk.z = tc::pack_bf16(x.v[i][4], x.v[i][5]);
-    pk.w = tc::pack_bf16(x.v[i][6], x.v[i][7]);
-    *reinterpret_cast<uint4*>(xs + tc::kmaj(r, qb, kXK)) = pk;
-  }
+// Thread 0 starts the bulk copy of X tile `t` into shared buffer `b`.
+__device__ __forceinline__ void x_fetch(uint8_t* sm_x, const uint8_t* xt, int64_t t,
+                                        uint64_t* xbar) {
+  tc::mbar_expect_tx(xbar, kXTile);
+  tc::bulk_g2s(sm_x, xt + t * kXTile, kXTile, xbar);
 }
 
 // 32 FP32 values (+ bias, relu) -> 4 x 8 BF16 into a K-major tile (ktot columns).
@@ -170,8 +172,7 @@ __device__ __forceinline__ void store_relu32(uint8_t* tile, int row, int col0, i
 }
 
 __global__ void __launch_bounds__(kTcThreads, 2)
-    k_mlp_fwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const float* __restrict__ k0,
-                 const int32_t* __restrict__ ray, const float* __restrict__ pe, int pe_stride,
+    k_mlp_fwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const uint8_t* __restrict__ xt,
                  const uint32_t* __restrict__ totals, float* out, int out_logits, uint32_t* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
@@ -190,9 +191,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   }
   if (tid < 128) b1s[tid] = a.b1[tid];
   if (tid < 16) b2s[tid] = tid < 3 ? a.b2[tid] : 0.f;
+  uint64_t* xbar = bar + 1;  // X tile barriers, one per buffer
   if (tid == 0) {
     *flag = 0;
     tc::mbar_init(bar, 1);
+    tc::mbar_init(xbar, 1);
+    tc::mbar_init(xbar + 1, 1);
+    x_fetch(sm + kSmX, xt, blockIdx.x, xbar);
   }
   if (warp == 0) {
     tc::tmem_alloc(tmem_slot, kTmemCols);
@@ -208,25 +213,26 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const int q = warp & 3, half = warp >> 2;
   const int row = 32 * q + lane;  // TMEM lane = tile row of this thread
   const uint32_t t_lane = tmem + (uint32_t(32 * q) << 16);
-  uint32_t phase = 0;
+  uint32_t phase = 0, xph[2] = {0u, 0u};
   bool ok = true;
-  XRegs xr;
-  x_load(a, k0, ray, pe, pe_stride, int64_t(blockIdx.x) * 128, M, xr);
-  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+  int it = 0;
+  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
     const int64_t row0 = t * 128;
-    x_store(sm + kSmX, xr);
-    tc::fence_async_smem();
-    __syncthreads();
+    const int b = it & 1;
+    // the next tile's X travels while this tile computes (its buffer was last
+    // read by the previous tile's layer-0 MMA, complete)
+    if (tid == 0 && t + gridDim.x < ntiles) x_fetch(sm + kSmX + (b ^ 1) * kXTile, xt, t + gridDim.x, xbar + (b ^ 1));
+    ok = wait_or_flag(xbar + b, xph[b], flag, err);
+    if (!ok) break;
+    xph[b] ^= 1u;
     if (tid == 0) {
       tc::fence_after();
 #pragma unroll
       for (int s = 0; s < 3; ++s)
-        tc::mma_bf16(tmem, tc::make_desc(sbase + kSmX + 256 * s, 128, 768),
+        tc::mma_bf16(tmem, tc::make_desc(sbase + kSmX + b * kXTile + 256 * s, 128, 768),
                      tc::make_desc(sbase + kOffW0 + 256 * s, 128, 768), id_n128, s > 0);
       tc::mma_commit(bar);
     }
-    // the next tile's inputs travel while this tile computes
-    if (t + gridDim.x < ntiles) x_load(a, k0, ray, pe, pe_stride, (t + gridDim.x) * 128, M, xr);
     ok = wait_or_flag(bar, phase, flag, err);
     phase ^= 1;
     if (!ok) break;
@@ -292,9 +298,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     __syncthreads();
   }
   if (!ok) {
-    // a wait gave up: give the MMAs in flight one more bounded wait before the
-    // TMEM they write is released
+    // a wait gave up: give the MMAs and X copies in flight one more bounded
+    // wait before their TMEM and shared memory are released
     tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
+    tc::mbar_wait(xbar, xph[0], kWaitIters);
+    tc::mbar_wait(xbar + 1, xph[1], kWaitIters);
   }
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
@@ -322,8 +330,8 @@ constexpr uint32_t kBdZ1 = 0;                        // dZ1 [128 r][128 n]
 constexpr uint32_t kBH1 = kBdZ1 + 128 * 128 * 2;     // H1, later dZ0 [128 r][128 n]
 constexpr uint32_t kBdZ0 = kBH1;
 constexpr uint32_t kBH0 = kBH1 + 128 * 128 * 2;      // H0  [128 r][144 k], col 128 = 1
-constexpr uint32_t kBX = kBH0 + 128 * 144 * 2;       // X   [128 r][48 q]: k0 | PE | 1 | 0
-constexpr uint32_t kBDl = kBX + 128 * kXK * 2;       // dl  [128 r][16 c]
+constexpr uint32_t kBX = kBH0 + 128 * 144 * 2;       // X x 2 [128 r][48 q]: k0 | PE | 1 | 0
+constexpr uint32_t kBDl = kBX + 2 * kXTile;          // dl  [128 r][16 c]
 constexpr uint32_t kBW = kBDl + 128 * 16 * 2;        // weights
 constexpr uint32_t kBW0f = kBW;                      // W0f  [128 n][48 q]
 constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;     // W1   [128 n][128 k]
@@ -331,8 +339,8 @@ constexpr uint32_t kBW1T = kBW1 + 128 * 128 * 2;     // W1T  [128 k][128 n]
 constexpr uint32_t kBW0T = kBW1T + 128 * 128 * 2;    // W0kT [16 q][128 n]
 constexpr uint32_t kBW2T = kBW0T + 16 * 128 * 2;     // W2T  [128 n][16 c]
 constexpr uint32_t kBB1 = kBW2T + 128 * 16 * 2;      // b1 f32[128]
-constexpr uint32_t kBBar = kBB1 + 128 * 4;
-constexpr uint32_t kBTmem = kBBar + 8;
+constexpr uint32_t kBBar = kBB1 + 128 * 4;          // mbarriers: MMA, X0, X1
+constexpr uint32_t kBTmem = kBBar + 24;
 constexpr uint32_t kBFlag = kBTmem + 4;
 constexpr uint32_t kSmBwdBytes = kBFlag + 12;
 static_assert(kSmBwdBytes <= 232448, "backward tile exceeds 227 KB of shared memory");
@@ -367,8 +375,7 @@ __device__ __forceinline__ uint4 mask_pack(const float* v, uint4 h) {
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_mlp_bwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const float* __restrict__ k0,
-                 const int32_t* __restrict__ ray, const float* __restrict__ pe, int pe_stride,
+    k_mlp_bwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const uint8_t* __restrict__ xt,
                  const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
                  const float* __restrict__ grad_rgb, float* grad_k0, float* wpart, uint32_t* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
@@ -405,9 +412,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 128, 144)) = one;
     *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 136, 144)) = make_uint4(0u, 0u, 0u, 0u);
   }
+  uint64_t* xbar = bar + 1;  // X tile barriers, one per buffer
   if (tid == 0) {
     *flag = 0;
     tc::mbar_init(bar, 1);
+    tc::mbar_init(xbar, 1);
+    tc::mbar_init(xbar + 1, 1);
+    x_fetch(sm + kBX, xt, blockIdx.x, xbar);
   }
   if (warp == 0) {
     tc::tmem_alloc(tmem_slot, kTmemBwdCols);
@@ -427,13 +438,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int row = 32 * q4 + lane;
   const uint32_t t_lane = tmem + (uint32_t(32 * q4) << 16);
   float db2[3] = {0.f, 0.f, 0.f};
-  uint32_t phase = 0;
+  uint32_t phase = 0, xph[2] = {0u, 0u};
   bool ok = true, first = true;
-  XRegs xr;
-  x_load(a, k0, ray, pe, pe_stride, int64_t(blockIdx.x) * 128, M, xr);
-  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+  int it = 0;
+  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
     const int64_t row0 = t * 128;
     const int64_t mrow = row0 + row;
+    const int xb = it & 1;
+    const uint32_t kBXt = kBX + uint32_t(xb) * kXTile;  // this tile's X buffer
     // sigmoid inputs of this thread's row (warps 0-3), read early
     float yv[3] = {0.f, 0.f, 0.f}, gv[3] = {0.f, 0.f, 0.f};
     if (half == 0 && mrow < M) {
@@ -443,18 +455,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         gv[c] = __ldg(grad_rgb + mrow * 3 + c);
       }
     }
-    x_store(sm + kBX, xr);
-    tc::fence_async_smem();
-    __syncthreads();
+    // the next tile's X travels while this tile computes (its buffer was last
+    // read by the previous tile's dW0 MMA, complete)
+    if (tid == 0 && t + gridDim.x < ntiles)
+      x_fetch(sm + kBX + uint32_t(xb ^ 1) * kXTile, xt, t + gridDim.x, xbar + (xb ^ 1));
+    ok = wait_or_flag(xbar + xb, xph[xb], flag, err);
+    if (!ok) break;
+    xph[xb] ^= 1u;
     if (tid == 0) {
       tc::fence_after();
 #pragma unroll
       for (int s = 0; s < 3; ++s)
-        tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX + 256 * s, 128, 768),
+        tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBXt + 256 * s, 128, 768),
                      tc::make_desc(sb + kBW0f + 256 * s, 128, 768), id_r128, s > 0);
       tc::mma_commit(bar);
     }
-    if (t + gridDim.x < ntiles) x_load(a, k0, ray, pe, pe_stride, (t + gridDim.x) * 128, M, xr);
     ok = wait_or_flag(bar, phase, flag, err);
     phase ^= 1;
     if (!ok) break;
@@ -578,7 +593,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
       for (int s = 0; s < 8; ++s)
         tc::mma_bf16(tmem + kTW0, tc::make_desc(sb + kBdZ0 + 4096 * s, 2048, 128),
-                     tc::make_desc(sb + kBX + 1536 * s, 768, 128), id_w0, (!first || s > 0));
+                     tc::make_desc(sb + kBXt + 1536 * s, 768, 128), id_w0, (!first || s > 0));
       tc::mma_commit(bar);
     }
     ok = wait_or_flag(bar, phase, flag, err);
@@ -599,7 +614,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
   }
   if (!ok) {
+    // a wait gave up: one more bounded wait for the MMAs and X copies in
+    // flight before their TMEM and shared memory are released
     tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
+    tc::mbar_wait(xbar, xph[0], kWaitIters);
+    tc::mbar_wait(xbar + 1, xph[1], kWaitIters);
     __syncthreads();
     for (int64_t i = tid; i < P; i += kTcThreads) pw0[i] = 0.f;
   } else {
@@ -680,42 +699,67 @@ int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* 
   return PVDB_OK;
 }
 
-// Runs the forward over rows k0rows [M, c0] (M = totals[1]); pe [rays,
-// pe_stride] holds each ray's view-direction PE. packed: the blob already
-// holds the weights of this call (else they are packed first).
+// The X tiles of rows k0rows [M, c0] (M = totals[1]) with the PE of each
+// row's ray (pe [rays, pe_stride]); room for max_rows rows is reserved.
+int mlp_tc_build_x(int c0, int dpe, const float* k0rows, const int32_t* ray, const float* pe,
+                   int pe_stride, const uint32_t* totals, int64_t max_rows, void** xt,
+                   size_t* xt_cap, cudaStream_t st) {
+  if (c0 > 16 || c0 + dpe + 1 > kXK)
+    return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
+  const int64_t ntiles = (max_rows + 127) / 128;
+  int rc = dev_reserve(xt, xt_cap, size_t(std::max<int64_t>(ntiles, 1)) * kXTile);
+  if (rc) return rc;
+  MlpArgsTc a{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, c0, dpe, c0 + dpe};
+  const int grid = int(std::min<int64_t>(ceil_div(ntiles * 128 * 6, 256), int64_t(num_sms()) * 16));
+  k_build_x<<<std::max(grid, 1), 256, 0, st>>>(a, k0rows, ray, pe, pe_stride, totals,
+                                               static_cast<uint8_t*>(*xt));
+  PVDB_CHECK_LAUNCH("k_build_x");
+  return PVDB_OK;
+}
+
+// Forward over the rows (see mlp_tc_build_x for the inputs). packed: the blob
+// already holds this call's weights; x_ready: the X tiles are already built.
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
                         const int32_t* ray, const float* pe, int pe_stride, const uint32_t* totals,
-                        float* out, int out_logits, void** blob, size_t* blob_cap, uint32_t* err,
-                        cudaStream_t st, int packed) {
+                        int64_t max_rows, float* out, int out_logits, void** blob,
+                        size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                        cudaStream_t st, int packed, int x_ready) {
   int rc = PVDB_OK;
   if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 0, blob, blob_cap, st)))
+    return rc;
+  if (!x_ready && (rc = mlp_tc_build_x(c0, dpe, k0rows, ray, pe, pe_stride, totals, max_rows, xt,
+                                       xt_cap, st)))
     return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_fwd_tc, int(kSmFwdBytes));
   k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
-      a, static_cast<const uint8_t*>(*blob), k0rows, ray, pe, pe_stride, totals, out, out_logits,
-      err);
+      a, static_cast<const uint8_t*>(*blob), static_cast<const uint8_t*>(*xt), totals, out,
+      out_logits, err);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_tc");
   return PVDB_OK;
 }
 
-// Weight and k0 gradients of the rows k0rows [M, c0] (M = totals[1]); per-CTA
-// partials go to wpart (grid x P floats), the caller sums them.
+// Weight and k0 gradients of the rows; per-CTA partials go to wpart (grid x P
+// floats), the caller sums them.
 int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                          const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
                          const int32_t* ray, const float* pe, int pe_stride,
-                         const uint32_t* totals, const float* rgb, const float* grad_rgb,
-                         float* grad_k0, float* wpart, int grid, void** blob, size_t* blob_cap,
-                         uint32_t* err, cudaStream_t st, int packed) {
+                         const uint32_t* totals, int64_t max_rows, const float* rgb,
+                         const float* grad_rgb, float* grad_k0, float* wpart, int grid,
+                         void** blob, size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                         cudaStream_t st, int packed, int x_ready) {
   int rc = PVDB_OK;
   if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 1, blob, blob_cap, st)))
     return rc;
+  if (!x_ready && (rc = mlp_tc_build_x(c0, dpe, k0rows, ray, pe, pe_stride, totals, max_rows, xt,
+                                       xt_cap, st)))
+    return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
-  k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob), k0rows,
-                                                      ray, pe, pe_stride, totals, rgb, grad_rgb,
-                                                      grad_k0, wpart, err);
+  k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob),
+                                                      static_cast<const uint8_t*>(*xt), totals, rgb,
+                                                      grad_rgb, grad_k0, wpart, err);
   PVDB_CHECK_LAUNCH("k_mlp_bwd_tc");
   return PVDB_OK;
 }

@@ -38,9 +38,10 @@ struct MlpArgs {
   int c0, dpe, din;
 };
 int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
-                     const float* viewdirs, int R, const uint32_t* totals, float* out,
-                     int out_logits, float* hpe_buf, int precision, void** blob,
-                     size_t* blob_cap, uint32_t* err, cudaStream_t st);
+                     const float* viewdirs, int R, const uint32_t* totals, int64_t max_rows,
+                     float* out, int out_logits, float* hpe_buf, int precision, void** blob,
+                     size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
+                     cudaStream_t st);
 
 struct RenderP {
   int H, W, inverse_y;
@@ -263,6 +264,8 @@ struct pvdb_renderer_s {
   int64_t rows_cap = 0;
   void* d_packed = nullptr;  // BF16 weight tiles of the tensor-core rgbnet
   size_t packed_cap = 0;
+  void* d_xt = nullptr;      // BF16 X tiles of the rows (tensor-core rgbnet)
+  size_t xt_cap = 0;
 };
 
 static int renderer_grow_rows(pvdb_renderer_s* r, int64_t need) {
@@ -315,7 +318,7 @@ int pvdb_renderer_destroy(pvdb_renderer r) {
   pvdb_grid_destroy(r->topo);
   void* ptrs[] = {r->d_rows, r->d_den, r->d_col, r->d_colh, r->d_params, r->d_n, r->d_off,
                   r->d_T, r->d_viewdirs, r->d_hpe, r->d_image, r->d_totals, r->scan_partial,
-                  r->d_rk0, r->d_rw, r->d_rpix, r->d_logits, r->d_packed};
+                  r->d_rk0, r->d_rw, r->d_rpix, r->d_logits, r->d_packed, r->d_xt};
   for (void* p : ptrs) dev_free(p);
   delete r;
   return PVDB_OK;
@@ -552,8 +555,9 @@ int pvdb_renderer_render(pvdb_renderer r, int32_t precision, pvdb_stream s) {
   a.dpe = r->dpe;
   a.din = din;
   if (total) {
-    rc = mlp_forward_rows(a, r->d_rk0, r->d_rpix, r->d_viewdirs, HW, r->d_totals, r->d_logits, 1,
-                          r->d_hpe, precision, &r->d_packed, &r->packed_cap, r->d_totals + 3, st);
+    rc = mlp_forward_rows(a, r->d_rk0, r->d_rpix, r->d_viewdirs, HW, r->d_totals, r->rows_cap,
+                          r->d_logits, 1, r->d_hpe, precision, &r->d_packed, &r->packed_cap,
+                          &r->d_xt, &r->xt_cap, r->d_totals + 3, st);
     if (rc) return rc;
   }
   prof_mark(st, 4);

@@ -314,6 +314,7 @@ static std::vector<uint8_t> graph_key(const TrainArgs& t) {
   key_put(k, m->hpe);
   key_put(k, m->wpart);
   key_put(k, m->mlp_packed);
+  key_put(k, m->mlp_xt);
   key_put(k, m->red.keys[0]);
   key_put(k, m->red.keys[1]);
   key_put(k, m->red.vals[0]);

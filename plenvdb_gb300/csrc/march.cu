@@ -421,15 +421,14 @@ __global__ void __launch_bounds__(kMarchThreads)
 // (k0). The samples are stably radix-sorted by cell key, a leaf-major code of
 // the cell's low corner, so each cell's samples form one segment in ascending
 // sample order, and the first sorted index of each cell goes into a dense cell
-// map. Then, in two passes:
-//   1. per (cell, corner c): the segment's contributions to corner c are summed
-//      in sample order into the cell's partial P[cell][c] (1 + C floats), and
-//      the corner voxel's leaf is flagged as touched;
-//   2. per voxel of the touched leaves: grad += sum over c' = 0..7, in that
-//      order, of P[v - delta(c')][c'] for the cells present in the map.
-// Every sum has an order fixed by the data, so the result is bitwise
-// reproducible without atomics. Corners in no allocated leaf are dropped
-// (densityvdb.cu:23).
+// map (which also flags the leaves of the cell's corners as touched). Then one
+// thread per voxel of the touched leaves computes
+//   grad += sum over c' = 0..7, in that order, of
+//           (sum over the samples of cell v - delta(c'), in sample order,
+//            of that sample's corner-c' contribution)
+// for the cells present in the map. Every sum has an order fixed by the data,
+// so the result is bitwise reproducible without atomics. Corners in no
+// allocated leaf are dropped (densityvdb.cu:23).
 __device__ __forceinline__ void cell_decode(const int ld[3], uint32_t key, int& i, int& j, int& k) {
   const int leaf = int(key >> 9), off = int(key & 511u);
   const int lk = leaf % ld[2];
@@ -445,17 +444,39 @@ __device__ __forceinline__ bool seg_head(const uint32_t* __restrict__ skeys, int
   return key != kInvalidKey && (i == 0 || skeys[i - 1] != key);
 }
 
-// Marks (or, clear, unmarks) the cells present; when marking, also lists the
-// segment heads (in no particular order: each head's work is independent).
+__device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, int cj, int ck,
+                                                   uint8_t* touched) {
+  int s[8];
+  corner_slots(g, ci, cj, ck, s);
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (s[c] >= 0) touched[s[c] >> 9] = 1;
+}
+
+// Marks the cells present in the cell map and flags the leaves holding their
+// corners as touched in the density grid and (touched_c != NULL) the k0 grid.
 __global__ void k_cell_map_set(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
-                               int32_t* map, int clear, int32_t* heads, uint32_t* nheads) {
+                               int32_t* map, GridView gd, GridView gc, uint8_t* touched_d,
+                               uint8_t* touched_c) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
     if (seg_head(skeys, i)) {
-      map[skeys[i]] = clear ? -1 : int32_t(i);
-      if (!clear) heads[atomicAdd(nheads, 1u)] = int32_t(i);
+      const uint32_t key = skeys[i];
+      map[key] = int32_t(i);
+      int ci, cj, ck;
+      cell_decode(gd.ldim, key, ci, cj, ck);
+      mark_corner_leaves(gd, ci, cj, ck, touched_d);
+      if (touched_c) mark_corner_leaves(gc, ci, cj, ck, touched_c);
     }
+}
+
+__global__ void k_cell_map_clear(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
+                                 int32_t* map) {
+  const int64_t n = *n_dev;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    if (seg_head(skeys, i)) map[skeys[i]] = -1;
 }
 
 // Corner weight c of the multi-channel formula, ((a*b)*c) (colorvdb.cu:100-107).
@@ -466,66 +487,16 @@ __device__ __forceinline__ float corner_scale(float u, float v, float w, int c) 
   return __fmul_rn(__fmul_rn(a, b), cc);
 }
 
-// Pass 1: thread per (sorted index j, corner c); segment heads only. NQ = the
-// number of float4 chunks of the k0 gradient (0 = density only).
-template <int NQ>
-__global__ void __launch_bounds__(256)
-    k_cell_partials(GridView gd, GridView gc, const uint32_t* __restrict__ skeys,
-                    const uint32_t* __restrict__ svals, const uint32_t* n_dev,
-                    const int32_t* __restrict__ heads, const uint32_t* __restrict__ nheads,
-                    const float4* __restrict__ rec, float* __restrict__ pd,
-                    float4* __restrict__ pk, uint8_t* touched_d, uint8_t* touched_c) {
-  const int64_t n = *n_dev;
-  const int64_t nh = *nheads;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nh * 8;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t h = heads[t >> 3];
-    const int c = int(t & 7);
-    const uint32_t key = skeys[h];
-    int ci, cj, ck, di, dj, dk;
-    cell_decode(gd.ldim, key, ci, cj, ck);
-    corner_delta(c, di, dj, dk);
-    const int sd = slot_of(gd, ci + di, cj + dj, ck + dk);
-    const int sc = NQ ? slot_of(gc, ci + di, cj + dj, ck + dk) : -1;
-    if (sd < 0 && sc < 0) continue;
-    float sum_d = 0.f;
-    float4 acc[NQ > 0 ? NQ : 1];
-#pragma unroll
-    for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t j = h; j < n && skeys[j] == key; ++j) {
-      const float4* r = rec + int64_t(svals[j]) * (1 + NQ);
-      const float4 p = r[0];
-      const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
-                  w = p.z - float(ifloor(p.z));
-      if (p.w != 0.f) sum_d = __fadd_rn(sum_d, density_corner_term(p.w, u, v, w, c));
-      if (NQ) {
-        const float sce = corner_scale(u, v, w, c);
-#pragma unroll
-        for (int b = 0; b < NQ; ++b) {
-          const float4 g = r[1 + b];
-          acc[b].x = __fadd_rn(acc[b].x, __fmul_rn(g.x, sce));
-          acc[b].y = __fadd_rn(acc[b].y, __fmul_rn(g.y, sce));
-          acc[b].z = __fadd_rn(acc[b].z, __fmul_rn(g.z, sce));
-          acc[b].w = __fadd_rn(acc[b].w, __fmul_rn(g.w, sce));
-        }
-      }
-    }
-    const int64_t e = int64_t(key) * 8 + c;
-    pd[e] = sum_d;
-#pragma unroll
-    for (int b = 0; b < NQ; ++b) pk[e * NQ + b] = acc[b];
-    if (sd >= 0) touched_d[sd >> 9] = 1;
-    if (NQ && sc >= 0) touched_c[sc >> 9] = 1;
-  }
-}
-
-// Pass 2: thread per voxel of the listed (touched) leaves of grid g; adds the
-// density partials to grad_d and/or the k0 partials to grad_c (C channels).
+// Thread per voxel of the listed (touched) leaves of grid g; adds the density
+// sum to grad_d and/or the k0 sums to grad_c (C channels). NQ = the number of
+// float4 chunks of the k0 gradient (0 = density only).
 template <int NQ>
 __global__ void __launch_bounds__(256)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
-                   const int32_t* __restrict__ map, const float* __restrict__ pd,
-                   const float4* __restrict__ pk, float* grad_d, float* grad_c, int C) {
+                   const int32_t* __restrict__ map, const uint32_t* __restrict__ skeys,
+                   const uint32_t* __restrict__ svals, const uint32_t* n_dev,
+                   const float4* __restrict__ rec, float* grad_d, float* grad_c, int C) {
+  const int64_t n = *n_dev;
   const int64_t nv = int64_t(*count) * kLeafVox;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -533,42 +504,56 @@ __global__ void __launch_bounds__(256)
     const int vox = int(i & 511);
     const int vi = g.origin[leaf * 3] + (vox >> 6), vj = g.origin[leaf * 3 + 1] + ((vox >> 3) & 7),
               vk = g.origin[leaf * 3 + 2] + (vox & 7);
-    // the up to 8 cells that have this voxel as corner c, in corner order
-    int64_t ent[8];
     bool any = false;
+    float sum_d = 0.f;
+    float4 acc[NQ > 0 ? NQ : 1];
+#pragma unroll
+    for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+    // the up to 8 cells that have this voxel as corner c, in corner order
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       int di, dj, dk;
       corner_delta(c, di, dj, dk);
       const uint32_t key = cell_key(g.ldim, vi - di, vj - dj, vk - dk);
-      ent[c] = (key != kInvalidKey && __ldg(map + key) >= 0) ? int64_t(key) * 8 + c : -1;
-      any = any || ent[c] >= 0;
+      if (key == kInvalidKey) continue;
+      const int32_t h = __ldg(map + key);
+      if (h < 0) continue;
+      any = true;
+      float pd = 0.f;
+      float4 pk[NQ > 0 ? NQ : 1];
+#pragma unroll
+      for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int64_t j = h; j < n && skeys[j] == key; ++j) {
+        const float4* r = rec + int64_t(svals[j]) * (1 + NQ);
+        const float4 p = r[0];
+        const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
+                    w = p.z - float(ifloor(p.z));
+        if (grad_d && p.w != 0.f) pd = __fadd_rn(pd, density_corner_term(p.w, u, v, w, c));
+        if (NQ && grad_c) {
+          const float sce = corner_scale(u, v, w, c);
+#pragma unroll
+          for (int b = 0; b < NQ; ++b) {
+            const float4 q = r[1 + b];
+            pk[b].x = __fadd_rn(pk[b].x, __fmul_rn(q.x, sce));
+            pk[b].y = __fadd_rn(pk[b].y, __fmul_rn(q.y, sce));
+            pk[b].z = __fadd_rn(pk[b].z, __fmul_rn(q.z, sce));
+            pk[b].w = __fadd_rn(pk[b].w, __fmul_rn(q.w, sce));
+          }
+        }
+      }
+      sum_d = __fadd_rn(sum_d, pd);
+#pragma unroll
+      for (int b = 0; b < NQ; ++b) {
+        acc[b].x = __fadd_rn(acc[b].x, pk[b].x);
+        acc[b].y = __fadd_rn(acc[b].y, pk[b].y);
+        acc[b].z = __fadd_rn(acc[b].z, pk[b].z);
+        acc[b].w = __fadd_rn(acc[b].w, pk[b].w);
+      }
     }
     if (!any) continue;
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
-    if (grad_d) {
-      float sum_d = 0.f;
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (ent[c] >= 0) sum_d = __fadd_rn(sum_d, pd[ent[c]]);
-      grad_d[slot] = __fadd_rn(grad_d[slot], sum_d);
-    }
+    if (grad_d) grad_d[slot] = __fadd_rn(grad_d[slot], sum_d);
     if (NQ && grad_c) {
-      float4 acc[NQ > 0 ? NQ : 1];
-#pragma unroll
-      for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        if (ent[c] < 0) continue;
-#pragma unroll
-        for (int b = 0; b < NQ; ++b) {
-          const float4 q = pk[ent[c] * NQ + b];
-          acc[b].x = __fadd_rn(acc[b].x, q.x);
-          acc[b].y = __fadd_rn(acc[b].y, q.y);
-          acc[b].z = __fadd_rn(acc[b].z, q.z);
-          acc[b].w = __fadd_rn(acc[b].w, q.w);
-        }
-      }
       float* dst = grad_c + slot * C;
 #pragma unroll
       for (int b = 0; b < NQ; ++b) {
@@ -587,11 +572,9 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const int grid = stride_grid();
   const GridView gv = density->view();
   const GridView kv = NQ ? k0->view() : gv;
-  k_cell_partials<NQ><<<grid * 2, 256, 0, st>>>(gv, kv, skeys, svals, m->w.totals + 0,
-                                                m->cell_heads, m->w.totals + 5, m->w.b_rec,
-                                                m->cell_pd, m->cell_pk, density->d_touched,
-                                                NQ ? k0->d_touched : density->d_touched);
-  PVDB_CHECK_LAUNCH("k_cell_partials");
+  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, gv, kv,
+                                       density->d_touched, NQ ? k0->d_touched : nullptr);
+  PVDB_CHECK_LAUNCH("k_cell_map_set");
   density->tlist_valid = false;
   if (NQ) k0->tlist_valid = false;
   int rc = touched_list(density, st);
@@ -599,13 +582,14 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const bool same = NQ && k0->h_table == density->h_table;
   const int C = NQ ? k0->C : 0;
   k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_map,
-                                           m->cell_pd, m->cell_pk, density->d_grad,
-                                           same ? k0->d_grad : nullptr, C);
+                                           skeys, svals, m->w.totals + 0, m->w.b_rec,
+                                           density->d_grad, same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
-    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_map,
-                                             m->cell_pd, m->cell_pk, nullptr, k0->d_grad, C);
+    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_map, skeys,
+                                             svals, m->w.totals + 0, m->w.b_rec, nullptr,
+                                             k0->d_grad, C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -777,10 +761,7 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   const int C = use_k0 ? k0->C : 0;
   PVDB_REQUIRE(C <= 16, "the march backward takes at most 16 k0 channels");
   const int nq = (C + 3) / 4;
-  if ((rc = dev_reserve((void**)&m->cell_heads, &m->cell_heads_cap, size_t(nmax) * 4)) ||
-      (rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)) ||
-      (rc = dev_reserve((void**)&m->cell_pd, &m->cell_pd_cap, size_t(ncells) * 8 * 4)) ||
-      (nq && (rc = dev_reserve((void**)&m->cell_pk, &m->cell_pk_cap, size_t(ncells) * 8 * nq * 16))))
+  if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)))
     return rc;
   const int nb = ceil_div(R, kMarchWarps);
   k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
@@ -795,10 +776,6 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   const uint32_t* skeys = m->red.keys[buf];
   const uint32_t* svals = m->red.vals[buf];
   const int grid = stride_grid();
-  PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals + 5, 0, 4, st));
-  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 0, m->cell_heads,
-                                       m->w.totals + 5);
-  PVDB_CHECK_LAUNCH("k_cell_map_set");
   switch (nq) {
     case 0: rc = cell_reduce_launch<0>(m, density, k0, skeys, svals, st); break;
     case 1: rc = cell_reduce_launch<1>(m, density, k0, skeys, svals, st); break;
@@ -807,8 +784,8 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
     default: rc = cell_reduce_launch<4>(m, density, k0, skeys, svals, st); break;
   }
   if (rc) return rc;
-  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, 1, nullptr, nullptr);
-  PVDB_CHECK_LAUNCH("k_cell_map_set(clear)");
+  k_cell_map_clear<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map);
+  PVDB_CHECK_LAUNCH("k_cell_map_clear");
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
 }
@@ -894,9 +871,6 @@ int pvdb_march_destroy(pvdb_march m) {
   for (void* p : ptrs) dev_free(p);
   free_scratch(m->red);
   dev_free(m->cell_map);
-  dev_free(m->cell_pd);
-  dev_free(m->cell_pk);
-  dev_free(m->cell_heads);
   dev_free(m->g_in);
   dev_free(m->g_scal);
   if (m->g_exec) cudaGraphExecDestroy(m->g_exec);

@@ -50,7 +50,7 @@ struct MarchW {
   float4* b_rec;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 sort look-back wait),
-  // [4] samples evaluated, [5] touched cells (backward)
+  // [4] samples evaluated, [5] unused
   uint32_t* totals;
 };
 
@@ -65,13 +65,7 @@ struct pvdb_march_s {
   pvdb::ReduceScratch red;   // kept samples sorted by cell key
   int32_t* cell_map = nullptr;  // [cells of the leaf lattice] first sorted index, -1 = none
   size_t cell_map_cap = 0;      // elements
-  float* cell_pd = nullptr;     // [cells][8 corners] density partial sums
-  size_t cell_pd_cap = 0;       // bytes
-  float4* cell_pk = nullptr;    // [cells][8 corners][nq] k0 partial sums
-  size_t cell_pk_cap = 0;       // bytes
   size_t b_rec_cap = 0;         // bytes of w.b_rec
-  int32_t* cell_heads = nullptr;  // sorted index of each touched cell's first sample
-  size_t cell_heads_cap = 0;      // bytes
   uint32_t* scan_partial = nullptr;
   size_t scan_partial_cap = 0;
   // state of the last forward

@@ -377,12 +377,22 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
   if (tid < 3) pb2[tid] = ab2;
 }
 
+// Sum of the per-CTA partials: eight interleaved running sums (partials c,
+// c+8, ...) combined in a fixed order, so the loads of eight partials are in
+// flight together and the result is the same on every run.
 __global__ void k_wgrad_reduce(const float* __restrict__ wpart, int nparts, int64_t P, float* out) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= P) return;
-  float s = 0.f;
-  for (int c = 0; c < nparts; ++c) s += wpart[int64_t(c) * P + i];
-  out[i] = s;
+  float acc[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) acc[u] = 0.f;
+  int c = 0;
+  for (; c + 8 <= nparts; c += 8) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] += wpart[int64_t(c + u) * P + i];
+  }
+  for (int u = 0; c < nparts; ++c, ++u) acc[u] += wpart[int64_t(c) * P + i];
+  out[i] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
 }
 
 __global__ void k_scatter_grads(const float* __restrict__ flat, int din, float* w0, float* b0,

@@ -323,9 +323,6 @@ static std::vector<uint8_t> graph_key(const TrainArgs& t) {
   key_put(k, m->red.partial);
   key_put(k, m->scan_partial);
   key_put(k, m->cell_map);
-  key_put(k, m->cell_pd);
-  key_put(k, m->cell_pk);
-  key_put(k, m->cell_heads);
   key_put(k, m->t_rgb);
   key_put(k, m->t_grad_k0);
   key_put(k, m->g_in);

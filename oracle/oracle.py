@@ -417,6 +417,59 @@ class CPUTrainer:
                                             C.c_float(w_ent), C.c_float(w_per), C.c_float(tv_w))
 
 
+class _RenderParams(C.Structure):
+    _fields_ = [("H", C.c_int), ("W", C.c_int), ("inverse_y", C.c_int), ("reso", C.c_int * 3),
+                ("K", C.c_float * 9), ("c2w", C.c_float * 16), ("xyz_min", C.c_float * 3),
+                ("xyz_max", C.c_float * 3), ("near_", C.c_float), ("stepdist", C.c_float),
+                ("shift", C.c_float), ("interval", C.c_float), ("thr", C.c_float),
+                ("bg", C.c_float), ("t_stop", C.c_float)]
+
+
+def render_pixels(index, den, col, mlp: MLPWeights, K, c2w, xyz_min, xyz_max, H, W, near,
+                  stepdist, act_shift, interval, thres, bg, t_stop, pixels=None, inverse_y=False,
+                  fp32=False):
+    """MGRenderer render march (renderer.cu:122-412) for the given pixel ids
+    (default: all H*W). index: dense int row ids [R0,R1,R2] (0 = empty);
+    den [N]; col [N, dcol]. Returns (rgb [n,3], colour samples [n], T [n])."""
+    idx = np.ascontiguousarray(index, np.int32)
+    den = np.ascontiguousarray(den, np.float32).reshape(-1)
+    col = np.ascontiguousarray(col, np.float32)
+    dcol = col.shape[1]
+    col = col.reshape(-1)
+    pix = np.arange(H * W, dtype=np.int64) if pixels is None else np.ascontiguousarray(pixels, np.int64)
+    P = _RenderParams()
+    P.H, P.W, P.inverse_y = int(H), int(W), int(bool(inverse_y))
+    P.reso[:] = [int(r) for r in idx.shape]
+    P.K[:] = [float(v) for v in np.asarray(K, np.float32).reshape(-1)]
+    P.c2w[:] = [float(v) for v in np.asarray(c2w, np.float32).reshape(-1)]
+    P.xyz_min[:] = [float(v) for v in xyz_min]
+    P.xyz_max[:] = [float(v) for v in xyz_max]
+    P.near_, P.stepdist, P.shift, P.interval = near, stepdist, act_shift, interval
+    P.thr, P.bg, P.t_stop = thres, bg, t_stop
+    n = pix.shape[0]
+    rgb = np.empty((n, 3))
+    ncol = np.empty(n, np.int32)
+    T = np.empty(n)
+    lib().oracle_render_pixels(C.byref(P), _p(idx), _p(den), _p(col), int(dcol), mlp.ref, _p(pix),
+                               C.c_int64(n), int(fp32), _p(rgb), _p(ncol), _p(T))
+    return rgb, ncol, T
+
+
+def index_density(index, den, xyz, fp32=False):
+    """Index-grid trilinear density (renderer.cu:271-300) and isActive(Round(xyz))
+    at index-space points xyz [n,3]; index: dense row ids [R0,R1,R2]."""
+    idx = np.ascontiguousarray(index, np.int32)
+    den = np.ascontiguousarray(den, np.float32).reshape(-1)
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    n = xyz.shape[0]
+    reso = np.asarray(idx.shape, np.int32)
+    out = np.empty(n)
+    act = np.empty(n, np.uint8)
+    lib().oracle_index_density(_p(reso), _p(idx), _p(den), _p(xyz), C.c_int64(n), int(fp32),
+                               _p(out), _p(act))
+    return out, act.astype(bool)
+
+
 def set_threads(n: int):
     lib().oracle_set_threads(int(n))
 

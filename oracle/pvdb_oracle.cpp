@@ -1172,3 +1172,209 @@ double oracle_train_step_fp32(otrain_grids* G, otrain_net* N, const float* ro, c
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ merged-index renderer
+// MGRenderer::render_an_image (plenvdb.h:1010-1060 -> renderer.cu:370-412) for a
+// list of pixels. The index grid is a dense row-id array (0 = empty row, the
+// voxels with a row id are the active ones); rows beyond the grid read row 0.
+//   get_rays / get_tminmax      renderer.cu:122-167, 50-64 (unit-cube frame,
+//                               float arithmetic, contractions written as fma)
+//   march                       renderer.cu:227-266 (t += steplen before each
+//                               sample, isActive(Round(xyz)), thresholds on
+//                               alpha and weight, stop once T < t_stop)
+//   trigetDensity2/trigetColor  renderer.cu:271-317 (int() truncation, corner
+//                               scales first, then the fma chain over corners)
+//   cuda_rgbnet                 renderer.cu:83-110 ([k0 | PE(viewdir)] -> 128
+//                               ReLU -> 128 ReLU -> 3)
+//   final_render + last_rgb     renderer.cu:112-119, 360-362 (T*bg plus
+//                               w/(1+exp(-logit)) in sample order; bg alone
+//                               for a pixel without a colour sample, :325-329)
+// The reference marches every pixel twice (count, then fill) and restarts the
+// fill pass from t_first - steplen, which can shift the fill pass's sample
+// positions by an ulp; this restatement uses one march for both, with the
+// fill pass's density association. fp32 mirrors the float operations; fp64
+// forms the positions in float as the reference does and evaluates density,
+// alpha, transmittance, features, the MLP and the composite in double.
+extern "C" {
+
+typedef struct {
+  int H, W, inverse_y;
+  int reso[3];
+  float K[9];
+  float c2w[16];
+  float xyz_min[3], xyz_max[3];
+  float near_, stepdist, shift, interval, thr, bg, t_stop;
+} orender_params;
+
+}  // extern "C"
+
+namespace {
+
+// The merged index grid: row id of voxel (i,j,k), 0 outside the grid.
+struct IndexGrid {
+  int r0, r1, r2;
+  const int32_t* index;
+  int32_t row(int i, int j, int k) const {
+    if (i < 0 || j < 0 || k < 0 || i >= r0 || j >= r1 || k >= r2) return 0;
+    return index[(int64_t(i) * r1 + j) * r2 + k];
+  }
+  // isActive(Round(xyz)) (renderer.cu:253): the voxels with a row are active
+  bool active_round(const float* xyz) const {
+    return row(int(std::nearbyint(xyz[0])), int(std::nearbyint(xyz[1])),
+               int(std::nearbyint(xyz[2]))) > 0;
+  }
+  // trigetDensity2 corner rows and scales (renderer.cu:271-300); returns the
+  // density, fp32: scales first, then the fma chain over the corners
+  template <class T>
+  T density(const float* xyz, const float* den, int32_t id[8], T sc[8]) const {
+    const int i = int(xyz[0]), j = int(xyz[1]), k = int(xyz[2]);
+    const float u = xyz[0] - float(i), v = xyz[1] - float(j), w = xyz[2] - float(k);
+    id[0] = row(i, j, k);         id[1] = row(i, j, k + 1);
+    id[2] = row(i, j + 1, k + 1); id[3] = row(i, j + 1, k);
+    id[4] = row(i + 1, j + 1, k); id[5] = row(i + 1, j + 1, k + 1);
+    id[6] = row(i + 1, j, k + 1); id[7] = row(i + 1, j, k);
+    const T U = u, V = v, Wt = w, iu = T(1) - U, iv = T(1) - V, iw = T(1) - Wt;
+    sc[0] = (iu * iv) * iw; sc[1] = (iu * iv) * Wt; sc[2] = (iu * V) * Wt; sc[3] = (iu * V) * iw;
+    sc[4] = (U * V) * iw;   sc[5] = (U * V) * Wt;   sc[6] = (U * iv) * Wt; sc[7] = (U * iv) * iw;
+    T sig = T(den[id[0]]) * sc[0];
+    for (int c = 1; c < 8; ++c) {
+      if constexpr (sizeof(T) == 4) sig = std::fma(den[id[c]], sc[c], sig);
+      else sig += T(den[id[c]]) * sc[c];
+    }
+    return sig;
+  }
+};
+
+template <class T>
+void render_pixel(const orender_params& P, const int32_t* index, const float* den,
+                  const float* col, int dcol, const MlpT<T>& mlp, int64_t n, double* rgb_out,
+                  int32_t* ncol_out, double* T_out) {
+  const IndexGrid ig{P.reso[0], P.reso[1], P.reso[2], index};
+  const int r0 = P.reso[0], r1 = P.reso[1], r2 = P.reso[2];
+  const float pi = float(n % P.W) + 0.5f, pj = float(n / P.W) + 0.5f;
+  float dir[3];
+  dir[0] = (pi - P.K[2]) / P.K[0];
+  if (P.inverse_y) {
+    dir[1] = (pj - P.K[5]) / P.K[4];
+    dir[2] = 1.f;
+  } else {
+    dir[1] = -((pj - P.K[5]) / P.K[4]);
+    dir[2] = -1.f;
+  }
+  float rd[3];
+  for (int a = 0; a < 3; ++a)
+    rd[a] = std::fma(dir[2], P.c2w[4 * a + 2], std::fma(dir[1], P.c2w[4 * a + 1], dir[0] * P.c2w[4 * a]));
+  const float len = std::sqrt(std::fma(rd[2], rd[2], std::fma(rd[1], rd[1], rd[0] * rd[0])));
+  const float steplen = P.stepdist / len;
+  float o[3], d[3], vd[3];
+  for (int a = 0; a < 3; ++a) {
+    const float ext = P.xyz_max[a] - P.xyz_min[a];
+    o[a] = (P.c2w[4 * a + 3] - P.xyz_min[a]) / ext;
+    d[a] = rd[a] / ext;
+    vd[a] = rd[a] / len;
+  }
+  const float vx = d[0] == 0.f ? float(1e-6) : d[0];
+  const float vy = d[1] == 0.f ? float(1e-6) : d[1];
+  const float vz = d[2] == 0.f ? float(1e-6) : d[2];
+  const float ax = (1.f - o[0]) / vx, ay = (1.f - o[1]) / vy, az = (1.f - o[2]) / vz;
+  const float bx = (-o[0]) / vx, by = (-o[1]) / vy, bz = (-o[2]) / vz;
+  const float far_ = 1e9f;
+  const float tmin = std::max(std::min(std::max(std::max(std::min(ax, bx), std::min(ay, by)), std::min(az, bz)), far_), P.near_);
+  const float tmax = std::max(std::min(std::min(std::min(std::max(ax, bx), std::max(ay, by)), std::max(az, bz)), far_), P.near_);
+  const float wsm1[3] = {float(r0 - 1), float(r1 - 1), float(r2 - 1)};
+  // PE of the view direction, shared by the pixel's colour samples
+  const int npe = mlp.pe;
+  std::vector<T> x(size_t(dcol) + 3 + 6 * npe), h0(mlp.W), h1(mlp.W);
+  view_pe<T>(vd, npe, x.data() + dcol);
+  T Tc = 1;
+  std::vector<T> terms;  // w/(1+exp(-logit)) of each colour sample, 3 per sample
+  int32_t cnt = 0;
+  float t = tmin;
+  const float nsteps_f = (tmax - tmin) / steplen;
+  const int max_it = (nsteps_f > 0.f && nsteps_f < 1e6f) ? int(nsteps_f) + 4 : 0;
+  for (int it = 0; t < tmax && it < max_it; ++it) {
+    t = t + steplen;
+    float p[3];
+    for (int a = 0; a < 3; ++a) p[a] = std::fma(t, d[a], o[a]);
+    if ((0.f > p[0]) | (0.f > p[1]) | (0.f > p[2]) | (1.f < p[0]) | (1.f < p[1]) | (1.f < p[2]))
+      continue;
+    float xyz[3];
+    for (int a = 0; a < 3; ++a) xyz[a] = p[a] * wsm1[a];
+    if (!ig.active_round(xyz)) continue;
+    int32_t id[8];
+    T sc[8];
+    const T sig = ig.density<T>(xyz, den, id, sc);
+    T alpha;
+    if constexpr (sizeof(T) == 4) alpha = 1.f - std::pow(1.f + std::exp(sig + P.shift), -P.interval);
+    else alpha = 1.0 - std::pow(1.0 + std::exp(sig + double(P.shift)), -double(P.interval));
+    if (alpha <= T(P.thr)) continue;
+    const T wt = Tc * alpha;
+    Tc = Tc * (T(1) - alpha);
+    if (wt <= T(P.thr)) continue;
+    for (int q = 0; q < dcol; ++q) {
+      T f = T(col[int64_t(id[0]) * dcol + q]) * sc[0];
+      for (int c = 1; c < 8; ++c) {
+        if constexpr (sizeof(T) == 4) f = std::fma(col[int64_t(id[c]) * dcol + q], sc[c], f);
+        else f += T(col[int64_t(id[c]) * dcol + q]) * sc[c];
+      }
+      x[q] = f;
+    }
+    T logit[3];
+    mlp_forward<T>(mlp, x.data(), h0.data(), h1.data(), logit);
+    for (int c = 0; c < 3; ++c) terms.push_back(wt / (T(1) + std::exp(-logit[c])));
+    ++cnt;
+    const bool stop = sizeof(T) == 4 ? (float(Tc) < P.t_stop) : (double(Tc) < double(P.t_stop));
+    if (stop) break;
+  }
+  ncol_out[0] = cnt;
+  T_out[0] = double(Tc);
+  for (int c = 0; c < 3; ++c) {
+    if (cnt == 0) {
+      rgb_out[c] = P.bg;
+      continue;
+    }
+    T s = Tc * T(P.bg);
+    for (int32_t q = 0; q < cnt; ++q) s += terms[size_t(q) * 3 + c];
+    rgb_out[c] = double(s);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Index-grid density and isActive(Round(xyz)) at index-space points (the
+// render march's per-sample lookups).
+void oracle_index_density(const int32_t* reso, const int32_t* index, const float* den,
+                          const float* xyz, int64_t n, int fp32, double* out, uint8_t* active) {
+  const IndexGrid ig{reso[0], reso[1], reso[2], index};
+  for (int64_t q = 0; q < n; ++q) {
+    int32_t id[8];
+    active[q] = ig.active_round(xyz + 3 * q) ? 1 : 0;
+    if (fp32) {
+      float sc[8];
+      out[q] = ig.density<float>(xyz + 3 * q, den, id, sc);
+    } else {
+      double sc[8];
+      out[q] = ig.density<double>(xyz + 3 * q, den, id, sc);
+    }
+  }
+}
+
+void oracle_render_pixels(const orender_params* P, const int32_t* index, const float* den,
+                          const float* col, int dcol, const omlp* mw, const int64_t* pix,
+                          int64_t npix, int fp32, double* rgb, int32_t* n_color, double* T_last) {
+  if (fp32) {
+    const MlpT<float> m(*mw);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t q = 0; q < npix; ++q)
+      render_pixel<float>(*P, index, den, col, dcol, m, pix[q], rgb + 3 * q, n_color + q, T_last + q);
+  } else {
+    const MlpT<double> m(*mw);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t q = 0; q < npix; ++q)
+      render_pixel<double>(*P, index, den, col, dcol, m, pix[q], rgb + 3 * q, n_color + q, T_last + q);
+  }
+}
+
+}  // extern "C"

@@ -90,3 +90,42 @@ def test_voxel_adam(golden, mode, kind):
     base = g.dense()
     base = base[..., 0] if kind == "d" else base
     assert np.array_equal(got[~act], base[~act])
+
+
+def test_index_density_matches_nanovdb(golden):
+    """The render march's index-grid lookups (renderer.cu:253, 271-300) against
+    the reference's NanoVDB accessor: isActive(Round(xyz)) exactly (rint ties
+    included), the trilinear density within float rounding (the golden vectors
+    use the count pass's association, the oracle the fill pass's)."""
+    rows = golden["idx_rows"].astype(np.int32)
+    out32, act = O.index_density(rows, golden["idx_den_rows"], golden["idx_xyz"], fp32=True)
+    np.testing.assert_array_equal(act, golden["idx_active_round"].astype(bool))
+    np.testing.assert_allclose(out32, golden["idx_density"], rtol=1e-5, atol=2e-6)
+    out64, _ = O.index_density(rows, golden["idx_den_rows"], golden["idx_xyz"], fp32=False)
+    np.testing.assert_allclose(out64, golden["idx_density"], rtol=1e-5, atol=2e-6)
+
+
+def test_render_oracle_fp32_tracks_fp64(golden):
+    """Render march restatement: the float-mirroring mode stays within float
+    rounding of FP64, and a pixel without a colour sample is the background."""
+    from plenvdb_gb300.scene import rgbnet_init, sphere_poses
+    rows = golden["idx_rows"].astype(np.int32)
+    R = rows.shape[0]
+    den = golden["idx_den_rows"] + np.float32(3.0)
+    rng = np.random.default_rng(0)
+    col = rng.normal(0, 0.1, (den.shape[0], 12)).astype(np.float32)
+    col[0] = 0.0
+    net = [t.numpy().astype(np.float64) for t in rgbnet_init(seed=1)]
+    mlp = O.MLPWeights(*net, c0=12, pe=4)
+    K = np.array([[60.0, 0, 24], [0, 60.0, 24], [0, 0, 1]], np.float32)
+    pose = sphere_poses(1, 4.03, seed=2)[0]
+    kw = dict(near=2.0, stepdist=0.5 * 3.0 / R, act_shift=-4.6, interval=0.5, thres=1e-4,
+              bg=1.0, t_stop=1e-4)
+    lo, hi = [-1.5] * 3, [1.5] * 3
+    r32, n32, _ = O.render_pixels(rows, den, col, mlp, K, pose, lo, hi, 48, 48, fp32=True, **kw)
+    r64, n64, _ = O.render_pixels(rows, den, col, mlp, K, pose, lo, hi, 48, 48, fp32=False, **kw)
+    assert (n64 > 0).mean() > 0.1
+    same = n32 == n64
+    assert same.mean() > 0.99
+    np.testing.assert_allclose(r32[same], r64[same], rtol=1e-5, atol=1e-6)
+    assert np.all(r64[n64 == 0] == 1.0)

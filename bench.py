@@ -3,9 +3,15 @@
 Workload (one "step"): one fine-stage iteration of PlenVDB's DVGO training on
 8192 rays over a 160^3 sparse scene (8 seeded ellipsoids, ~10% voxels active,
 8^3 leaves), k0 = 12 channels, rgbnet 39-128-128-3, per-voxel Adam on both
-grids (skip-zero-grad), Adam on the rgbnet, TV weight 1e-4 — the FP32 plain
-method (BASELINE configs[1]). Synthetic seeded data stands in for the NeRF
-datasets; targets are rendered from a seeded ground-truth grid.
+grids (skip-zero-grad), Adam on the rgbnet, TV weight 1e-4, in FP32 (the plain
+method) or BF16 (--precision bf16). Synthetic seeded data stands in for the
+NeRF datasets; targets are rendered from a seeded ground-truth grid.
+
+Beside the headline line's step timing the JSON carries: per-stage times and
+rooflines, the end-to-end number through the public API with host buffers,
+the merged-VDB render of 200 800x800 frames (FP32 plain and BF16), the PSNR
+of FP32- and BF16-trained models after 2000 iterations on 8 held-out 800x800
+views, and the 320^3 / 65536-ray BF16 training step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -40,7 +46,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32")
-    ap.add_argument("--render-frames", type=int, default=20)
+    ap.add_argument("--render-frames", type=int, default=200)
+    ap.add_argument("--psnr-iters", type=int, default=2000,
+                    help="training iterations of the BF16-vs-FP32 PSNR run (0: skip)")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 320^3 / 65536-ray training measurement")
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
@@ -200,12 +210,39 @@ def run_ours(args):
     ms_per_step = step_ms / args.steps
     value = ws_ * args.steps / (step_ms / 1e3)
     stage_ms = stage_profile(tr, dev, nb, flush, args)
+    # ---------------- the FP32 plain method on the same workload, same timing
+    plain = None
+    if args.precision == "bf16":
+        import dataclasses
+        pcfg = dataclasses.replace(cfg, precision=0)
+        pdg, pkg = build_grids(scfg)
+        ptr = FineStageTrainer(pdg, pkg, rgbnet_init(seed=2), pcfg, max_rays=RAYS)
+        for i in range(args.warmup):
+            ptr.step(*dev[i % nb])
+        psteps = min(args.steps, 30)
+        pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(psteps)]
+        torch.cuda.synchronize()
+        for i in range(psteps):
+            flush_l2(flush)
+            pev[i][0].record(st)
+            ptr.step(*dev[(args.warmup + i) % nb])
+            pev[i][1].record(st)
+        torch.cuda.synchronize()
+        pms = float(sum(a.elapsed_time(b) for a, b in pev)) / psteps
+        plain = {"it_s": 1e3 / pms, "ms_per_step": pms, "steps": psteps,
+                 "speedup_bf16": (1e3 / pms and value / (1e3 / pms))}
+        del ptr, pdg, pkg
     # ---------------- end to end through the public API with host buffers
     e2e = run_e2e(tr, ro, rd, vd, tgt, args, flush)
     # ---------------- roofline of the dominant stage
     roof = roofline(stage_ms, tr, scfg)
-    # ---------------- render FPS (config 5)
+    # ---------------- render FPS: 800x800 frames from the merged index
     render = None if args.no_render else run_render(scfg, cfg, cam, tr, args)
+    # ---------------- BF16 vs FP32 quality after training from one seed
+    psnr = run_psnr(scfg, cfg, cam, args.psnr_iters) if args.psnr_iters > 0 else None
+    # ---------------- 320^3 grid, 65536 rays per step
+    large = None if args.no_large else run_large(args)
     out = None
     if rank == 0:
         out = {
@@ -225,8 +262,14 @@ def run_ours(args):
             "wall_s": t_wall, "clocks": clk, "gpu_launches": int(launches),
             "stage_ms": stage_ms, "roofline": roof, "e2e": e2e,
         }
+        if plain:
+            out["fp32_plain"] = plain
         if render:
             out["render"] = render
+        if psnr:
+            out["psnr"] = psnr
+        if large:
+            out["large"] = large
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(scfg, cfg, ro, rd, vd, tgt)
         print(json.dumps(out), flush=True)
@@ -293,7 +336,7 @@ def run_e2e(tr, ro, rd, vd, tgt, args, flush):
             "d2h_bytes_per_step": 4}
 
 
-# Algorithmic work per unit of each train-step stage (the design doc table):
+# Algorithmic work per unit of each train-step stage:
 #   march_fwd       36 B per evaluated sample (8 density corners + the alpha)
 #   k0_gather       8*C*4 + 16 B per colour row (8 k0 corners + row record)
 #   rgbnet_fwd      36,608 FLOP per row + 6,912 per ray (PE part of layer 0)
@@ -378,8 +421,9 @@ def run_render(scfg, cfg, cam, tr, args):
               for t in tr.rgbnet_tensors()]
     poses = spiral_poses(max(args.render_frames, 1), cam.radius, -30.0, seed=0)
     res = {}
-    for storage, tag in ((0, "fp32"), (1, "bf16_features")):
+    for storage, tag in ((0, "fp32"), (1, "bf16")):
         r = MGRenderer(12, 27, 128, 3)
+        r.precision = storage  # BF16 features go with the BF16 tensor-core rgbnet
         r.load_data(den_rows, col_rows, idx, n + 1, storage=storage)
         r.load_params(params[0], params[1], params[2], params[3], params[4], params[5])
         r.setScene([R] * 3, cam.K, cfg.xyz_min, cfg.xyz_max)
@@ -397,6 +441,138 @@ def run_render(scfg, cfg, cam, tr, args):
         img = r.output_an_image()
         res[tag] = {"fps": args.render_frames / dt, "frames": args.render_frames,
                     "mean_rgb": float(img.mean())}
+        res[tag + "_last_frame"] = img
+    a, b = res.pop("fp32_last_frame"), res.pop("bf16_last_frame")
+    res["bf16_vs_fp32_max_abs_rgb"] = float(np.abs(a - b).max())
+    res["speedup_bf16"] = res["bf16"]["fps"] / res["fp32"]["fps"]
+    res["size"] = f"{cam.W}x{cam.H}"
+    res["t_stop"] = 1e-4
+    res["timing"] = "wall clock over the frames after one warm-up frame, synchronised"
+    return res
+
+
+def _forward_rgb(ws, dg, kg, net, ro, rd, vd, cfg, precision, batch=RAYS):
+    """Composited RGB of many rays through the training forward, in batches."""
+    import torch
+
+    from plenvdb_gb300.march import CompositeFn, MarchSample, RgbNetFn, march_params
+    p = march_params(cfg.xyz_min, cfg.xyz_max, cfg.near, cfg.stepdist, cfg.act_shift,
+                     cfg.interval, cfg.fast_color_thres, cfg.bg)
+    dummy = torch.zeros(1, device="cuda")
+    out = []
+    with torch.no_grad():
+        for b in range(0, ro.shape[0], batch):
+            sl = slice(b, b + batch)
+            w, last, k0, _ = MarchSample.apply(dummy, ws, dg, kg, ro[sl], rd[sl], p)
+            rgb = RgbNetFn.apply(k0, vd[sl], ws, 4, precision, *net)
+            out.append(CompositeFn.apply(w, rgb, last, ws, cfg.bg).clone())
+    return torch.cat(out)
+
+
+def run_psnr(scfg, cfg, cam, iters, n_views=8):
+    """FP32 and BF16 fine-stage training from the same seed (same initial grids,
+    rgbnet, ray batches), then PSNR against the ground-truth model on n_views
+    held-out 800x800 views, each model evaluated in its own precision."""
+    import dataclasses
+
+    import torch
+
+    from plenvdb_gb300.march import MarchWorkspace
+    from plenvdb_gb300.scene import (build_grids, random_rays, rays_of_pixels, rgbnet_init,
+                                     sphere_poses)
+    from plenvdb_gb300.trainer import FineStageTrainer
+    t_start = time.perf_counter()
+    ws = MarchWorkspace(RAYS, cfg.xyz_min, cfg.xyz_max, cfg.stepdist)
+    gd, gk = build_grids(scfg, value_seed=4242)
+    gt_net = [t.cuda() for t in rgbnet_init(seed=99)]
+    # training pool: 64 batches of rays over 100 training views, targets from the
+    # ground-truth model
+    pool = [torch.from_numpy(a).cuda() for a in random_rays(cam, 64 * RAYS, 100, seed=11)]
+    tgt = _forward_rgb(ws, gd, gk, gt_net, *pool, cfg, 0)
+    # held-out views (poses not among the training views)
+    poses = sphere_poses(n_views, cam.radius, seed=777)
+    py, px = np.meshgrid(np.arange(cam.H), np.arange(cam.W), indexing="ij")
+    views = []
+    for c2w in poses:
+        o, d, v = rays_of_pixels(cam, c2w, px.reshape(-1), py.reshape(-1))
+        rays = [torch.from_numpy(a).cuda() for a in (o, d, v)]
+        views.append((rays, _forward_rgb(ws, gd, gk, gt_net, *rays, cfg, 0)))
+    del gd, gk
+    gen = torch.Generator(device="cuda")
+    res = {"iters": iters, "views": n_views, "size": f"{cam.W}x{cam.H}", "rays_per_iter": RAYS}
+    for prec, tag in ((0, "fp32"), (1, "bf16")):
+        pcfg = dataclasses.replace(cfg, precision=prec)
+        dg, kg = build_grids(scfg)
+        tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), pcfg, max_rays=RAYS)
+        gen.manual_seed(5)
+        for _ in range(iters):
+            idx = torch.randint(0, pool[0].shape[0], (RAYS,), device="cuda", generator=gen)
+            tr.step(pool[0][idx], pool[1][idx], pool[2][idx], tgt[idx])
+        torch.cuda.synchronize()
+        net = [t.contiguous() for t in tr.rgbnet_tensors()]
+        ps = []
+        for rays, gt in views:
+            img = _forward_rgb(ws, dg, kg, net, *rays, cfg, prec)
+            mse = float(((img - gt) ** 2).mean())
+            ps.append(-10.0 * np.log10(max(mse, 1e-12)))
+        res[f"psnr_{tag}"] = float(np.mean(ps))
+        res[f"psnr_{tag}_per_view"] = [round(x, 3) for x in ps]
+        del tr, dg, kg
+    res["delta_db"] = res["psnr_fp32"] - res["psnr_bf16"]
+    res["wall_s"] = time.perf_counter() - t_start
+    return res
+
+
+def run_large(args, steps=10, warmup=3):
+    """BF16 (and FP32) fine-stage iteration on a 320^3 grid (32 seeded ellipsoids
+    plus a thin shell) with 65536 rays per step; targets from a ground-truth
+    model of the same scene with other seeded values."""
+    import torch
+
+    from plenvdb_gb300.march import MarchWorkspace
+    from plenvdb_gb300.scene import (CameraConfig, SceneConfig, build_grids, random_rays,
+                                     rgbnet_init, scene_mask)
+    from plenvdb_gb300.trainer import FineStageConfig, FineStageTrainer
+    R, reso = 65536, 320
+    t_start = time.perf_counter()
+    scfg = SceneConfig(reso=reso, n_ellipsoids=32, shell=True, seed=0)
+    cam = CameraConfig()
+    res = {"workload": f"fine-stage iteration, {R} rays, {reso}^3 sparse VDB (32 ellipsoids + "
+                       "shell), k0=12, rgbnet 39-128-128-3, TV 1e-4", "rays": R, "reso": reso}
+    nb = 2
+    rays = [torch.from_numpy(a).cuda() for a in random_rays(cam, nb * R, 100, seed=21)]
+    cfg0 = FineStageConfig(reso=reso)
+    gws = MarchWorkspace(R, cfg0.xyz_min, cfg0.xyz_max, cfg0.stepdist)
+    gd, gk = build_grids(scfg, value_seed=4242)
+    tgt = _forward_rgb(gws, gd, gk, [t.cuda() for t in rgbnet_init(seed=99)], *rays, cfg0, 0,
+                       batch=R)
+    del gd, gk, gws
+    res["active_fraction"] = float(scene_mask(scfg).mean())
+    for prec, tag in ((1, "bf16"), (0, "fp32")):
+        cfg = FineStageConfig(reso=reso, precision=prec)
+        dg, kg = build_grids(scfg)
+        tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), cfg, max_rays=R)
+        batches = [tuple(t[b * R:(b + 1) * R] for t in (*rays, tgt)) for b in range(nb)]
+        for i in range(warmup):
+            tr.step(*batches[i % nb])
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for i in range(steps):
+            tr.step(*batches[i % nb])
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        kept, rows, evaluated = tr.ws.stats()
+        res[tag] = {"it_s": 1e3 / ms, "ms_per_step": ms, "rays_per_s": R * 1e3 / ms,
+                    "kept_samples": kept, "color_rows": rows, "evaluated_samples": evaluated,
+                    "loss": float(tr.loss.item())}
+        del tr, dg, kg
+    res["speedup_bf16"] = res["bf16"]["it_s"] / res["fp32"]["it_s"]
+    res["timing"] = (f"CUDA events over {steps} steps after {warmup} warm-up steps; inputs "
+                     "(2 x 65536 rays) larger than L2 are not the dominant traffic, no flush")
+    res["wall_s"] = time.perf_counter() - t_start
     return res
 
 

@@ -357,7 +357,8 @@ int pvdb_march_backward(pvdb_march m, pvdb_grid density, pvdb_grid k0, const flo
                         const float* grad_last, const float* grad_k0, pvdb_stream s);
 
 /* Deterministic per-ray composite (segment_coo sum + bg, dvgo.py:365-370):
- * rgb_marched[r] = sum_m weight[m]*rgb[m] + alphainv_last[r]*bg over rows of ray r. */
+ * rgb_marched[r] = sum_m weight[m]*rgb[m] + alphainv_last[r]*bg over rows of ray r.
+ * rgb may be NULL when the forward kept no colour row (M == 0): no row is read. */
 int pvdb_composite_forward(pvdb_march m, const float* rgb, float bg, float* rgb_marched,
                            int32_t n_rays, pvdb_stream s);
 /* grad_rgb[m] = weight[m]*g[r]; grad_weight[m] = dot(g[r], rgb[m]);

@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kMarchThreads)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
-  const int n = int(W.n_color[r]);
+  const int n = rgb ? int(W.n_color[r]) : 0;  // NULL rgb: no colour rows
   const int64_t off = W.color_off[r];
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   for (int j = lane; j < n; j += 32) {
@@ -959,7 +959,6 @@ int pvdb_composite_forward(pvdb_march m, const float* rgb, float bg, float* rgb_
   clear_error();
   PVDB_REQUIRE(m && rgb_marched, "null argument");
   PVDB_REQUIRE(m->has_fwd && n_rays == m->n_rays, "n_rays differs from the forward's");
-  PVDB_REQUIRE(rgb || n_rays == 0, "null rgb");
   return composite_forward_impl(m, rgb, bg, rgb_marched, n_rays, as_stream(s));
 }
 

@@ -260,3 +260,43 @@ def test_graph_replay_matches_eager_steps(setup, precision):
     assert eager[0] == graph[0]
     for a, b in zip(eager[1:], graph[1:]):
         assert np.array_equal(np.asarray(a), np.asarray(b))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_rays_that_miss_the_scene(setup, precision):
+    """Rays pointing away from the bbox keep no sample: the three stages and
+    their backward run with zero colour rows, the composite is bg, and the
+    fused step leaves the grids unchanged apart from nothing to update."""
+    import torch
+    from plenvdb_gb300.march import CompositeFn, MarchSample, MarchWorkspace, RgbNetFn
+    from plenvdb_gb300.scene import build_grids, rgbnet_init
+    from plenvdb_gb300.trainer import FineStageTrainer
+    s = setup
+    cfg = s["cfg"]
+    R = 64
+    ro = torch.full((R, 3), 5.0, device="cuda")
+    rd = torch.nn.functional.normalize(torch.rand(R, 3, device="cuda") + 0.1, dim=-1)
+    vd = rd.clone()
+    dg, kg = build_grids(s["scfg"])
+    ws = MarchWorkspace(256, cfg.xyz_min, cfg.xyz_max, cfg.stepdist)
+    dummy = torch.zeros(1, device="cuda", requires_grad=True)
+    params = [p.cuda().requires_grad_() for p in rgbnet_init(seed=2)]
+    w, last, k0, rid = MarchSample.apply(dummy, ws, dg, kg, ro, rd, s["gp"])
+    assert w.shape[0] == 0 and k0.shape[0] == 0
+    rgb = RgbNetFn.apply(k0, vd, ws, 4, precision, *params)
+    out = CompositeFn.apply(w, rgb, last, ws, 0.25)
+    torch.testing.assert_close(out, torch.full((R, 3), 0.25, device="cuda"))
+    torch.testing.assert_close(last, torch.ones(R, device="cuda"))
+    out.sum().backward()
+    torch.cuda.synchronize()
+    from plenvdb_gb300 import _lib as L
+    assert float(np.abs(dg.get_dense_grid(L.WHICH_GRAD)).max()) == 0.0
+    # the fused step on the same rays
+    dg2, kg2 = build_grids(s["scfg"])
+    before = dg2.get_dense_grid().copy()
+    tr = FineStageTrainer(dg2, kg2, rgbnet_init(seed=2),
+                          type(cfg)(**{**cfg.__dict__, "precision": precision}), max_rays=256)
+    tgt = torch.zeros(R, 3, device="cuda")
+    loss = float(tr.step(ro, rd, vd, tgt))
+    assert np.isfinite(loss)
+    np.testing.assert_array_equal(dg2.get_dense_grid(), before)

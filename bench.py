@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--render-frames", type=int, default=200)
     ap.add_argument("--psnr-iters", type=int, default=2000,
                     help="training iterations of the BF16-vs-FP32 PSNR run (0: skip)")
+    ap.add_argument("--no-fp32-plain", action="store_true",
+                    help="skip the FP32 plain-method leg of a --precision bf16 run")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 320^3 / 65536-ray training measurement")
     ap.add_argument("--no-render", action="store_true")
@@ -212,7 +214,7 @@ def run_ours(args):
     stage_ms = stage_profile(tr, dev, nb, flush, args)
     # ---------------- the FP32 plain method on the same workload, same timing
     plain = None
-    if args.precision == "bf16":
+    if args.precision == "bf16" and not args.no_fp32_plain:
         import dataclasses
         pcfg = dataclasses.replace(cfg, precision=0)
         pdg, pkg = build_grids(scfg)
@@ -298,7 +300,7 @@ def stage_profile(tr, dev, nb, flush, args):
     L.call("pvdb_profile_end", marks, 16, ctypes.byref(ncalls))
     tr.tc.use_graph = use_graph
     stage_names = {1: "march_fwd", 2: "k0_gather", 3: "rgbnet_fwd", 4: "composite_loss",
-                   5: "rgbnet_bwd", 6: "march_bwd", 7: "radix_sort", 8: "segment_reduce",
+                   5: "rgbnet_bwd", 6: "march_bwd", 7: "cell_grouping", 8: "voxel_gather",
                    9: "tv", 10: "voxel_adam", 11: "rgbnet_adam"}
     return {stage_names[i]: marks[i] / max(1, ncalls.value) for i in stage_names}
 
@@ -343,8 +345,9 @@ def run_e2e(tr, ro, rd, vd, tgt, args, flush):
 #   rgbnet_bwd      122,880 FLOP per row (backward GEMMs + layer 0/1 recompute)
 #   march_bwd       120 B per kept sample (saved alpha/weight/step/row, grad,
 #                   8 density corners, 64 B gradient record, 4 B key)
-#   radix_sort      (8 B read + 8 B write) * passes + 4 B histogram per key
-#   segment_reduce  64 B record + 8 corner partials (1 + C floats) per kept sample
+#   cell_grouping   32 B per kept sample (key read twice, rank written and read,
+#                   cell offset read, grouped key and index written)
+#   voxel_gather    64 B record + 8 corner gradients (1 + C floats) per kept sample
 #   voxel_adam      28 B per visited voxel-channel (p, g, m, v read; p, m, v written)
 RGBNET_FWD_ROW, RGBNET_FWD_RAY, RGBNET_BWD_ROW = 36608.0, 6912.0, 122880.0
 
@@ -353,15 +356,14 @@ def stage_work(tr, R):
     """(bound, algorithmic units per launch) of each stage for the last step."""
     kept, rows, evaluated = tr.ws.stats()
     C = 12
-    npass = 3
     return {
         "march_fwd": ("hbm", evaluated * 36.0),
         "k0_gather": ("hbm", rows * (8 * C * 4 + 16.0)),
         "rgbnet_fwd": ("tensor", rows * RGBNET_FWD_ROW + R * RGBNET_FWD_RAY),
         "rgbnet_bwd": ("tensor", rows * RGBNET_BWD_ROW),
         "march_bwd": ("hbm", kept * 120.0),
-        "radix_sort": ("hbm", kept * (16.0 * npass + 4.0)),
-        "segment_reduce": ("hbm", kept * (64.0 + 8 * (1 + C) * 4.0)),
+        "cell_grouping": ("hbm", kept * 32.0),
+        "voxel_gather": ("hbm", kept * (64.0 + 8 * (1 + C) * 4.0)),
     }, (kept, rows, evaluated)
 
 

@@ -418,17 +418,27 @@ __global__ void __launch_bounds__(kMarchThreads)
 //
 // Each kept sample s sits in the trilinear cell whose low corner is
 // floor(idx); its 8 corners receive w_c * gs (density) and w_c * gk0[row]
-// (k0). The samples are stably radix-sorted by cell key, a leaf-major code of
-// the cell's low corner, so each cell's samples form one segment in ascending
-// sample order, and the first sorted index of each cell goes into a dense cell
-// map (which also flags the leaves of the cell's corners as touched). Then one
-// thread per voxel of the touched leaves computes
+// (k0). The cell key is a leaf-major code of the low corner (dense leaf index
+// x 512 + NanoVDB offset). The samples are grouped by cell with a counting
+// placement:
+//   k_cell_count   per sample: its rank among the samples of its cell (an
+//                  atomic counter, so in no particular order) and the counts
+//                  per cell and per leaf;
+//   leaf scan      exclusive scan of the per-leaf counts (one block);
+//   k_cell_offsets per leaf with samples: exclusive scan of its 512 cell
+//                  counts, offset by the leaf's start;
+//   k_cell_place   per sample: position = cell offset + rank;
+//   k_cell_heads   per cell: sorts its segment by sample index (so the
+//                  placement equals a stable sort by key: each cell's samples
+//                  contiguous, in ascending sample order), and flags the leaves
+//                  holding the cell's corners as touched.
+// Then one thread per voxel of the touched leaves computes
 //   grad += sum over c' = 0..7, in that order, of
 //           (sum over the samples of cell v - delta(c'), in sample order,
-//            of that sample's corner-c' contribution)
-// for the cells present in the map. Every sum has an order fixed by the data,
-// so the result is bitwise reproducible without atomics. Corners in no
-// allocated leaf are dropped (densityvdb.cu:23).
+//            of that sample's corner-c' contribution).
+// Every sum has an order fixed by the data, so the result is bitwise
+// reproducible without atomics on floats. Corners in no allocated leaf are
+// dropped (densityvdb.cu:23).
 __device__ __forceinline__ void cell_decode(const int ld[3], uint32_t key, int& i, int& j, int& k) {
   const int leaf = int(key >> 9), off = int(key & 511u);
   const int lk = leaf % ld[2];
@@ -437,11 +447,6 @@ __device__ __forceinline__ void cell_decode(const int ld[3], uint32_t key, int& 
   i = (li << 3) | (off >> 6);
   j = (lj << 3) | ((off >> 3) & 7);
   k = (lk << 3) | (off & 7);
-}
-
-__device__ __forceinline__ bool seg_head(const uint32_t* __restrict__ skeys, int64_t i) {
-  const uint32_t key = skeys[i];
-  return key != kInvalidKey && (i == 0 || skeys[i - 1] != key);
 }
 
 __device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, int cj, int ck,
@@ -453,30 +458,131 @@ __device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, in
     if (s[c] >= 0) touched[s[c] >> 9] = 1;
 }
 
-// Marks the cells present in the cell map and flags the leaves holding their
-// corners as touched in the density grid and (touched_c != NULL) the k0 grid.
-__global__ void k_cell_map_set(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
-                               int32_t* map, GridView gd, GridView gc, uint8_t* touched_d,
-                               uint8_t* touched_c) {
+__global__ void k_cell_count(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
+                             uint32_t* cnt, uint32_t* leaf_cnt, uint32_t* rank) {
   const int64_t n = *n_dev;
-  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    if (seg_head(skeys, i)) {
-      const uint32_t key = skeys[i];
-      map[key] = int32_t(i);
-      int ci, cj, ck;
-      cell_decode(gd.ldim, key, ci, cj, ck);
-      mark_corner_leaves(gd, ci, cj, ck, touched_d);
-      if (touched_c) mark_corner_leaves(gc, ci, cj, ck, touched_c);
-    }
+  for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
+       s += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t key = keys[s];
+    if (key == kInvalidKey) continue;
+    rank[s] = atomicAdd(cnt + key, 1u);
+    atomicAdd(leaf_cnt + (key >> 9), 1u);
+  }
 }
 
-__global__ void k_cell_map_clear(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
-                                 int32_t* map) {
+// Block (512 threads) per dense leaf with samples.
+__global__ void __launch_bounds__(kLeafVox)
+    k_cell_offsets(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ leaf_cnt,
+                   const uint32_t* __restrict__ leaf_off, int64_t nleaves, uint32_t* off) {
+  __shared__ uint32_t warp_sums[kLeafVox / 32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
+    if (leaf_cnt[l] == 0) continue;  // uniform over the block
+    const int64_t e = l * kLeafVox + t;
+    const uint32_t v = cnt[e];
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      uint32_t s = lane < kLeafVox / 32 ? warp_sums[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      if (lane < kLeafVox / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    off[e] = leaf_off[l] + (w ? warp_sums[w - 1] : 0u) + x - v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_cell_place(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
+                             const uint32_t* __restrict__ off, const uint32_t* __restrict__ rank,
+                             uint32_t* skeys, uint32_t* svals) {
+  const int64_t n = *n_dev;
+  for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
+       s += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t key = keys[s];
+    if (key == kInvalidKey) continue;
+    const uint32_t pos = off[key] + rank[s];
+    skeys[pos] = key;
+    svals[pos] = uint32_t(s);
+  }
+}
+
+// Ascending sort of a[0..len): insertion sort for short segments, heapsort
+// (O(len log len), in place) for long ones.
+__device__ void sort_segment(uint32_t* a, uint32_t len) {
+  if (len <= 24) {
+    for (uint32_t i = 1; i < len; ++i) {
+      const uint32_t v = a[i];
+      uint32_t j = i;
+      while (j > 0 && a[j - 1] > v) {
+        a[j] = a[j - 1];
+        --j;
+      }
+      a[j] = v;
+    }
+    return;
+  }
+  auto sift = [&](uint32_t root, uint32_t end) {
+    for (;;) {
+      uint32_t child = 2 * root + 1;
+      if (child >= end) return;
+      if (child + 1 < end && a[child + 1] > a[child]) ++child;
+      if (a[root] >= a[child]) return;
+      const uint32_t t = a[root];
+      a[root] = a[child];
+      a[child] = t;
+      root = child;
+    }
+  };
+  for (uint32_t r = len / 2; r-- > 0;) sift(r, len);
+  for (uint32_t end = len - 1; end > 0; --end) {
+    const uint32_t t = a[0];
+    a[0] = a[end];
+    a[end] = t;
+    sift(0, end);
+  }
+}
+
+// Thread per placed index; cell heads sort their segment and flag the leaves
+// of the cell's corners as touched in the density grid and (touched_c !=
+// NULL) the k0 grid.
+__global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
+                             const uint32_t* __restrict__ cnt, uint32_t* svals, GridView gd,
+                             GridView gc, uint8_t* touched_d, uint8_t* touched_c) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x)
-    if (seg_head(skeys, i)) map[skeys[i]] = -1;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t key = skeys[i];
+    if (i > 0 && skeys[i - 1] == key) continue;
+    sort_segment(svals + i, cnt[key]);
+    int ci, cj, ck;
+    cell_decode(gd.ldim, key, ci, cj, ck);
+    mark_corner_leaves(gd, ci, cj, ck, touched_d);
+    if (touched_c) mark_corner_leaves(gc, ci, cj, ck, touched_c);
+  }
+}
+
+// Resets the counts of the cells and leaves that got samples.
+__global__ void k_cell_clear(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
+                             uint32_t* cnt, uint32_t* leaf_cnt) {
+  const int64_t n = *n_dev;
+  for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
+       s += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t key = keys[s];
+    if (key == kInvalidKey) continue;
+    cnt[key] = 0u;
+    leaf_cnt[key >> 9] = 0u;
+  }
 }
 
 // Corner weight c of the multi-channel formula, ((a*b)*c) (colorvdb.cu:100-107).
@@ -493,10 +599,9 @@ __device__ __forceinline__ float corner_scale(float u, float v, float w, int c) 
 template <int NQ>
 __global__ void __launch_bounds__(256)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
-                   const int32_t* __restrict__ map, const uint32_t* __restrict__ skeys,
-                   const uint32_t* __restrict__ svals, const uint32_t* n_dev,
-                   const float4* __restrict__ rec, float* grad_d, float* grad_c, int C) {
-  const int64_t n = *n_dev;
+                   const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
+                   const uint32_t* __restrict__ svals, const float4* __restrict__ rec,
+                   float* grad_d, float* grad_c, int C) {
   const int64_t nv = int64_t(*count) * kLeafVox;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -516,14 +621,15 @@ __global__ void __launch_bounds__(256)
       corner_delta(c, di, dj, dk);
       const uint32_t key = cell_key(g.ldim, vi - di, vj - dj, vk - dk);
       if (key == kInvalidKey) continue;
-      const int32_t h = __ldg(map + key);
-      if (h < 0) continue;
+      const uint32_t len = __ldg(cnt + key);
+      if (len == 0) continue;
+      const uint32_t h = __ldg(off + key);
       any = true;
       float pd = 0.f;
       float4 pk[NQ > 0 ? NQ : 1];
 #pragma unroll
       for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int64_t j = h; j < n && skeys[j] == key; ++j) {
+      for (uint32_t j = h; j < h + len; ++j) {
         const float4* r = rec + int64_t(svals[j]) * (1 + NQ);
         const float4 p = r[0];
         const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
@@ -572,24 +678,25 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const int grid = stride_grid();
   const GridView gv = density->view();
   const GridView kv = NQ ? k0->view() : gv;
-  k_cell_map_set<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map, gv, kv,
-                                       density->d_touched, NQ ? k0->d_touched : nullptr);
-  PVDB_CHECK_LAUNCH("k_cell_map_set");
+  k_cell_heads<<<grid, 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt,
+                                     const_cast<uint32_t*>(svals), gv, kv, density->d_touched,
+                                     NQ ? k0->d_touched : nullptr);
+  PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;
   if (NQ) k0->tlist_valid = false;
   int rc = touched_list(density, st);
   if (rc) return rc;
   const bool same = NQ && k0->h_table == density->h_table;
   const int C = NQ ? k0->C : 0;
-  k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_map,
-                                           skeys, svals, m->w.totals + 0, m->w.b_rec,
-                                           density->d_grad, same ? k0->d_grad : nullptr, C);
+  k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_cnt,
+                                           m->cell_off, svals, m->w.b_rec, density->d_grad,
+                                           same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
-    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_map, skeys,
-                                             svals, m->w.totals + 0, m->w.b_rec, nullptr,
-                                             k0->d_grad, C);
+    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
+                                             m->cell_off, svals, m->w.b_rec, nullptr, k0->d_grad,
+                                             C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -749,13 +856,21 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   int rc = scratch_reserve(m->red, nmax);
   if (rc) return rc;
   const int64_t ncells = int64_t(density->ldim[0]) * density->ldim[1] * density->ldim[2] * kLeafVox;
-  if (m->cell_map_cap < size_t(ncells)) {
-    dev_free(m->cell_map);
-    m->cell_map = nullptr;
-    m->cell_map_cap = 0;
-    if ((rc = dev_alloc((void**)&m->cell_map, size_t(ncells) * 4))) return rc;
-    PVDB_CHECK_CUDA(cudaMemsetAsync(m->cell_map, 0xFF, size_t(ncells) * 4, st));
-    m->cell_map_cap = size_t(ncells);
+  const int64_t nleaves = ncells / kLeafVox;
+  if (m->cell_cap < size_t(ncells)) {
+    for (uint32_t** p : {&m->cell_cnt, &m->cell_off, &m->leaf_cnt, &m->leaf_off}) {
+      dev_free(*p);
+      *p = nullptr;
+    }
+    m->cell_cap = 0;
+    if ((rc = dev_alloc((void**)&m->cell_cnt, size_t(ncells) * 4)) ||
+        (rc = dev_alloc((void**)&m->cell_off, size_t(ncells) * 4)) ||
+        (rc = dev_alloc((void**)&m->leaf_cnt, size_t(nleaves) * 4)) ||
+        (rc = dev_alloc((void**)&m->leaf_off, size_t(nleaves) * 4)))
+      return rc;
+    PVDB_CHECK_CUDA(cudaMemsetAsync(m->cell_cnt, 0, size_t(ncells) * 4, st));
+    PVDB_CHECK_CUDA(cudaMemsetAsync(m->leaf_cnt, 0, size_t(nleaves) * 4, st));
+    m->cell_cap = size_t(ncells);
   }
   const bool use_k0 = k0 && grad_k0;
   const int C = use_k0 ? k0->C : 0;
@@ -768,14 +883,23 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
                                             use_k0 ? grad_k0 : nullptr, C, m->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
-  int buf = 0;
-  rc = radix_sort_pairs_dev(m->red, nmax, m->w.totals + 0, slot_key_bits(ncells), true, &buf, st,
-                            m->w.totals + 3);
+  // group the kept samples by cell (stable order, see above)
+  const uint32_t* keys = m->red.keys[0];
+  uint32_t* rank = m->red.vals[1];
+  uint32_t* skeys = m->red.keys[1];
+  uint32_t* svals = m->red.vals[0];
+  const int sgrid = int(std::min<int64_t>(ceil_div(nmax, 256), int64_t(stride_grid())));
+  k_cell_count<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_cnt, m->leaf_cnt, rank);
+  PVDB_CHECK_LAUNCH("k_cell_count");
+  rc = scan_exclusive_u32(m->leaf_cnt, m->leaf_off, nleaves, m->w.totals + 5, &m->scan_partial,
+                          &m->scan_partial_cap, st);
   if (rc) return rc;
+  k_cell_offsets<<<int(std::min<int64_t>(nleaves, int64_t(num_sms()) * 4)), kLeafVox, 0, st>>>(
+      m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off);
+  PVDB_CHECK_LAUNCH("k_cell_offsets");
+  k_cell_place<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
+  PVDB_CHECK_LAUNCH("k_cell_place");
   if (m->prof) prof_mark(st, 7);
-  const uint32_t* skeys = m->red.keys[buf];
-  const uint32_t* svals = m->red.vals[buf];
-  const int grid = stride_grid();
   switch (nq) {
     case 0: rc = cell_reduce_launch<0>(m, density, k0, skeys, svals, st); break;
     case 1: rc = cell_reduce_launch<1>(m, density, k0, skeys, svals, st); break;
@@ -784,8 +908,8 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
     default: rc = cell_reduce_launch<4>(m, density, k0, skeys, svals, st); break;
   }
   if (rc) return rc;
-  k_cell_map_clear<<<grid, 256, 0, st>>>(skeys, m->w.totals + 0, m->cell_map);
-  PVDB_CHECK_LAUNCH("k_cell_map_clear");
+  k_cell_clear<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
+  PVDB_CHECK_LAUNCH("k_cell_clear");
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
 }
@@ -870,7 +994,7 @@ int pvdb_march_destroy(pvdb_march m) {
                   m->t_loss_part, m->t_rgb_marched};
   for (void* p : ptrs) dev_free(p);
   free_scratch(m->red);
-  dev_free(m->cell_map);
+  for (uint32_t* p : {m->cell_cnt, m->cell_off, m->leaf_cnt, m->leaf_off}) dev_free(p);
   dev_free(m->g_in);
   dev_free(m->g_scal);
   if (m->g_exec) cudaGraphExecDestroy(m->g_exec);

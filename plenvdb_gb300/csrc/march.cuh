@@ -50,7 +50,7 @@ struct MarchW {
   float4* b_rec;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 sort look-back wait),
-  // [4] samples evaluated, [5] unused
+  // [4] samples evaluated, [5] samples grouped by cell (backward), [5] unused
   uint32_t* totals;
 };
 
@@ -62,9 +62,14 @@ struct pvdb_march_s {
   int64_t slots = 0;  // max_rays * cap
   int k0_channels = 0;
   pvdb::MarchW w{};
-  pvdb::ReduceScratch red;   // kept samples sorted by cell key
-  int32_t* cell_map = nullptr;  // [cells of the leaf lattice] first sorted index, -1 = none
-  size_t cell_map_cap = 0;      // elements
+  pvdb::ReduceScratch red;   // kept samples grouped by cell key
+  // per cell of the leaf lattice (dense leaf-major keys): sample count (zero
+  // between calls) and first grouped index; per dense leaf: count and start
+  uint32_t* cell_cnt = nullptr;
+  uint32_t* cell_off = nullptr;
+  uint32_t* leaf_cnt = nullptr;
+  uint32_t* leaf_off = nullptr;
+  size_t cell_cap = 0;  // cells
   size_t b_rec_cap = 0;         // bytes of w.b_rec
   uint32_t* scan_partial = nullptr;
   size_t scan_partial_cap = 0;

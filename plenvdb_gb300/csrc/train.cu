@@ -322,7 +322,10 @@ static std::vector<uint8_t> graph_key(const TrainArgs& t) {
   key_put(k, m->red.hist);
   key_put(k, m->red.partial);
   key_put(k, m->scan_partial);
-  key_put(k, m->cell_map);
+  key_put(k, m->cell_cnt);
+  key_put(k, m->cell_off);
+  key_put(k, m->leaf_cnt);
+  key_put(k, m->leaf_off);
   key_put(k, m->t_rgb);
   key_put(k, m->t_grad_k0);
   key_put(k, m->g_in);

@@ -11,16 +11,16 @@
 // kept samples. Only per-ray alpha / weight / step lists are kept for the
 // backward.
 //
-// k_march_rowmeta / k_march_k0 lay the colour samples (weight > thres,
-// dvgo.py:329-335) out as dense rows and sample the k0 grid there
+// k_march_chain also lays the colour samples (weight > thres,
+// dvgo.py:329-335) out as dense rows, and k_march_k0 samples the k0 grid there
 // (colorvdb.cu:81-111).
 //
 // Backward (k_march_bwd) recovers transmittance from the saved alphas and
 // weights, runs alpha2weight_backward (:653-677) as a suffix scan and
 // raw2alpha_backward (:506-517), and keys every kept sample by its trilinear
-// cell; a stable radix sort by cell, per-cell partial sums and a per-voxel
-// gather over the touched leaves then add the density and k0 gradients
-// deterministically (see the reduction below).
+// cell; a counting placement groups the samples by cell in sample order and a
+// per-voxel gather over the touched leaves then adds the density and k0
+// gradients deterministically (see the reduction below).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -52,7 +52,8 @@ __device__ __forceinline__ void load_ray(const float* __restrict__ ro, const flo
 //  k_march_chain (warp per ray): the transmittance chain over the kept
 //    samples in order, the T < t_stop early stop, and the in-place compaction
 //    of the kept samples (a kept sample moves to a slot at or before its own,
-//    after the whole chunk has been read).
+//    after the whole chunk has been read); then the ray's offsets among all
+//    kept samples and colour rows, and its colour rows' records.
 __global__ void __launch_bounds__(256)
     k_march_setup(const float* __restrict__ ro, const float* __restrict__ rd, int R, MarchP P,
                   MarchW W) {
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(256)
   }
   W.ray_ns[r] = int32_t(ns);
   atomicAdd(W.totals + 4, uint32_t(ns));
+  if (r < (R + kMarchWarps - 1) / kMarchWarps) W.chain_status[r] = 0ull;  // k_march_chain tiles
 }
 
 // One block per ray, threads over the ray's samples.
@@ -117,134 +119,137 @@ __global__ void __launch_bounds__(256)
 
 constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
 
+// Ray offsets: CTAs take 8-ray tiles in order from a counter (totals[6]); a
+// tile publishes its (colour, kept) counts, then sums the earlier tiles'
+// published counts back to the first inclusive prefix (decoupled look-back).
+// A tile publishes before it waits and only waits on tiles taken earlier
+// (running or done), so every wait ends; each is still bounded, and one that
+// gives up sets error bit 4.
+constexpr uint64_t kChainAgg = 1ull << 62;     // status: tile counts published
+constexpr uint64_t kChainPrefix = 1ull << 63;  // status: inclusive prefix published
+constexpr uint64_t kChainValue = kChainAgg - 1;
+constexpr uint32_t kChainSpinMax = 1u << 24;
+
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_chain(int R, MarchP P, MarchW W) {
+  __shared__ int tile_s;
+  __shared__ uint64_t wcnt[kMarchWarps];  // (colour << 32) | kept per ray
+  __shared__ uint64_t base_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kMarchWarps + warp;
-  if (r >= R) return;
-  const int ns = W.ray_ns[r];
+  if (threadIdx.x == 0) tile_s = int(atomicAdd(W.totals + 6, 1u));
+  __syncthreads();
+  const int tile = tile_s;
+  const int r = tile * kMarchWarps + warp;
   const unsigned lt = lanemask_lt();
   const int64_t sbase = int64_t(r) * P.cap;
-  float T = 1.f;
   int nk = 0, nc = 0;
-  bool stop = false;
-  for (int b0 = 0; b0 < ns && !stop; b0 += 32 * kChainBatch) {
-    // the batch's alphas, loaded before any of them is used
-    float al[kChainBatch];
+  if (r < R) {
+    const int ns = W.ray_ns[r];
+    float T = 1.f;
+    bool stop = false;
+    for (int b0 = 0; b0 < ns && !stop; b0 += 32 * kChainBatch) {
+      // the batch's alphas, loaded before any of them is used
+      float al[kChainBatch];
 #pragma unroll
-    for (int j = 0; j < kChainBatch; ++j) {
-      const int k = b0 + 32 * j + lane;
-      al[j] = k < ns ? W.k_alpha[sbase + k] : 0.f;
-    }
-    __syncwarp();  // every lane has read its alphas before the compaction writes
+      for (int j = 0; j < kChainBatch; ++j) {
+        const int k = b0 + 32 * j + lane;
+        al[j] = k < ns ? W.k_alpha[sbase + k] : 0.f;
+      }
+      __syncwarp();  // every lane has read its alphas before the compaction writes
 #pragma unroll
-    for (int j = 0; j < kChainBatch; ++j) {
-      if (stop) continue;
-      const int k = b0 + 32 * j + lane;
-      unsigned km = __ballot_sync(0xffffffffu, al[j] > P.thr);
-      // alpha2weight over the kept lanes, in sample order (uniform across the warp)
-      float w = 0.f;
-      unsigned rem = km;
-      while (rem) {
-        const int l = __ffs(rem) - 1;
-        rem &= rem - 1;
-        const float a = __shfl_sync(0xffffffffu, al[j], l);
-        const float wl = T * a;
-        if (lane == l) w = wl;
-        T = trans_step(T, a);
-        if (T < P.t_stop) {
-          km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
-          stop = true;
-          break;
+      for (int j = 0; j < kChainBatch; ++j) {
+        if (stop) continue;
+        const int k = b0 + 32 * j + lane;
+        unsigned km = __ballot_sync(0xffffffffu, al[j] > P.thr);
+        // alpha2weight over the kept lanes, in sample order (uniform across the warp)
+        float w = 0.f;
+        unsigned rem = km;
+        while (rem) {
+          const int l = __ffs(rem) - 1;
+          rem &= rem - 1;
+          const float a = __shfl_sync(0xffffffffu, al[j], l);
+          const float wl = T * a;
+          if (lane == l) w = wl;
+          T = trans_step(T, a);
+          if (T < P.t_stop) {
+            km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
+            stop = true;
+            break;
+          }
         }
+        const bool kept = (km >> lane) & 1u;
+        const bool col = kept && (w > P.thr);
+        const unsigned cm = __ballot_sync(0xffffffffu, col);
+        if (kept) {
+          const int64_t pos = sbase + nk + __popc(km & lt);
+          W.k_alpha[pos] = al[j];
+          W.k_w[pos] = w;
+          W.k_step[pos] = int32_t(k) | (col ? int32_t(0x80000000) : 0);
+          W.k_row[pos] = col ? nc + __popc(cm & lt) : -1;  // rank among the ray's colour rows
+        }
+        nk += __popc(km);
+        nc += __popc(cm);
       }
-      const bool kept = (km >> lane) & 1u;
-      const bool col = kept && (w > P.thr);
-      const unsigned cm = __ballot_sync(0xffffffffu, col);
-      if (kept) {
-        const int64_t pos = sbase + nk + __popc(km & lt);
-        W.k_alpha[pos] = al[j];
-        W.k_w[pos] = w;
-        W.k_step[pos] = int32_t(k) | (col ? int32_t(0x80000000) : 0);
-        W.k_row[pos] = col ? nc + __popc(cm & lt) : -1;  // rank among the ray's colour rows
-      }
-      nk += __popc(km);
-      nc += __popc(cm);
+    }
+    if (lane == 0) {
+      W.T_last[r] = T;
+      W.n_kept[r] = nk;
+      W.n_color[r] = nc;
     }
   }
-  if (lane == 0) {
-    W.T_last[r] = T;
-    W.n_kept[r] = nk;
-    W.n_color[r] = nc;
-  }
-}
-
-// Per-ray offsets of the kept samples and colour rows (exclusive prefix sums
-// of n_kept and n_color, in ray order) and the totals, in one block: both
-// counts ride in one 64-bit word (colour count in the high half).
-__device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t* total) {
-  __shared__ uint64_t ws[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  uint64_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) ws[wid] = x;
+  if (lane == 0) wcnt[warp] = (uint64_t(nc) << 32) | uint64_t(uint32_t(nk));
   __syncthreads();
-  if (wid == 0) {
-    uint64_t s = lane < nw ? ws[lane] : 0ull;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint64_t y = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < nw) ws[lane] = s;
-  }
-  __syncthreads();
-  const uint64_t r = (wid ? ws[wid - 1] : 0ull) + x - v;
-  *total = ws[nw - 1];
-  __syncthreads();
-  return r;
-}
-
-constexpr int kOffThreads = 1024;
-constexpr int kOffItems = 4;
-
-__global__ void __launch_bounds__(kOffThreads) k_march_offsets(MarchW W, int R) {
-  __shared__ uint64_t buf[kOffThreads * kOffItems];
-  uint64_t carry = 0;
-  for (int c0 = 0; c0 < R; c0 += kOffThreads * kOffItems) {
-#pragma unroll
-    for (int q = 0; q < kOffItems; ++q) {  // coalesced loads
-      const int i = c0 + q * kOffThreads + threadIdx.x;
-      buf[q * kOffThreads + threadIdx.x] =
-          i < R ? (uint64_t(W.n_color[i]) << 32) | uint64_t(W.n_kept[i]) : 0ull;
-    }
-    __syncthreads();
-    uint64_t v[kOffItems], s = 0;
-#pragma unroll
-    for (int q = 0; q < kOffItems; ++q) {
-      v[q] = buf[threadIdx.x * kOffItems + q];
-      s += v[q];
-    }
-    uint64_t tot;
-    uint64_t run = block_excl_scan64(s, &tot) + carry;
-#pragma unroll
-    for (int q = 0; q < kOffItems; ++q) {
-      const int i = c0 + threadIdx.x * kOffItems + q;
-      if (i < R) {
-        W.kept_off[i] = uint32_t(run);
-        W.color_off[i] = uint32_t(run >> 32);
-      }
-      run += v[q];
-    }
-    carry += tot;
-  }
   if (threadIdx.x == 0) {
-    W.totals[0] = uint32_t(carry);
-    W.totals[1] = uint32_t(carry >> 32);
+    uint64_t agg = 0;
+#pragma unroll
+    for (int q = 0; q < kMarchWarps; ++q) agg += wcnt[q];
+    volatile uint64_t* status = W.chain_status;
+    uint64_t excl = 0;
+    if (tile == 0) {
+      status[0] = kChainPrefix | agg;
+    } else {
+      status[tile] = kChainAgg | agg;
+      for (int t = tile - 1; t >= 0; --t) {
+        uint64_t v = status[t];
+        for (uint32_t it = 0; v == 0ull; ++it) {
+          if (it >= kChainSpinMax) {
+            atomicOr(W.totals + 3, 4u);
+            v = kChainPrefix;  // give up: offsets wrong, but the kernel ends
+            break;
+          }
+          v = status[t];
+        }
+        excl += v & kChainValue;
+        if (v & kChainPrefix) break;
+      }
+      status[tile] = kChainPrefix | (excl + agg);
+    }
+    base_s = excl;
+    if ((tile + 1) * kMarchWarps >= R) {
+      W.totals[0] = uint32_t(excl + agg);
+      W.totals[1] = uint32_t((excl + agg) >> 32);
+    }
+  }
+  __syncthreads();
+  if (r >= R) return;
+  uint64_t off = base_s;
+  for (int q = 0; q < warp; ++q) off += wcnt[q];
+  const uint32_t coff = uint32_t(off >> 32);
+  if (lane == 0) {
+    W.kept_off[r] = uint32_t(off);
+    W.color_off[r] = coff;
+  }
+  // colour rows: global row m = color_off + rank, the row record, k_row = m
+  for (int i = lane; i < nk; i += 32) {
+    const int64_t t = sbase + i;
+    const int32_t rank = W.k_row[t];
+    if (rank < 0) continue;
+    const int64_t m = int64_t(coff) + rank;
+    W.r_w[m] = W.k_w[t];
+    W.r_alpha[m] = W.k_alpha[t];
+    W.r_ray[m] = r;
+    W.r_step[m] = W.k_step[t] & 0x7fffffff;
+    W.k_row[t] = int32_t(m);
   }
 }
 
@@ -298,31 +303,8 @@ __device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[
   }
 }
 
-// Colour rows. k_march_rowmeta (warp per ray): each colour sample gets its
-// global row m = color_off[r] + its rank in the ray and the row record;
-// k_row becomes m. k_march_k0 (thread per row): the k0 trilinear at the row's
-// position (colorvdb.cu:81-111).
-__global__ void __launch_bounds__(kMarchThreads)
-    k_march_rowmeta(int R, MarchP P, MarchW W) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kMarchWarps + warp;
-  if (r >= R) return;
-  const int nk = int(W.n_kept[r]);
-  const int64_t sbase = int64_t(r) * P.cap;
-  const int64_t coff = W.color_off[r];
-  for (int i = lane; i < nk; i += 32) {
-    const int64_t t = sbase + i;
-    const int32_t rank = W.k_row[t];
-    if (rank < 0) continue;
-    const int64_t m = coff + rank;
-    W.r_w[m] = W.k_w[t];
-    W.r_alpha[m] = W.k_alpha[t];
-    W.r_ray[m] = r;
-    W.r_step[m] = W.k_step[t] & 0x7fffffff;
-    W.k_row[t] = int32_t(m);
-  }
-}
-
+// k_march_k0 (thread per colour row): the k0 trilinear at the row's position
+// (colorvdb.cu:81-111).
 __global__ void __launch_bounds__(256)
     k_march_k0(GridView gk, MarchP P, MarchW W) {
   const int64_t M = W.totals[1];
@@ -828,13 +810,9 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     PVDB_CHECK_LAUNCH("k_march_alpha");
     k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_chain");
-    k_march_offsets<<<1, kOffThreads, 0, st>>>(m->w, R);
-    PVDB_CHECK_LAUNCH("k_march_offsets");
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
     if (k0) gk = k0->view();
-    k_march_rowmeta<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_rowmeta");
     if (k0) {
       k_march_k0<<<int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16)), 256, 0,
                    st>>>(gk, m->p, m->w);
@@ -963,6 +941,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
   const size_t R = max_rays, S = size_t(m->slots);
   int rc;
   if ((rc = dev_alloc((void**)&w.ray_sd, R * 24)) || (rc = dev_alloc((void**)&w.ray_ns, R * 4)) ||
+      (rc = dev_alloc((void**)&w.chain_status, ((R + kMarchWarps - 1) / kMarchWarps) * 8)) ||
       (rc = dev_alloc((void**)&w.T_last, R * 4)) || (rc = dev_alloc((void**)&w.n_kept, R * 4)) ||
       (rc = dev_alloc((void**)&w.n_color, R * 4)) ||
       (rc = dev_alloc((void**)&w.kept_off, R * 4)) ||
@@ -987,7 +966,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
 int pvdb_march_destroy(pvdb_march m) {
   if (!m) return PVDB_OK;
   MarchW& w = m->w;
-  void* ptrs[] = {w.ray_sd, w.ray_ns, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
+  void* ptrs[] = {w.ray_sd, w.ray_ns, w.chain_status, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
                   w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec,
                   w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed, m->mlp_xt,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,
@@ -1050,7 +1029,7 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
   if (total_rows) *total_rows = t[1];
   if (t[3] & 1u) return set_error(PVDB_ERR_STATE, "a ray had more samples than samples_cap");
   if (t[3] & 2u) return set_error(PVDB_ERR_TIMEOUT, "a tensor-core MMA wait timed out");
-  if (t[3] & 4u) return set_error(PVDB_ERR_TIMEOUT, "a radix-sort look-back wait timed out");
+  if (t[3] & 4u) return set_error(PVDB_ERR_TIMEOUT, "a ray-offset look-back wait of the march timed out");
   return PVDB_OK;
 }
 

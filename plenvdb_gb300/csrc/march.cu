@@ -537,10 +537,11 @@ __device__ void sort_segment(uint32_t* a, uint32_t len) {
 
 // Thread per placed index; cell heads sort their segment and flag the leaves
 // of the cell's corners as touched in the density grid and (touched_c !=
-// NULL) the k0 grid.
+// NULL) the k0 grid (k0_same: the k0 grid has the density topology, so the
+// density grid's corner slots serve both).
 __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
                              const uint32_t* __restrict__ cnt, uint32_t* svals, GridView gd,
-                             GridView gc, uint8_t* touched_d, uint8_t* touched_c) {
+                             GridView gc, uint8_t* touched_d, uint8_t* touched_c, int k0_same) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -549,8 +550,15 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
     sort_segment(svals + i, cnt[key]);
     int ci, cj, ck;
     cell_decode(gd.ldim, key, ci, cj, ck);
-    mark_corner_leaves(gd, ci, cj, ck, touched_d);
-    if (touched_c) mark_corner_leaves(gc, ci, cj, ck, touched_c);
+    int sl[8];
+    corner_slots(gd, ci, cj, ck, sl);
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (sl[c] >= 0) {
+        touched_d[sl[c] >> 9] = 1;
+        if (touched_c && k0_same) touched_c[sl[c] >> 9] = 1;
+      }
+    if (touched_c && !k0_same) mark_corner_leaves(gc, ci, cj, ck, touched_c);
   }
 }
 
@@ -662,7 +670,8 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const GridView kv = NQ ? k0->view() : gv;
   k_cell_heads<<<grid, 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt,
                                      const_cast<uint32_t*>(svals), gv, kv, density->d_touched,
-                                     NQ ? k0->d_touched : nullptr);
+                                     NQ ? k0->d_touched : nullptr,
+                                     NQ && k0->h_table == density->h_table ? 1 : 0);
   PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;
   if (NQ) k0->tlist_valid = false;

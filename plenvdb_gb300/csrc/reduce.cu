@@ -120,40 +120,58 @@ __global__ void k_scan_apply(const uint32_t* __restrict__ in, uint32_t* out, int
 }
 
 // Single-block scan for short inputs: 1024 threads walk the input in chunks
-// of 16384 with a running carry (one launch instead of three).
+// of 8192 with a running carry (one launch instead of three). Each chunk goes
+// through shared memory so that global loads and stores are coalesced; thread
+// t scans elements 8t .. 8t+7 of the chunk (the padded index spreads them
+// over the banks).
 constexpr int kScan1Threads = 1024;
-constexpr int kScan1Items = 16;
+constexpr int kScan1Items = 8;
 constexpr int64_t kScan1Max = 262144;  // inputs up to this length take the one-block path
+
+__device__ __forceinline__ int scan1_pad(int i) { return i + (i >> 5); }
 
 __global__ void __launch_bounds__(kScan1Threads)
     k_scan_single(const uint32_t* __restrict__ in, uint32_t* out, int64_t n_max,
                   const uint32_t* n_dev, uint32_t* total) {
+  constexpr int kChunk = kScan1Threads * kScan1Items;
+  __shared__ uint32_t buf[kChunk + kChunk / 32];
   __shared__ uint32_t carry_s;
   const int64_t n = eff_size(n_max, n_dev);
-  if (threadIdx.x == 0) carry_s = 0;
+  const int t = threadIdx.x;
+  if (t == 0) carry_s = 0;
   __syncthreads();
-  constexpr int64_t kChunk = int64_t(kScan1Threads) * kScan1Items;
   for (int64_t c0 = 0; c0 < n; c0 += kChunk) {
-    const int64_t base = c0 + int64_t(threadIdx.x) * kScan1Items;
-    uint32_t v[kScan1Items];
-    uint32_t s = 0;
 #pragma unroll
     for (int q = 0; q < kScan1Items; ++q) {
-      v[q] = base + q < n ? in[base + q] : 0u;
-      s += v[q];
+      const int e = q * kScan1Threads + t;
+      buf[scan1_pad(e)] = c0 + e < n ? in[c0 + e] : 0u;
+    }
+    __syncthreads();
+    uint32_t v[kScan1Items];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < kScan1Items; ++q) {
+      v[q] = buf[scan1_pad(t * kScan1Items + q)];
+      sum += v[q];
     }
     uint32_t tot;
-    uint32_t run = block_exclusive_scan(s, &tot) + carry_s;
+    uint32_t run = block_exclusive_scan(sum, &tot) + carry_s;
 #pragma unroll
     for (int q = 0; q < kScan1Items; ++q) {
-      if (base + q < n) out[base + q] = run;
+      buf[scan1_pad(t * kScan1Items + q)] = run;
       run += v[q];
     }
     __syncthreads();
-    if (threadIdx.x == 0) carry_s += tot;
+#pragma unroll
+    for (int q = 0; q < kScan1Items; ++q) {
+      const int e = q * kScan1Threads + t;
+      if (c0 + e < n) out[c0 + e] = buf[scan1_pad(e)];
+    }
+    __syncthreads();
+    if (t == 0) carry_s += tot;
     __syncthreads();
   }
-  if (threadIdx.x == 0 && total) *total = carry_s;
+  if (t == 0 && total) *total = carry_s;
 }
 
 int scan_exclusive_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total,

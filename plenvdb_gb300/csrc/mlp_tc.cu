@@ -339,8 +339,8 @@ constexpr uint32_t kBW1T = kBW1 + 128 * 128 * 2;     // W1T  [128 k][128 n]
 constexpr uint32_t kBW0T = kBW1T + 128 * 128 * 2;    // W0kT [16 q][128 n]
 constexpr uint32_t kBW2T = kBW0T + 16 * 128 * 2;     // W2T  [128 n][16 c]
 constexpr uint32_t kBB1 = kBW2T + 128 * 16 * 2;      // b1 f32[128]
-constexpr uint32_t kBBar = kBB1 + 128 * 4;          // mbarriers: MMA, X0, X1
-constexpr uint32_t kBTmem = kBBar + 24;
+constexpr uint32_t kBBar = kBB1 + 128 * 4;          // mbarriers: MMA, X0, X1, layer 0
+constexpr uint32_t kBTmem = kBBar + 32;
 constexpr uint32_t kBFlag = kBTmem + 4;
 constexpr uint32_t kSmBwdBytes = kBFlag + 12;
 static_assert(kSmBwdBytes <= 232448, "backward tile exceeds 227 KB of shared memory");
@@ -413,11 +413,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 136, 144)) = make_uint4(0u, 0u, 0u, 0u);
   }
   uint64_t* xbar = bar + 1;  // X tile barriers, one per buffer
+  uint64_t* lbar = bar + 3;  // layer-0 MMA of a tile, issued during the previous tile
   if (tid == 0) {
     *flag = 0;
     tc::mbar_init(bar, 1);
     tc::mbar_init(xbar, 1);
     tc::mbar_init(xbar + 1, 1);
+    tc::mbar_init(lbar, 1);
     x_fetch(sm + kBX, xt, blockIdx.x, xbar);
   }
   if (warp == 0) {
@@ -438,8 +440,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int row = 32 * q4 + lane;
   const uint32_t t_lane = tmem + (uint32_t(32 * q4) << 16);
   float db2[3] = {0.f, 0.f, 0.f};
-  uint32_t phase = 0, xph[2] = {0u, 0u};
+  uint32_t phase = 0, lph = 0, xph[2] = {0u, 0u};
   bool ok = true, first = true;
+  // layer 0 of tile t into TMEM columns kTA (free once the previous tile's
+  // dZ1 has been read); issued by thread 0 after its X tile has landed
+  auto issue_l0 = [&](int buf) {
+    if (!tc::mbar_wait(xbar + buf, xph[buf], kWaitIters)) {
+      atomicOr(flag, 1u);
+      if (err) atomicOr(err, 2u);
+      return;
+    }
+    tc::fence_after();
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX + uint32_t(buf) * kXTile + 256 * s, 128, 768),
+                   tc::make_desc(sb + kBW0f + 256 * s, 128, 768), id_r128, s > 0);
+    tc::mma_commit(lbar);
+  };
   int it = 0;
   for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
     const int64_t row0 = t * 128;
@@ -455,23 +472,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         gv[c] = __ldg(grad_rgb + mrow * 3 + c);
       }
     }
+    const bool has_next = t + gridDim.x < ntiles;
     // the next tile's X travels while this tile computes (its buffer was last
     // read by the previous tile's dW0 MMA, complete)
-    if (tid == 0 && t + gridDim.x < ntiles)
+    if (tid == 0 && has_next)
       x_fetch(sm + kBX + uint32_t(xb ^ 1) * kXTile, xt, t + gridDim.x, xbar + (xb ^ 1));
-    ok = wait_or_flag(xbar + xb, xph[xb], flag, err);
-    if (!ok) break;
-    xph[xb] ^= 1u;
-    if (tid == 0) {
-      tc::fence_after();
-#pragma unroll
-      for (int s = 0; s < 3; ++s)
-        tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBXt + 256 * s, 128, 768),
-                     tc::make_desc(sb + kBW0f + 256 * s, 128, 768), id_r128, s > 0);
-      tc::mma_commit(bar);
+    if (it == 0) {
+      if (tid == 0) issue_l0(xb);
+      xph[xb] ^= 1u;
     }
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
+    ok = wait_or_flag(lbar, lph, flag, err);
+    lph ^= 1u;
     if (!ok) break;
     tc::fence_after();
     // ---- H0 = relu(Z0)
@@ -562,7 +573,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc::mma_bf16(tmem + kTW1, tc::make_desc(sb + kBdZ1 + 4096 * s, 2048, 128),
                      tc::make_desc(sb + kBH0 + 4608 * s, 2304, 128), id_w1, (!first || s > 0));
       tc::mma_commit(bar);
+      // the next tile's layer 0 runs behind these on the tensor pipe
+      if (has_next) issue_l0(xb ^ 1);
     }
+    if (has_next) xph[xb ^ 1] ^= 1u;
     ok = wait_or_flag(bar, phase, flag, err);
     phase ^= 1;
     if (!ok) break;
@@ -617,6 +631,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // a wait gave up: one more bounded wait for the MMAs and X copies in
     // flight before their TMEM and shared memory are released
     tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
+    tc::mbar_wait(lbar, lph, kWaitIters);
     tc::mbar_wait(xbar, xph[0], kWaitIters);
     tc::mbar_wait(xbar + 1, xph[1], kWaitIters);
     __syncthreads();

@@ -330,9 +330,7 @@ __global__ void __launch_bounds__(256)
 // chunks.
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_bwd(GridView gd, int R, MarchP P, MarchW W, const float* __restrict__ grad_w,
-                const float* __restrict__ grad_last, const float* __restrict__ grad_k0, int C,
-                uint32_t* keys) {
-  const int nq = (C + 3) >> 2;
+                const float* __restrict__ grad_last, uint32_t* keys) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -378,19 +376,8 @@ __global__ void __launch_bounds__(kMarchThreads)
       (void)raw2alpha(sigma, P.shift, P.interval, e);
       const float gs = raw2alpha_grad(e, P.interval, ga);
       const int64_t s = kb + i;
-      float4* rec = W.b_rec + s * (1 + nq);
-      rec[0] = make_float4(idx[0], idx[1], idx[2], gs);
-      for (int b = 0; b < nq; ++b) {
-        float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (row >= 0 && grad_k0) {
-          const float* gr = grad_k0 + int64_t(row) * C + 4 * b;
-          g4.x = gr[0];
-          g4.y = 4 * b + 1 < C ? gr[1] : 0.f;
-          g4.z = 4 * b + 2 < C ? gr[2] : 0.f;
-          g4.w = 4 * b + 3 < C ? gr[3] : 0.f;
-        }
-        rec[1 + b] = g4;
-      }
+      W.b_rec[s] = make_float4(idx[0], idx[1], idx[2], gs);
+      W.b_row[s] = row;
       keys[s] = cell_key(gd.ldim, ifloor(idx[0]), ifloor(idx[1]), ifloor(idx[2]));
     }
   }
@@ -591,6 +578,7 @@ __global__ void __launch_bounds__(256)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                    const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
                    const uint32_t* __restrict__ svals, const float4* __restrict__ rec,
+                   const int32_t* __restrict__ brow, const float* __restrict__ gk0, int gk0_vec,
                    float* grad_d, float* grad_c, int C) {
   const int64_t nv = int64_t(*count) * kLeafVox;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv;
@@ -620,16 +608,26 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
       for (uint32_t j = h; j < h + len; ++j) {
-        const float4* r = rec + int64_t(svals[j]) * (1 + NQ);
-        const float4 p = r[0];
+        const uint32_t smp = svals[j];
+        const float4 p = rec[smp];
         const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
                     w = p.z - float(ifloor(p.z));
         if (grad_d && p.w != 0.f) pd = __fadd_rn(pd, density_corner_term(p.w, u, v, w, c));
-        if (NQ && grad_c) {
+        const int32_t row = NQ && grad_c ? brow[smp] : -1;
+        if (row >= 0) {  // a sample without a colour row adds nothing to k0
           const float sce = corner_scale(u, v, w, c);
+          const float* gr = gk0 + int64_t(row) * C;
 #pragma unroll
           for (int b = 0; b < NQ; ++b) {
-            const float4 q = r[1 + b];
+            float4 q;
+            if (gk0_vec) {
+              q = __ldg(reinterpret_cast<const float4*>(gr) + b);
+            } else {
+              q.x = __ldg(gr + 4 * b);
+              q.y = 4 * b + 1 < C ? __ldg(gr + 4 * b + 1) : 0.f;
+              q.z = 4 * b + 2 < C ? __ldg(gr + 4 * b + 2) : 0.f;
+              q.w = 4 * b + 3 < C ? __ldg(gr + 4 * b + 3) : 0.f;
+            }
             pk[b].x = __fadd_rn(pk[b].x, __fmul_rn(q.x, sce));
             pk[b].y = __fadd_rn(pk[b].y, __fmul_rn(q.y, sce));
             pk[b].z = __fadd_rn(pk[b].z, __fmul_rn(q.z, sce));
@@ -664,30 +662,25 @@ __global__ void __launch_bounds__(256)
 
 template <int NQ>
 static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0,
-                              const uint32_t* skeys, const uint32_t* svals, cudaStream_t st) {
+                              const float* grad_k0, cudaStream_t st) {
   const int grid = stride_grid();
   const GridView gv = density->view();
   const GridView kv = NQ ? k0->view() : gv;
-  k_cell_heads<<<grid, 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt,
-                                     const_cast<uint32_t*>(svals), gv, kv, density->d_touched,
-                                     NQ ? k0->d_touched : nullptr,
-                                     NQ && k0->h_table == density->h_table ? 1 : 0);
-  PVDB_CHECK_LAUNCH("k_cell_heads");
-  density->tlist_valid = false;
-  if (NQ) k0->tlist_valid = false;
   int rc = touched_list(density, st);
   if (rc) return rc;
   const bool same = NQ && k0->h_table == density->h_table;
   const int C = NQ ? k0->C : 0;
+  const int vec = NQ && C % 4 == 0 && (reinterpret_cast<uintptr_t>(grad_k0) & 15u) == 0;
+  const uint32_t* svals = m->red.vals[0];
   k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_cnt,
-                                           m->cell_off, svals, m->w.b_rec, density->d_grad,
-                                           same ? k0->d_grad : nullptr, C);
+                                           m->cell_off, svals, m->w.b_rec, m->w.b_row, grad_k0,
+                                           vec, density->d_grad, same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
     k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
-                                             m->cell_off, svals, m->w.b_rec, nullptr, k0->d_grad,
-                                             C);
+                                             m->cell_off, svals, m->w.b_rec, m->w.b_row, grad_k0,
+                                             vec, nullptr, k0->d_grad, C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -833,10 +826,15 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   return PVDB_OK;
 }
 
-int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_last,
-                        const float* grad_k0, cudaStream_t st) {
+// Backward, first part: the density-path gradients of every kept sample
+// (k_march_bwd) and the grouping of the kept samples by cell, which need only
+// the gradients w.r.t. the weights and alphainv_last — so it can run while
+// the rgbnet backward produces the k0-row gradients. with_k0: the k0 grid gets
+// gradients (its touched leaves are flagged too).
+int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
+                        bool with_k0, cudaStream_t st) {
   pvdb_grid_s* density = m->density;
-  pvdb_grid_s* k0 = m->k0;
+  pvdb_grid_s* k0 = with_k0 ? m->k0 : nullptr;
   const int R = m->n_rays;
   if (R == 0) return PVDB_OK;
   const int64_t nmax = m->slots;
@@ -859,15 +857,12 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
     PVDB_CHECK_CUDA(cudaMemsetAsync(m->leaf_cnt, 0, size_t(nleaves) * 4, st));
     m->cell_cap = size_t(ncells);
   }
-  const bool use_k0 = k0 && grad_k0;
-  const int C = use_k0 ? k0->C : 0;
-  PVDB_REQUIRE(C <= 16, "the march backward takes at most 16 k0 channels");
-  const int nq = (C + 3) / 4;
-  if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * (1 + nq) * 16)))
+  if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * 16)) ||
+      (rc = dev_reserve((void**)&m->w.b_row, &m->b_row_cap, size_t(nmax) * 4)))
     return rc;
   const int nb = ceil_div(R, kMarchWarps);
   k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
-                                            use_k0 ? grad_k0 : nullptr, C, m->red.keys[0]);
+                                            m->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
   // group the kept samples by cell (stable order, see above)
@@ -886,19 +881,54 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   PVDB_CHECK_LAUNCH("k_cell_offsets");
   k_cell_place<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
   PVDB_CHECK_LAUNCH("k_cell_place");
+  const GridView gv = density->view();
+  const GridView kv = k0 ? k0->view() : gv;
+  k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals, gv, kv,
+                                              density->d_touched, k0 ? k0->d_touched : nullptr,
+                                              k0 && k0->h_table == density->h_table ? 1 : 0);
+  PVDB_CHECK_LAUNCH("k_cell_heads");
+  density->tlist_valid = false;
+  if (k0) k0->tlist_valid = false;
   if (m->prof) prof_mark(st, 7);
-  switch (nq) {
-    case 0: rc = cell_reduce_launch<0>(m, density, k0, skeys, svals, st); break;
-    case 1: rc = cell_reduce_launch<1>(m, density, k0, skeys, svals, st); break;
-    case 2: rc = cell_reduce_launch<2>(m, density, k0, skeys, svals, st); break;
-    case 3: rc = cell_reduce_launch<3>(m, density, k0, skeys, svals, st); break;
-    default: rc = cell_reduce_launch<4>(m, density, k0, skeys, svals, st); break;
+  m->bwd_keys_ready = true;
+  m->bwd_with_k0 = with_k0;
+  return PVDB_OK;
+}
+
+// Backward, second part: the per-voxel sums into the density and k0 gradients
+// (grad_k0 [M, C]: the k0-row gradients; ignored when the first part ran
+// without k0), then the cell counts are reset.
+int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st) {
+  if (m->n_rays == 0) return PVDB_OK;
+  if (!m->bwd_keys_ready) return set_error(PVDB_ERR_STATE, "march backward: keys not grouped");
+  m->bwd_keys_ready = false;
+  pvdb_grid_s* density = m->density;
+  pvdb_grid_s* k0 = m->k0;
+  const int C = m->bwd_with_k0 && grad_k0 ? k0->C : 0;
+  PVDB_REQUIRE(C <= 16, "the march backward takes at most 16 k0 channels");
+  int rc;
+  switch ((C + 3) / 4) {
+    case 0: rc = cell_reduce_launch<0>(m, density, k0, grad_k0, st); break;
+    case 1: rc = cell_reduce_launch<1>(m, density, k0, grad_k0, st); break;
+    case 2: rc = cell_reduce_launch<2>(m, density, k0, grad_k0, st); break;
+    case 3: rc = cell_reduce_launch<3>(m, density, k0, grad_k0, st); break;
+    default: rc = cell_reduce_launch<4>(m, density, k0, grad_k0, st); break;
   }
   if (rc) return rc;
-  k_cell_clear<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
+  const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(stride_grid())));
+  k_cell_clear<<<sgrid, 256, 0, st>>>(m->red.keys[0], m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
   PVDB_CHECK_LAUNCH("k_cell_clear");
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
+}
+
+int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_last,
+                        const float* grad_k0, cudaStream_t st) {
+  const bool use_k0 = m->k0 && grad_k0;
+  if (use_k0) PVDB_REQUIRE(m->k0->C <= 16, "the march backward takes at most 16 k0 channels");
+  int rc = march_backward_keys(m, grad_w, grad_last, use_k0, st);
+  if (rc) return rc;
+  return march_backward_reduce(m, grad_k0, st);
 }
 
 int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
@@ -976,7 +1006,7 @@ int pvdb_march_destroy(pvdb_march m) {
   if (!m) return PVDB_OK;
   MarchW& w = m->w;
   void* ptrs[] = {w.ray_sd, w.ray_ns, w.chain_status, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
-                  w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec,
+                  w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec, w.b_row,
                   w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed, m->mlp_xt,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,
                   m->t_loss_part, m->t_rgb_marched};

@@ -45,10 +45,11 @@ struct MarchW {
   float* r_alpha;
   int32_t* r_ray;
   int32_t* r_step;
-  // per kept sample (global kept index), backward: record of 1 + nq float4,
-  // (x, y, z, dL/dsigma) then the k0 gradient of the sample's colour row
-  // (zeros for a sample without one), nq = ceil(C/4)
+  // per kept sample (global kept index), backward: (x, y, z, dL/dsigma) and
+  // the sample's colour row (-1: none), whose k0 gradient is read from the
+  // rgbnet backward's output
   float4* b_rec;
+  int32_t* b_row;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 ray-offset look-back
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
@@ -73,6 +74,9 @@ struct pvdb_march_s {
   uint32_t* leaf_off = nullptr;
   size_t cell_cap = 0;  // cells
   size_t b_rec_cap = 0;         // bytes of w.b_rec
+  size_t b_row_cap = 0;         // bytes of w.b_row
+  bool bwd_keys_ready = false;  // march_backward_keys ran since the last reduce
+  bool bwd_with_k0 = false;
   uint32_t* scan_partial = nullptr;
   size_t scan_partial_cap = 0;
   // state of the last forward

@@ -29,8 +29,9 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st);
-int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_last,
-                        const float* grad_k0, cudaStream_t st);
+int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
+                        bool with_k0, cudaStream_t st);
+int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st);
 int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
                            cudaStream_t st);
 float opt_next_stepsz(pvdb_opt_s* o);
@@ -224,11 +225,27 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, t.loss);
   PVDB_CHECK_LAUNCH("k_loss_sum");
   if (t.prof) prof_mark(st, 4);
+  // The march backward's density path and the grouping of the kept samples by
+  // cell need only the weight / alphainv_last gradients: they run beside the
+  // rgbnet backward, whose k0-row gradients the per-voxel sums then read.
+  // (The stage profiler keeps the stages in sequence.)
+  const bool par = !t.prof;
+  if (par && (rc = fork_side(m, st, 1))) return rc;
+  if (par) {
+    rc = march_backward_keys(m, m->t_grad_w, m->t_grad_last, true, m->side[0]);
+    if (rc) return rc;
+  }
   rc = mlp_backward_impl(m, a, m->w.r_k0, m->t_rgb, m->t_grad_rgb, m->t_grad_k0, net->grads,
                          cfg->precision, st, true);
   if (rc) return rc;
   if (t.prof) prof_mark(st, 5);
-  rc = march_backward_impl(m, m->t_grad_w, m->t_grad_last, m->t_grad_k0, st);
+  if (par) {
+    if ((rc = join_side(m, st, 1))) return rc;
+  } else {
+    rc = march_backward_keys(m, m->t_grad_w, m->t_grad_last, true, st);
+    if (rc) return rc;
+  }
+  rc = march_backward_reduce(m, m->t_grad_k0, st);
   if (rc) return rc;
   // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
   // TV of the two grids side by side (each grid's own touched list), then the

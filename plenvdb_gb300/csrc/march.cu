@@ -27,6 +27,7 @@
 
 #include "march.cuh"
 #include "reduce.cuh"
+#include "tc.cuh"
 
 namespace pvdb {
 
@@ -317,6 +318,49 @@ __global__ void __launch_bounds__(256)
     ray_point(rs, P.stepdist, W.r_step[m], p);
     world_to_index(p, P.mn, P.ext, P.wsm1, idx);
     k0_trilinear(gk, idx, W.r_k0 + m * gk.C);
+  }
+}
+
+// BF16 tensor-core path of the train step: the k0 trilinear of each colour row
+// goes straight into the row of its X tile ([k0 | PE | 1 | 0], BF16), so the
+// FP32 k0 rows are never written. pe: per-ray PE (pe_stride floats per ray).
+// The padding rows of the last tile are zero.
+__global__ void __launch_bounds__(256)
+    k_march_k0_x(GridView gk, MarchP P, MarchW W, const float* __restrict__ pe, int pe_stride,
+                 int dpe, uint8_t* xt) {
+  const int64_t M = W.totals[1];
+  const int64_t Mpad = (M + 127) / 128 * 128;
+  const int C = gk.C, din = C + dpe;
+  for (int64_t m = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; m < Mpad;
+       m += int64_t(gridDim.x) * blockDim.x) {
+    float k0v[16];
+    int r = 0;
+    if (m < M) {
+      r = W.r_ray[m];
+      RaySetup rs;
+      load_setup(W, r, rs);
+      float p[3], idx[3];
+      ray_point(rs, P.stepdist, W.r_step[m], p);
+      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+      k0_trilinear(gk, idx, k0v);
+    }
+    uint8_t* tile = xt + (m >> 7) * int64_t(kRgbXTile);
+    const int row = int(m & 127);
+#pragma unroll
+    for (int cb = 0; cb < kRgbXK / 8; ++cb) {
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int q = 8 * cb + e;
+        v[e] = m >= M ? 0.f
+               : q < C ? k0v[q < 16 ? q : 15]
+               : q < din ? __ldg(pe + int64_t(r) * pe_stride + (q - C))
+               : q == din ? 1.f : 0.f;
+      }
+      const uint4 pk = make_uint4(tc::pack_bf16(v[0], v[1]), tc::pack_bf16(v[2], v[3]),
+                                  tc::pack_bf16(v[4], v[5]), tc::pack_bf16(v[6], v[7]));
+      *reinterpret_cast<uint4*>(tile + tc::kmaj(row, 8 * cb, kRgbXK)) = pk;
+    }
   }
 }
 
@@ -781,7 +825,7 @@ static void fill_params(const pvdb_march_params* in, const pvdb_grid_s* gd, cons
 
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
-                       const int32_t* mshape, cudaStream_t st) {
+                       const int32_t* mshape, cudaStream_t st, bool skip_k0) {
   if (k0) {
     for (int a = 0; a < 3; ++a) {
       PVDB_REQUIRE(k0->reso[a] == density->reso[a], "k0 and density grids need the same resolution");
@@ -815,7 +859,7 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
     if (k0) gk = k0->view();
-    if (k0) {
+    if (k0 && !skip_k0) {
       k_march_k0<<<int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16)), 256, 0,
                    st>>>(gk, m->p, m->w);
       PVDB_CHECK_LAUNCH("k_march_k0");
@@ -831,6 +875,20 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
 // the gradients w.r.t. the weights and alphainv_last — so it can run while
 // the rgbnet backward produces the k0-row gradients. with_k0: the k0 grid gets
 // gradients (its touched leaves are flagged too).
+// The fused k0 + X-tile pass (after a forward run with skip_k0); xt must hold
+// ceil(slots / 128) tiles.
+int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t* xt,
+               cudaStream_t st) {
+  if (m->n_rays == 0 || !m->k0) return PVDB_OK;
+  PVDB_REQUIRE(m->k0->C <= 16 && m->k0->C + dpe + 1 <= kRgbXK,
+               "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
+  const int grid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16));
+  k_march_k0_x<<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt);
+  PVDB_CHECK_LAUNCH("k_march_k0_x");
+  if (m->prof) prof_mark(st, 2);
+  return PVDB_OK;
+}
+
 int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
                         bool with_k0, cudaStream_t st) {
   pvdb_grid_s* density = m->density;
@@ -1037,7 +1095,7 @@ int pvdb_march_forward(pvdb_march m, pvdb_grid density, pvdb_grid k0, const floa
   PVDB_REQUIRE(!mask || mask_shape, "mask needs mask_shape");
   PVDB_REQUIRE(p->stepdist > 0.f, "stepdist must be positive");
   return march_forward_impl(m, density, k0, rays_o, rays_d, n_rays, p, mask, mask_shape,
-                            as_stream(s));
+                            as_stream(s), false);
 }
 
 int pvdb_march_views(pvdb_march m, pvdb_march_views_t* v) {

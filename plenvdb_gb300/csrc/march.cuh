@@ -53,7 +53,7 @@ struct MarchW {
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 ray-offset look-back
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
-  // [6] k_march_chain tile counter
+  // [6] k_march_chain tile counter, [7] train-step loss block counter
   uint32_t* totals;
 };
 

@@ -455,10 +455,22 @@ int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R,
   return PVDB_OK;
 }
 
-// prepared: mlp_prepare already ran for these rays and weights.
+// The per-ray PE that mlp_prepare writes (stride floats per ray), and the X
+// tiles of the tensor-core path reserved for the workspace's rows.
+const float* mlp_pe_buffer(pvdb_march_s* m, int* stride) {
+  *stride = kMaxPe;
+  return m->hpe ? m->hpe + size_t(m->max_rays) * kW : nullptr;
+}
+int mlp_reserve_x(pvdb_march_s* m) {
+  const int64_t ntiles = (m->slots + 127) / 128;
+  return dev_reserve(&m->mlp_xt, &m->mlp_xt_cap, size_t(std::max<int64_t>(ntiles, 1)) * kRgbXTile);
+}
+
+// prepared: mlp_prepare already ran for these rays and weights; x_ready: the
+// BF16 X tiles are already built (march_k0_x).
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
                      const float* viewdirs, float* rgb, int precision, cudaStream_t st,
-                     bool prepared) {
+                     bool prepared, bool x_ready) {
   const int R = m->n_rays;
   if (R <= 0) return PVDB_OK;
   int rc = mlp_reserve(m, a.din);
@@ -473,7 +485,7 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows,
                                m->w.r_ray, pe, kMaxPe, m->w.totals, m->slots, rgb, 0,
                                &m->mlp_packed, &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap,
-                               m->w.totals + 3, st, prepared ? 1 : 0, 0);
+                               m->w.totals + 3, st, prepared ? 1 : 0, x_ready ? 1 : 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
   k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
       a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
@@ -575,7 +587,7 @@ int pvdb_mlp_forward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   MlpArgs a;
   int rc = mlp_args_from(w, a);
   if (rc) return rc;
-  return mlp_forward_impl(m, a, k0 ? k0 : m->w.r_k0, viewdirs, rgb, precision, as_stream(s),
+  return mlp_forward_impl(m, a, k0 ? k0 : m->w.r_k0, viewdirs, rgb, precision, as_stream(s), false,
                           false);
 }
 

@@ -28,7 +28,7 @@ namespace {
 
 constexpr int kW = 128;
 constexpr int kTcThreads = 256;
-constexpr int kXK = 48;  // input columns of a row: k0 | PE | 1 | 0
+constexpr int kXK = kRgbXK;  // input columns of a row: k0 | PE | 1 | 0
 // packed weight blob (bytes, canonical K-major BF16 tiles)
 constexpr uint32_t kOffW0 = 0;                             // W0f  [128 n][48 q]
 constexpr uint32_t kOffW1 = kOffW0 + 128 * kXK * 2;        // W1   [128 n][128 k]   12288
@@ -39,7 +39,7 @@ constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16 q][128 n]
 constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T  [128 n][16 c]    86016
 constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 90112
 // shared-memory layout of the forward kernel
-constexpr uint32_t kXTile = 128 * kXK * 2;             // 12288 B: one X tile
+constexpr uint32_t kXTile = kRgbXTile;                // 12288 B: one X tile
 constexpr uint32_t kSmX = kPackFwdBytes;              // two X tiles [128 x 48] bf16
 constexpr uint32_t kSmH = kSmX + 2 * kXTile;          // H tile [128 x 128] bf16
 constexpr uint32_t kSmB1 = kSmH + 128 * 128 * 2;      // b1 f32[128]

@@ -318,6 +318,10 @@ int radix_sort_words(int64_t n_max, int key_bits);
 int scratch_reserve(ReduceScratch& rs, int64_t n);
 void free_scratch(ReduceScratch& rs);
 int num_sms();
+// rgbnet X tiles of the tensor-core path: per 128 rows one [128][48] BF16 tile
+// in the canonical no-swizzle K-major layout, a row = [k0 | PE | 1 | 0].
+constexpr int kRgbXK = 48;
+constexpr uint32_t kRgbXTile = 128 * kRgbXK * 2;
 
 // Ensure the reduce scratch of g can hold n contributions.
 int reduce_reserve(pvdb_grid_s* g, int64_t n);

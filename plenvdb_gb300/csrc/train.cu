@@ -22,18 +22,20 @@ int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R,
                 cudaStream_t st);
 int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
                      const float* viewdirs, float* rgb, int precision, cudaStream_t st,
-                     bool prepared);
+                     bool prepared, bool x_ready);
 int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, const float* rgb,
                       const float* grad_rgb, float* grad_k0, float* grad_flat, int precision,
                       cudaStream_t st, bool prepared);
 int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, const float* ro,
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
-                       const int32_t* mshape, cudaStream_t st);
+                       const int32_t* mshape, cudaStream_t st, bool skip_k0);
+int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t* xt,
+               cudaStream_t st);
+const float* mlp_pe_buffer(pvdb_march_s* m, int* stride);
+int mlp_reserve_x(pvdb_march_s* m);
 int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
                         bool with_k0, cudaStream_t st);
 int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st);
-int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
-                           cudaStream_t st);
 float opt_next_stepsz(pvdb_opt_s* o);
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
                cudaStream_t st);
@@ -45,60 +47,94 @@ struct LossW {
   float main, ent, rgbper, bg;
 };
 
-// Per ray: losses and their gradients w.r.t. rgb_marched (folded into the
-// per-row colour gradient), alphainv_last, and the colour weights.
+// Per ray (warp per ray): the composite rgb_marched = sum_rows w*rgb + T*bg
+// (the same arithmetic as k_composite_fwd), the losses and their gradients
+// w.r.t. rgb_marched (folded into the per-row colour gradient), alphainv_last
+// and the colour weights. The last block to finish sums the per-ray loss
+// partials in a fixed order (a counter in totals[7] picks it and is reset).
 __global__ void __launch_bounds__(256)
-    k_loss(MarchW W, const float* __restrict__ rgb, const float* __restrict__ rgbm,
+    k_loss(MarchW W, const float* __restrict__ rgb, float* rgbm_out,
            const float* __restrict__ target, int R, LossW L, float* grad_rgb, float* grad_w,
-           float* grad_last, float* loss_part) {
+           float* grad_last, float* loss_part, float* loss) {
+  __shared__ float red[256];
+  __shared__ bool last_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * 8 + warp;
-  if (r >= R) return;
-  const float t0 = target[r * 3], t1 = target[r * 3 + 1], t2 = target[r * 3 + 2];
-  const float e0 = rgbm[r * 3] - t0, e1 = rgbm[r * 3 + 1] - t1, e2 = rgbm[r * 3 + 2] - t2;
-  // d/d rgb_marched of weight_main * mean((rgbm-target)^2) over R*3 entries
-  const float cm = L.main * 2.f / (3.f * float(R));
-  const float g0 = cm * e0, g1 = cm * e1, g2 = cm * e2;
-  const int n = int(W.n_color[r]);
-  const int64_t off = W.color_off[r];
-  const float cp = L.rgbper * 2.f / float(R);
-  float per = 0.f;
-  for (int j = lane; j < n; j += 32) {
-    const int64_t m = off + j;
-    const float w = W.r_w[m];
-    const float y0 = rgb[m * 3], y1 = rgb[m * 3 + 1], y2 = rgb[m * 3 + 2];
-    const float d0 = y0 - t0, d1 = y1 - t1, d2 = y2 - t2;
-    per += (d0 * d0 + d1 * d1 + d2 * d2) * w;
-    grad_rgb[m * 3] = w * g0 + cp * w * d0;
-    grad_rgb[m * 3 + 1] = w * g1 + cp * w * d1;
-    grad_rgb[m * 3 + 2] = w * g2 + cp * w * d2;
-    grad_w[m] = g0 * y0 + g1 * y1 + g2 * y2;
-  }
+  if (r < R) {
+    const int n = int(W.n_color[r]);
+    const int64_t off = W.color_off[r];
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      const int64_t m = off + j;
+      const float w = W.r_w[m];
+      s0 = __fadd_rn(s0, __fmul_rn(w, rgb[m * 3]));
+      s1 = __fadd_rn(s1, __fmul_rn(w, rgb[m * 3 + 1]));
+      s2 = __fadd_rn(s2, __fmul_rn(w, rgb[m * 3 + 2]));
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) per += __shfl_xor_sync(0xffffffffu, per, o);
-  if (lane == 0) {
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 = __fadd_rn(s0, __shfl_xor_sync(0xffffffffu, s0, o));
+      s1 = __fadd_rn(s1, __shfl_xor_sync(0xffffffffu, s1, o));
+      s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+    }
     const float T = W.T_last[r];
-    const float p = fminf(fmaxf(T, 1e-6f), 1.f - 1e-6f);
-    const float ent = -(p * logf(p) + (1.f - p) * logf(1.f - p));
-    const float dent = (T > 1e-6f && T < 1.f - 1e-6f) ? logf((1.f - p) / p) : 0.f;
-    grad_last[r] = L.bg * (g0 + g1 + g2) + L.ent / float(R) * dent;
-    loss_part[r] = L.main * (e0 * e0 + e1 * e1 + e2 * e2) / (3.f * float(R)) +
-                   L.ent * ent / float(R) + L.rgbper * per / float(R);
+    const float tb = __fmul_rn(T, L.bg);
+    const float m0 = __fadd_rn(__shfl_sync(0xffffffffu, s0, 0), tb);
+    const float m1 = __fadd_rn(__shfl_sync(0xffffffffu, s1, 0), tb);
+    const float m2 = __fadd_rn(__shfl_sync(0xffffffffu, s2, 0), tb);
+    if (lane == 0) {
+      rgbm_out[r * 3] = m0;
+      rgbm_out[r * 3 + 1] = m1;
+      rgbm_out[r * 3 + 2] = m2;
+    }
+    const float t0 = target[r * 3], t1 = target[r * 3 + 1], t2 = target[r * 3 + 2];
+    const float e0 = m0 - t0, e1 = m1 - t1, e2 = m2 - t2;
+    // d/d rgb_marched of weight_main * mean((rgbm-target)^2) over R*3 entries
+    const float cm = L.main * 2.f / (3.f * float(R));
+    const float g0 = cm * e0, g1 = cm * e1, g2 = cm * e2;
+    const float cp = L.rgbper * 2.f / float(R);
+    float per = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      const int64_t m = off + j;
+      const float w = W.r_w[m];
+      const float y0 = rgb[m * 3], y1 = rgb[m * 3 + 1], y2 = rgb[m * 3 + 2];
+      const float d0 = y0 - t0, d1 = y1 - t1, d2 = y2 - t2;
+      per += (d0 * d0 + d1 * d1 + d2 * d2) * w;
+      grad_rgb[m * 3] = w * g0 + cp * w * d0;
+      grad_rgb[m * 3 + 1] = w * g1 + cp * w * d1;
+      grad_rgb[m * 3 + 2] = w * g2 + cp * w * d2;
+      grad_w[m] = g0 * y0 + g1 * y1 + g2 * y2;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) per += __shfl_xor_sync(0xffffffffu, per, o);
+    if (lane == 0) {
+      const float p = fminf(fmaxf(T, 1e-6f), 1.f - 1e-6f);
+      const float ent = -(p * logf(p) + (1.f - p) * logf(1.f - p));
+      const float dent = (T > 1e-6f && T < 1.f - 1e-6f) ? logf((1.f - p) / p) : 0.f;
+      grad_last[r] = L.bg * (g0 + g1 + g2) + L.ent / float(R) * dent;
+      loss_part[r] = L.main * (e0 * e0 + e1 * e1 + e2 * e2) / (3.f * float(R)) +
+                     L.ent * ent / float(R) + L.rgbper * per / float(R);
+    }
   }
-}
-
-// Fixed-order sum of the per-ray loss partials (one block).
-__global__ void k_loss_sum(const float* __restrict__ part, int R, float* out) {
-  __shared__ float s[1024];
+  // the last block sums the partials
+  __threadfence();  // this block's partials are visible device-wide before its ticket
+  __syncthreads();
+  if (threadIdx.x == 0) last_s = atomicAdd(W.totals + 7, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last_s) return;
+  __threadfence();
   float acc = 0.f;
-  for (int i = threadIdx.x; i < R; i += blockDim.x) acc += part[i];
-  s[threadIdx.x] = acc;
+  for (int i = threadIdx.x; i < R; i += blockDim.x) acc += ((volatile float*)loss_part)[i];
+  red[threadIdx.x] = acc;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[0] = s[0];
+  if (threadIdx.x == 0) {
+    loss[0] = red[0];
+    W.totals[7] = 0u;
+  }
 }
 
 static int train_reserve(pvdb_march_s* m, int C) {
@@ -209,21 +245,28 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   // rgbnet inputs (PE, packed weights) beside the march
   if ((rc = fork_side(m, st, 1))) return rc;
   if ((rc = mlp_prepare(m, a, t.vd, n_rays, cfg->precision, m->side[0]))) return rc;
-  rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st);
+  // BF16: the k0 trilinear writes the rgbnet's X tiles directly (after the
+  // join: the tiles hold the PE too)
+  const bool fused_x = cfg->precision == 1;
+  if (fused_x && (rc = mlp_reserve_x(m))) return rc;
+  rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st,
+                          fused_x);
   if (rc) return rc;
   if ((rc = join_side(m, st, 1))) return rc;
-  rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st, true);
+  if (fused_x) {
+    int pe_stride = 0;
+    const float* pe = mlp_pe_buffer(m, &pe_stride);
+    rc = march_k0_x(m, pe, pe_stride, a.dpe, static_cast<uint8_t*>(m->mlp_xt), st);
+    if (rc) return rc;
+  }
+  rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st, true, fused_x);
   if (rc) return rc;
   if (t.prof) prof_mark(st, 3);
-  rc = composite_forward_impl(m, m->t_rgb, cfg->march.bg, m->t_rgb_marched, n_rays, st);
-  if (rc) return rc;
   LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
   k_loss<<<ceil_div(n_rays, 8), 256, 0, st>>>(m->w, m->t_rgb, m->t_rgb_marched, t.tgt, n_rays, L,
                                               m->t_grad_rgb, m->t_grad_w, m->t_grad_last,
-                                              m->t_loss_part);
+                                              m->t_loss_part, t.loss);
   PVDB_CHECK_LAUNCH("k_loss");
-  k_loss_sum<<<1, 1024, 0, st>>>(m->t_loss_part, n_rays, t.loss);
-  PVDB_CHECK_LAUNCH("k_loss_sum");
   if (t.prof) prof_mark(st, 4);
   // The march backward's density path and the grouping of the kept samples by
   // cell need only the weight / alphainv_last gradients: they run beside the

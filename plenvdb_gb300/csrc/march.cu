@@ -956,7 +956,20 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
 // Backward, second part: the per-voxel sums into the density and k0 gradients
 // (grad_k0 [M, C]: the k0-row gradients; ignored when the first part ran
 // without k0), then the cell counts are reset.
-int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st) {
+// Resets the counts of the cells and leaves that got samples (needed before
+// the next backward's grouping; a caller may run it on another stream once
+// the per-voxel sums are done).
+int march_backward_clear(pvdb_march_s* m, cudaStream_t st) {
+  if (m->n_rays == 0) return PVDB_OK;
+  const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(stride_grid())));
+  k_cell_clear<<<sgrid, 256, 0, st>>>(m->red.keys[0], m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
+  PVDB_CHECK_LAUNCH("k_cell_clear");
+  return PVDB_OK;
+}
+
+// clear: also reset the cell counts here (else the caller runs
+// march_backward_clear).
+int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st, bool clear) {
   if (m->n_rays == 0) return PVDB_OK;
   if (!m->bwd_keys_ready) return set_error(PVDB_ERR_STATE, "march backward: keys not grouped");
   m->bwd_keys_ready = false;
@@ -973,9 +986,7 @@ int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st
     default: rc = cell_reduce_launch<4>(m, density, k0, grad_k0, st); break;
   }
   if (rc) return rc;
-  const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(stride_grid())));
-  k_cell_clear<<<sgrid, 256, 0, st>>>(m->red.keys[0], m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
-  PVDB_CHECK_LAUNCH("k_cell_clear");
+  if (clear && (rc = march_backward_clear(m, st))) return rc;
   if (m->prof) prof_mark(st, 8);
   return PVDB_OK;
 }
@@ -986,7 +997,7 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
   if (use_k0) PVDB_REQUIRE(m->k0->C <= 16, "the march backward takes at most 16 k0 channels");
   int rc = march_backward_keys(m, grad_w, grad_last, use_k0, st);
   if (rc) return rc;
-  return march_backward_reduce(m, grad_k0, st);
+  return march_backward_reduce(m, grad_k0, st, true);
 }
 
 int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,

@@ -35,7 +35,8 @@ const float* mlp_pe_buffer(pvdb_march_s* m, int* stride);
 int mlp_reserve_x(pvdb_march_s* m);
 int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
                         bool with_k0, cudaStream_t st);
-int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st);
+int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st, bool clear);
+int march_backward_clear(pvdb_march_s* m, cudaStream_t st);
 float opt_next_stepsz(pvdb_opt_s* o);
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
                cudaStream_t st);
@@ -288,7 +289,8 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
     rc = march_backward_keys(m, m->t_grad_w, m->t_grad_last, true, st);
     if (rc) return rc;
   }
-  rc = march_backward_reduce(m, m->t_grad_k0, st);
+  // the cell counts are reset beside TV / Adam (stage profiling: in sequence)
+  rc = march_backward_reduce(m, m->t_grad_k0, st, t.prof);
   if (rc) return rc;
   // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
   // TV of the two grids side by side (each grid's own touched list), then the
@@ -296,6 +298,7 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   // gradients, complete since the MLP backward
   const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
   if ((rc = fork_side(m, st, 2))) return rc;
+  if (!t.prof && (rc = march_backward_clear(m, m->side[1]))) return rc;
   rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
                          t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0,
                          m->side[1], t.ss_dev ? t.ss_dev + 2 : nullptr);

@@ -37,6 +37,8 @@ sys.path.insert(0, ROOT)
 RAYS = 8192
 RESO = 160
 METRIC = "fine-stage train it/s @8192 rays (160^3, k0=12, rgbnet 39-128-128-3)"
+WORKLOAD = (f"fine-stage iteration, {RAYS} rays, {RESO}^3 sparse VDB (8^3 leaves, 8 seeded "
+            "ellipsoids), k0=12, rgbnet 39-128-128-3, TV 1e-4")
 
 
 def parse():
@@ -45,7 +47,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32")
+    ap.add_argument("--precision", choices=["fp32", "bf16"], default="bf16",
+                    help="bf16: BF16 rgbnet on the tensor cores (the FP32 plain method is "
+                         "timed beside it); fp32: the plain method alone")
     ap.add_argument("--render-frames", type=int, default=200)
     ap.add_argument("--psnr-iters", type=int, default=2000,
                     help="training iterations of the BF16-vs-FP32 PSNR run (0: skip)")
@@ -254,9 +258,7 @@ def run_ours(args):
             "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
             "data": "synthetic: seeded 8-ellipsoid 160^3 scene, 100 seeded 800x800 views, "
                     "targets rendered from a seeded ground-truth grid",
-            "config": {"workload": f"fine-stage iteration, {RAYS} rays, {RESO}^3 sparse VDB "
-                                   f"(8^3 leaves), k0=12, rgbnet 39-128-128-3, TV 1e-4, "
-                                   f"{args.precision}",
+            "config": {"workload": WORKLOAD, "precision": args.precision,
                        "rays": RAYS, "reso": RESO, "l2": "512 MB buffer written between "
                                                          "timed steps, outside the step events",
                        "parallelism": "replicas" if ws_ > 1 else "single GPU",
@@ -634,8 +636,9 @@ def run_reference(args):
            "n_gpus": ws_, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic: seeded 8-ellipsoid 160^3 scene, seeded rays and targets",
-           "config": {"workload": f"fine-stage iteration, {RAYS} rays, {RESO}^3 sparse VDB, "
-                                  "k0=12, rgbnet 39-128-128-3, TV 1e-4, fp32"},
+           "config": {"workload": WORKLOAD, "precision": "fp32 (the CPU implementation has no "
+                                                            "BF16 path)",
+                      "rays": RAYS, "reso": RESO},
            "cpu_baseline": {"value": val, "unit": "it/s", "cores": O.num_threads(),
                             "kind": "port",
                             "sample": f"each step: {n} of the {RAYS} rays, time scaled by "

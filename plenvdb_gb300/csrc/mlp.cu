@@ -495,14 +495,32 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
 
 // Rows from any producer (the merged renderer): k0rows [M, c0], ray [M] ->
 // viewdirs [R,3]; M = totals[1]. hpe_buf holds R*(128+32) floats.
+// The per-ray PE alone into hpe_buf + R * 128 (stride kMaxPe floats): the
+// input of rgbnet X tiles that a caller builds itself.
+int mlp_pe_rows(const MlpArgs& a, const float* viewdirs, int R, float* hpe_buf, int* pe_stride,
+                cudaStream_t st) {
+  *pe_stride = kMaxPe;
+  if (R <= 0) return PVDB_OK;
+  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a,
+                                                 hpe_buf + size_t(R) * kW, nullptr);
+  PVDB_CHECK_LAUNCH("k_pe_hpe");
+  return PVDB_OK;
+}
+
+// x_ready (BF16 only): the X tiles in *xt are already built from the rows and
+// the PE (mlp_pe_rows), so neither is recomputed here.
 int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
                      const float* viewdirs, int R, const uint32_t* totals, int64_t max_rows,
                      float* out, int out_logits, float* hpe_buf, int precision, void** blob,
                      size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
-                     cudaStream_t st) {
+                     cudaStream_t st, int x_ready) {
   if (R <= 0) return PVDB_OK;
   float* hpe = hpe_buf;
   float* pe = hpe_buf + size_t(R) * kW;
+  if (precision == 1 && x_ready)
+    return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
+                               kMaxPe, totals, max_rows, out, out_logits, blob, blob_cap, xt,
+                               xt_cap, err, st, 0, 1);
   k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)

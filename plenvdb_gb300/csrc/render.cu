@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "pvdb_internal.cuh"
+#include "tc.cuh"
 
 namespace pvdb {
 
@@ -41,7 +42,9 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
                      const float* viewdirs, int R, const uint32_t* totals, int64_t max_rows,
                      float* out, int out_logits, float* hpe_buf, int precision, void** blob,
                      size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
-                     cudaStream_t st);
+                     cudaStream_t st, int x_ready);
+int mlp_pe_rows(const MlpArgs& a, const float* viewdirs, int R, float* hpe_buf, int* pe_stride,
+                cudaStream_t st);
 
 struct RenderP {
   int H, W, inverse_y;
@@ -70,6 +73,11 @@ struct RenderW {
   int32_t* rpix;     // [cap]
   uint32_t* totals;  // [0] unused, [1] total rows
   int64_t cap;
+  // BF16 rgbnet: the fill pass writes each colour sample's rgbnet input row
+  // ([k0 | PE | 1 | 0], BF16) into the X tiles instead of the FP32 k0 row
+  uint8_t* xt;       // [ceil(cap/128)] tiles, or NULL
+  const float* pe;   // [HW][pe_stride] per-pixel PE
+  int pe_stride, dpe;
 };
 
 __device__ __forceinline__ int32_t row_at(const RenderP& P, int i, int j, int k) {
@@ -82,6 +90,114 @@ __device__ __forceinline__ bool index_active(const RenderP& P, int i, int j, int
   if (l < 0) return false;
   const int v = vox_offset(i, j, k);
   return (__ldg(P.idx.mask + l * 8 + (v >> 6)) >> (v & 63)) & 1ull;
+}
+
+// 12-channel rows (the reference's k0): three float4, or three 8-byte BF16
+// quads per corner.
+__device__ __forceinline__ void fill_features12(const RenderP& P, const int32_t id[8],
+                                                const float sc[8], float acc[12]) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    float v[12];
+    if (P.storage == 0) {
+      const float4* src = reinterpret_cast<const float4*>(P.col + int64_t(id[c]) * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float4 f = __ldg(src + b);
+        v[4 * b] = f.x; v[4 * b + 1] = f.y; v[4 * b + 2] = f.z; v[4 * b + 3] = f.w;
+      }
+    } else {
+      const uint2* src = reinterpret_cast<const uint2*>(P.colh + int64_t(id[c]) * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const uint2 h = __ldg(src + b);
+        v[4 * b] = __uint_as_float(h.x << 16);
+        v[4 * b + 1] = __uint_as_float(h.x & 0xFFFF0000u);
+        v[4 * b + 2] = __uint_as_float(h.y << 16);
+        v[4 * b + 3] = __uint_as_float(h.y & 0xFFFF0000u);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 12; ++q)
+      acc[q] = c == 0 ? __fmul_rn(v[q], sc[0]) : __fmaf_rn(v[q], sc[c], acc[q]);
+  }
+}
+
+// Trilinear features of a colour sample (trigetColor, renderer.cu:303-310):
+// per channel c0*s0, then the fma chain over corners 1..7. 12-channel rows are
+// read with vector loads (three float4, or three 8-byte BF16 quads).
+__device__ __forceinline__ void fill_features(const RenderP& P, const int32_t id[8],
+                                              const float sc[8], float acc[16]) {
+  if (P.dcol == 12) {
+    fill_features12(P, id, sc, acc);
+    return;
+  }
+  for (int q = 0; q < P.dcol; ++q) {
+    float a;
+    if (P.storage == 0) {
+      a = __fmul_rn(__ldg(P.col + int64_t(id[0]) * P.dcol + q), sc[0]);
+      for (int c = 1; c < 8; ++c) a = __fmaf_rn(__ldg(P.col + int64_t(id[c]) * P.dcol + q), sc[c], a);
+    } else {
+      a = __fmul_rn(__bfloat162float(P.colh[int64_t(id[0]) * P.dcol + q]), sc[0]);
+      for (int c = 1; c < 8; ++c)
+        a = __fmaf_rn(__bfloat162float(P.colh[int64_t(id[c]) * P.dcol + q]), sc[c], a);
+    }
+    acc[q] = a;
+  }
+}
+
+// 12 k0 channels and 27 PE values (the rgbnet of the reference): the row is
+// 2 k0 chunks, the first of which carries PE 0..3, then pixel-constant chunks.
+__device__ __forceinline__ void write_x_row12(const RenderW& Wk, int64_t m, const float* k0v,
+                                              const uint4* pe_chunks) {
+  uint8_t* tile = Wk.xt + (m >> 7) * int64_t(kRgbXTile);
+  const int row = int(m & 127);
+  const uint4 c0 = make_uint4(tc::pack_bf16(k0v[0], k0v[1]), tc::pack_bf16(k0v[2], k0v[3]),
+                              tc::pack_bf16(k0v[4], k0v[5]), tc::pack_bf16(k0v[6], k0v[7]));
+  const uint4 c1 = make_uint4(tc::pack_bf16(k0v[8], k0v[9]), tc::pack_bf16(k0v[10], k0v[11]),
+                              pe_chunks[0].z, pe_chunks[0].w);
+  *reinterpret_cast<uint4*>(tile + tc::kmaj(row, 0, kRgbXK)) = c0;
+  *reinterpret_cast<uint4*>(tile + tc::kmaj(row, 8, kRgbXK)) = c1;
+#pragma unroll
+  for (int cb = 2; cb < 6; ++cb)
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(row, 8 * cb, kRgbXK)) = pe_chunks[cb - 1];
+}
+
+// The BF16 X row m of pixel n: [k0 (dcol) | PE (dpe) | 1 | 0 ...] in the
+// canonical K-major tile layout; pe_bits holds the pixel's PE as BF16 pairs.
+__device__ __forceinline__ void write_x_row(const RenderW& Wk, int64_t m, int n,
+                                            const float* k0v, int dcol, const uint32_t* pe_bits) {
+  uint8_t* tile = Wk.xt + (m >> 7) * int64_t(kRgbXTile);
+  const int row = int(m & 127);
+  const int din = dcol + Wk.dpe;
+#pragma unroll
+  for (int cb = 0; cb < kRgbXK / 8; ++cb) {
+    uint32_t w4[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      float v2[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = 8 * cb + 2 * e + h;
+        v2[h] = q < dcol ? k0v[q < 16 ? q : 15] : q == din ? 1.f : 0.f;
+      }
+      uint32_t bits = tc::pack_bf16(v2[0], v2[1]);
+      // PE columns come pre-rounded from pe_bits
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = 8 * cb + 2 * e + h;
+        if (q >= dcol && q < din) {
+          const int pq = q - dcol;
+          const uint32_t pb = (pe_bits[pq >> 1] >> (16 * (pq & 1))) & 0xFFFFu;
+          bits = h == 0 ? ((bits & 0xFFFF0000u) | pb) : ((bits & 0x0000FFFFu) | (pb << 16));
+        }
+      }
+      w4[e] = bits;
+    }
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(row, 8 * cb, kRgbXK)) =
+        make_uint4(w4[0], w4[1], w4[2], w4[3]);
+  }
+  (void)n;
 }
 
 template <bool FILL>
@@ -127,6 +243,53 @@ __global__ void __launch_bounds__(128)
   float T = 1.f;
   uint32_t cnt = 0;
   const int64_t base = FILL ? int64_t(Wk.off[n]) : 0;
+  // BF16 fill: the pixel's PE, rounded to BF16 once — for 12 k0 channels and
+  // 27 PE values as the pixel-constant part of its X rows (pe_chunks[0].zw =
+  // PE 0..3, pe_chunks[1..4] = columns 16..47), else as BF16 pairs
+  const bool fast12 = FILL && Wk.xt && P.dcol == 12 && Wk.dpe == 27;
+  uint4 pe_chunks[5];
+  uint32_t pe_bits[16];
+  if (fast12) {
+    const float* pp = Wk.pe + int64_t(n) * Wk.pe_stride;
+    float pv[27];
+#pragma unroll
+    for (int q = 0; q < 27; ++q) pv[q] = pp[q];
+    pe_chunks[0] = make_uint4(0u, 0u, tc::pack_bf16(pv[0], pv[1]), tc::pack_bf16(pv[2], pv[3]));
+#pragma unroll
+    for (int cb = 2; cb < 5; ++cb) {  // columns 8cb .. 8cb+7 = PE 8cb-12 ..
+      uint32_t w4[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int p0 = 8 * cb - 12 + 2 * e, p1 = p0 + 1;
+        const float a0 = p0 < 27 ? pv[p0 < 27 ? p0 : 0] : (p0 == 27 ? 1.f : 0.f);
+        const float a1 = p1 < 27 ? pv[p1 < 27 ? p1 : 0] : (p1 == 27 ? 1.f : 0.f);
+        w4[e] = tc::pack_bf16(a0, a1);
+      }
+      pe_chunks[cb - 1] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+    }
+    pe_chunks[4] = make_uint4(0u, 0u, 0u, 0u);
+  } else if (FILL && Wk.xt) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int q0 = 2 * i, q1 = 2 * i + 1;
+      const float a0 = q0 < Wk.dpe ? Wk.pe[int64_t(n) * Wk.pe_stride + q0] : 0.f;
+      const float a1 = q1 < Wk.dpe ? Wk.pe[int64_t(n) * Wk.pe_stride + q1] : 0.f;
+      pe_bits[i] = tc::pack_bf16(a0, a1);
+    }
+  }
+  if (FILL && Wk.xt) {
+    // the padding rows of the last tile are zero (block 0 writes them)
+    if (blockIdx.x == 0) {
+      const int64_t M = Wk.totals[1], Mpad = (M + 127) / 128 * 128;
+      const int64_t mz = M + threadIdx.x;
+      if (mz < Mpad) {  // Mpad <= the tiles reserved for cap rows
+        uint8_t* tile = Wk.xt + (mz >> 7) * int64_t(kRgbXTile);
+        for (int cb = 0; cb < kRgbXK / 8; ++cb)
+          *reinterpret_cast<uint4*>(tile + tc::kmaj(int(mz & 127), 8 * cb, kRgbXK)) =
+              make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
+  }
   float t = tmin;
   // the reference loops while t < tmax; the iteration bound (the sample count
   // of the [tmin,tmax] chord plus slack) only guards against a step that no
@@ -167,19 +330,26 @@ __global__ void __launch_bounds__(128)
     if (FILL) {
       const int64_t m = base + cnt;
       if (m < Wk.cap) {
-        float* dst = Wk.rk0 + m * P.dcol;
-        for (int q = 0; q < P.dcol; ++q) {
-          float acc;
-          if (P.storage == 0) {
-            acc = __fmul_rn(__ldg(P.col + int64_t(id[0]) * P.dcol + q), sc[0]);
-            for (int c = 1; c < 8; ++c)
-              acc = __fmaf_rn(__ldg(P.col + int64_t(id[c]) * P.dcol + q), sc[c], acc);
-          } else {
-            acc = __fmul_rn(__bfloat162float(P.colh[int64_t(id[0]) * P.dcol + q]), sc[0]);
-            for (int c = 1; c < 8; ++c)
-              acc = __fmaf_rn(__bfloat162float(P.colh[int64_t(id[c]) * P.dcol + q]), sc[c], acc);
-          }
-          dst[q] = acc;
+        if (Wk.xt && fast12) {
+          float acc[12];
+          fill_features12(P, id, sc, acc);
+          write_x_row12(Wk, m, acc, pe_chunks);
+        } else if (Wk.xt) {
+          float acc[16];
+          fill_features(P, id, sc, acc);
+          write_x_row(Wk, m, n, acc, P.dcol, pe_bits);
+        } else if (P.dcol == 12) {
+          float acc[12];
+          fill_features12(P, id, sc, acc);
+          float4* dst = reinterpret_cast<float4*>(Wk.rk0 + m * 12);
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            dst[b] = make_float4(acc[4 * b], acc[4 * b + 1], acc[4 * b + 2], acc[4 * b + 3]);
+        } else {
+          float* dst = Wk.rk0 + m * P.dcol;
+          float acc[16];
+          fill_features(P, id, sc, acc);
+          for (int q = 0; q < P.dcol; ++q) dst[q] = acc[q];
         }
         Wk.rw[m] = wt;
         Wk.rpix[m] = n;
@@ -540,9 +710,6 @@ int pvdb_renderer_render(pvdb_renderer r, int32_t precision, pvdb_stream s) {
   Wk.rw = r->d_rw;
   Wk.rpix = r->d_rpix;
   Wk.cap = r->rows_cap;
-  k_render_march<true><<<ceil_div(HW, 128), 128, 0, st>>>(P, Wk);
-  PVDB_CHECK_LAUNCH("k_render_march<fill>");
-  prof_mark(st, 3);
   MlpArgs a;
   const int din = r->dcol + r->dpe, H = r->dhid;
   a.w0 = r->d_params;
@@ -554,10 +721,25 @@ int pvdb_renderer_render(pvdb_renderer r, int32_t precision, pvdb_stream s) {
   a.c0 = r->dcol;
   a.dpe = r->dpe;
   a.din = din;
+  // BF16 rgbnet: the fill pass writes the X tiles (with the PE computed first)
+  const bool x_direct = precision == 1 && total > 0 && din + 1 <= kRgbXK;
+  if (x_direct) {
+    const int64_t ntiles = (r->rows_cap + 127) / 128;
+    if ((rc = dev_reserve(&r->d_xt, &r->xt_cap, size_t(ntiles) * kRgbXTile))) return rc;
+    int pe_stride = 0;
+    if ((rc = mlp_pe_rows(a, r->d_viewdirs, HW, r->d_hpe, &pe_stride, st))) return rc;
+    Wk.xt = static_cast<uint8_t*>(r->d_xt);
+    Wk.pe = r->d_hpe + size_t(HW) * H;
+    Wk.pe_stride = pe_stride;
+    Wk.dpe = r->dpe;
+  }
+  k_render_march<true><<<ceil_div(HW, 128), 128, 0, st>>>(P, Wk);
+  PVDB_CHECK_LAUNCH("k_render_march<fill>");
+  prof_mark(st, 3);
   if (total) {
     rc = mlp_forward_rows(a, r->d_rk0, r->d_rpix, r->d_viewdirs, HW, r->d_totals, r->rows_cap,
                           r->d_logits, 1, r->d_hpe, precision, &r->d_packed, &r->packed_cap,
-                          &r->d_xt, &r->xt_cap, r->d_totals + 3, st);
+                          &r->d_xt, &r->xt_cap, r->d_totals + 3, st, x_direct ? 1 : 0);
     if (rc) return rc;
   }
   prof_mark(st, 4);

@@ -282,19 +282,20 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def stage_profile(tr, dev, nb, flush, args):
+def stage_profile(tr, dev, nb, flush, args, n=None):
     """Per-stage device time from events between the stages of eagerly launched
     steps (a graph replay has no stage boundaries); a separate, shorter pass
     after the timed region."""
     import ctypes
     import torch
     from plenvdb_gb300 import _lib as L
-    n = max(5, min(args.steps, 20))
+    n = n or max(5, min(args.steps, 20))
     use_graph = tr.tc.use_graph
     tr.tc.use_graph = 0
     L.call("pvdb_profile_begin", n)
     for i in range(n):
-        flush_l2(flush)
+        if flush is not None:
+            flush_l2(flush)
         tr.step(*dev[i % nb])
     torch.cuda.synchronize()
     marks = (ctypes.c_float * 16)()
@@ -369,7 +370,7 @@ def stage_work(tr, R):
     }, (kept, rows, evaluated)
 
 
-def roofline(stage_ms, tr, scfg):
+def roofline(stage_ms, tr, scfg, R=RAYS):
     """Roofline of the dominant stage: algorithmic bytes (or FLOPs) per launch
     over the stage's CUDA-event time, against the measured peaks."""
     import json as _json
@@ -380,7 +381,7 @@ def roofline(stage_ms, tr, scfg):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     tflops = float(peaks.get("bf16_tflops", 1900.0))
-    work, (kept, rows, evaluated) = stage_work(tr, RAYS)
+    work, (kept, rows, evaluated) = stage_work(tr, R)
     table = {}
     for name, ms in stage_ms.items():
         if name not in work or ms <= 0:
@@ -572,6 +573,12 @@ def run_large(args, steps=10, warmup=3):
         res[tag] = {"it_s": 1e3 / ms, "ms_per_step": ms, "rays_per_s": R * 1e3 / ms,
                     "kept_samples": kept, "color_rows": rows, "evaluated_samples": evaluated,
                     "loss": float(tr.loss.item())}
+        if prec == 1:
+            # per-stage times and rooflines at this size (grids beyond L2)
+            sm = stage_profile(tr, batches, nb, None, None, n=5)
+            roof = roofline(sm, tr, scfg, R=R)
+            res[tag]["stage_ms"] = sm
+            res[tag]["stages"] = roof["stages"]
         del tr, dg, kg
     res["speedup_bf16"] = res["bf16"]["it_s"] / res["fp32"]["it_s"]
     res["timing"] = (f"CUDA events over {steps} steps after {warmup} warm-up steps; inputs "

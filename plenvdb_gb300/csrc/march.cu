@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(256)
 // chunks.
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_bwd(GridView gd, int R, MarchP P, MarchW W, const float* __restrict__ grad_w,
-                const float* __restrict__ grad_last, uint32_t* keys) {
+                const float* __restrict__ grad_last, uint32_t* keys, uint32_t* cnt,
+                uint32_t* leaf_cnt, uint32_t* rank) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -383,6 +384,7 @@ __global__ void __launch_bounds__(kMarchThreads)
   const int64_t sbase = int64_t(r) * P.cap;
   const int64_t kb = W.kept_off[r];
   const int nchunks = (nk + 31) >> 5;
+  const unsigned lt = lanemask_lt();
   RaySetup rs;
   load_setup(W, r, rs);
   float carry = (grad_last ? grad_last[r] : 0.f) * W.T_last[r];
@@ -391,6 +393,7 @@ __global__ void __launch_bounds__(kMarchThreads)
     const bool valid = i < nk;
     float a = 1.f, w = 0.f, gw = 0.f;
     int32_t st = 0, row = -1;
+    uint32_t key = kInvalidKey;
     if (valid) {
       a = W.k_alpha[sbase + i];
       w = W.k_w[sbase + i];
@@ -422,8 +425,22 @@ __global__ void __launch_bounds__(kMarchThreads)
       const int64_t s = kb + i;
       W.b_rec[s] = make_float4(idx[0], idx[1], idx[2], gs);
       W.b_row[s] = row;
-      keys[s] = cell_key(gd.ldim, ifloor(idx[0]), ifloor(idx[1]), ifloor(idx[2]));
+      key = cell_key(gd.ldim, ifloor(idx[0]), ifloor(idx[1]), ifloor(idx[2]));
+      keys[s] = key;
     }
+    // counts per cell and per leaf for the grouping: one atomic per distinct
+    // cell (leaf) among the warp's samples; each sample gets a distinct rank
+    // within its cell (in no particular order)
+    const bool counted = valid && key != kInvalidKey;
+    const unsigned same = __match_any_sync(0xffffffffu, counted ? key : kInvalidKey);
+    const int lead = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (counted && lane == lead) base = atomicAdd(cnt + key, uint32_t(__popc(same)));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    if (counted) rank[kb + i] = base + uint32_t(__popc(same & lt));
+    const uint32_t lkey = counted ? (key >> 9) : 0xFFFFFFFFu;
+    const unsigned same_l = __match_any_sync(0xffffffffu, lkey);
+    if (counted && lane == __ffs(same_l) - 1) atomicAdd(leaf_cnt + lkey, uint32_t(__popc(same_l)));
   }
 }
 
@@ -434,9 +451,9 @@ __global__ void __launch_bounds__(kMarchThreads)
 // (k0). The cell key is a leaf-major code of the low corner (dense leaf index
 // x 512 + NanoVDB offset). The samples are grouped by cell with a counting
 // placement:
-//   k_cell_count   per sample: its rank among the samples of its cell (an
-//                  atomic counter, so in no particular order) and the counts
-//                  per cell and per leaf;
+//   k_march_bwd    per sample: its rank among the samples of its cell (an
+//                  atomic counter per distinct cell of a warp, so in no
+//                  particular order) and the counts per cell and per leaf;
 //   leaf scan      exclusive scan of the per-leaf counts (one block);
 //   k_cell_offsets per leaf with samples: exclusive scan of its 512 cell
 //                  counts, offset by the leaf's start;
@@ -469,18 +486,6 @@ __device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, in
 #pragma unroll
   for (int c = 0; c < 8; ++c)
     if (s[c] >= 0) touched[s[c] >> 9] = 1;
-}
-
-__global__ void k_cell_count(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
-                             uint32_t* cnt, uint32_t* leaf_cnt, uint32_t* rank) {
-  const int64_t n = *n_dev;
-  for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
-       s += int64_t(gridDim.x) * blockDim.x) {
-    const uint32_t key = keys[s];
-    if (key == kInvalidKey) continue;
-    rank[s] = atomicAdd(cnt + key, 1u);
-    atomicAdd(leaf_cnt + (key >> 9), 1u);
-  }
 }
 
 // Block (512 threads) per dense leaf with samples.
@@ -919,18 +924,18 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
       (rc = dev_reserve((void**)&m->w.b_row, &m->b_row_cap, size_t(nmax) * 4)))
     return rc;
   const int nb = ceil_div(R, kMarchWarps);
-  k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
-                                            m->red.keys[0]);
-  PVDB_CHECK_LAUNCH("k_march_bwd");
-  if (m->prof) prof_mark(st, 6);
-  // group the kept samples by cell (stable order, see above)
+  // the kept samples' keys, with their per-cell ranks and the per-cell and
+  // per-leaf counts of the grouping below
   const uint32_t* keys = m->red.keys[0];
   uint32_t* rank = m->red.vals[1];
   uint32_t* skeys = m->red.keys[1];
   uint32_t* svals = m->red.vals[0];
+  k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
+                                            m->red.keys[0], m->cell_cnt, m->leaf_cnt, rank);
+  PVDB_CHECK_LAUNCH("k_march_bwd");
+  if (m->prof) prof_mark(st, 6);
+  // group the kept samples by cell (stable order, see above)
   const int sgrid = int(std::min<int64_t>(ceil_div(nmax, 256), int64_t(stride_grid())));
-  k_cell_count<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_cnt, m->leaf_cnt, rank);
-  PVDB_CHECK_LAUNCH("k_cell_count");
   rc = scan_exclusive_u32(m->leaf_cnt, m->leaf_off, nleaves, m->w.totals + 5, &m->scan_partial,
                           &m->scan_partial_cap, st);
   if (rc) return rc;

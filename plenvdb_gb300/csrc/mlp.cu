@@ -380,19 +380,21 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
 // Sum of the per-CTA partials: eight interleaved running sums (partials c,
 // c+8, ...) combined in a fixed order, so the loads of eight partials are in
 // flight together and the result is the same on every run.
-__global__ void k_wgrad_reduce(const float* __restrict__ wpart, int nparts, int64_t P, float* out) {
-  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (i >= P) return;
-  float acc[8];
-#pragma unroll
-  for (int u = 0; u < 8; ++u) acc[u] = 0.f;
-  int c = 0;
-  for (; c + 8 <= nparts; c += 8) {
-#pragma unroll
-    for (int u = 0; u < 8; ++u) acc[u] += wpart[int64_t(c + u) * P + i];
-  }
-  for (int u = 0; c < nparts; ++c, ++u) acc[u] += wpart[int64_t(c) * P + i];
-  out[i] = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+// 256 threads per 32 parameters: warp u sums the partials c = u, u+8, ... in
+// increasing c, then the 8 warp sums combine as ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)).
+__global__ void __launch_bounds__(256)
+    k_wgrad_reduce(const float* __restrict__ wpart, int nparts, int64_t P, float* out) {
+  __shared__ float part[8][33];
+  const int u = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = blockIdx.x * 32ll + lane;
+  float acc = 0.f;
+  if (i < P)
+    for (int c = u; c < nparts; c += 8) acc += __ldg(wpart + int64_t(c) * P + i);
+  part[u][lane] = acc;
+  __syncthreads();
+  if (u == 0 && i < P)
+    out[i] = ((part[0][lane] + part[1][lane]) + (part[2][lane] + part[3][lane])) +
+             ((part[4][lane] + part[5][lane]) + (part[6][lane] + part[7][lane]));
 }
 
 __global__ void k_scatter_grads(const float* __restrict__ flat, int din, float* w0, float* b0,
@@ -563,7 +565,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
                               &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap, m->w.totals + 3, st,
                               prepared ? 1 : 0, prepared ? 1 : 0);
     if (rc) return rc;
-    k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+    k_wgrad_reduce<<<ceil_div(P, 32), 256, 0, st>>>(m->wpart, G, P, grad_flat);
     PVDB_CHECK_LAUNCH("k_wgrad_reduce");
     return PVDB_OK;
   }
@@ -572,7 +574,7 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
       a, k0rows, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
       grad_rgb, grad_k0, m->wpart);
   PVDB_CHECK_LAUNCH("k_mlp_bwd_f32");
-  k_wgrad_reduce<<<ceil_div(P, 256), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+  k_wgrad_reduce<<<ceil_div(P, 32), 256, 0, st>>>(m->wpart, G, P, grad_flat);
   PVDB_CHECK_LAUNCH("k_wgrad_reduce");
   return PVDB_OK;
 }

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256)
   }
   W.ray_ns[r] = int32_t(ns);
   atomicAdd(W.totals + 4, uint32_t(ns));
-  if (r < (R + kMarchWarps - 1) / kMarchWarps) W.chain_status[r] = 0ull;  // k_march_chain tiles
+  W.chain_status[r] = 0ull;  // k_march_chain look-back status of this ray
 }
 
 // One block per ray, threads over the ray's samples.
@@ -120,31 +120,28 @@ __global__ void __launch_bounds__(256)
 
 constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
 
-// Ray offsets: CTAs take 8-ray tiles in order from a counter (totals[6]); a
-// tile publishes its (colour, kept) counts, then sums the earlier tiles'
-// published counts back to the first inclusive prefix (decoupled look-back).
-// A tile publishes before it waits and only waits on tiles taken earlier
-// (running or done), so every wait ends; each is still bounded, and one that
-// gives up sets error bit 4.
-constexpr uint64_t kChainAgg = 1ull << 62;     // status: tile counts published
+// Ray offsets: warps take rays in order from a counter (totals[6]); a ray
+// publishes its (colour, kept) counts, then sums the earlier rays' published
+// counts back to the first inclusive prefix, 32 rays at a time (decoupled
+// look-back). A ray publishes before it waits and only waits on rays taken
+// earlier (running or done), so every wait ends; each is still bounded, and
+// one that gives up sets error bit 4.
+constexpr uint64_t kChainAgg = 1ull << 62;     // status: ray counts published
 constexpr uint64_t kChainPrefix = 1ull << 63;  // status: inclusive prefix published
 constexpr uint64_t kChainValue = kChainAgg - 1;
 constexpr uint32_t kChainSpinMax = 1u << 24;
 
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_chain(int R, MarchP P, MarchW W) {
-  __shared__ int tile_s;
-  __shared__ uint64_t wcnt[kMarchWarps];  // (colour << 32) | kept per ray
-  __shared__ uint64_t base_s;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) tile_s = int(atomicAdd(W.totals + 6, 1u));
-  __syncthreads();
-  const int tile = tile_s;
-  const int r = tile * kMarchWarps + warp;
+  const int lane = threadIdx.x & 31;
+  uint32_t ticket = 0;
+  if (lane == 0) ticket = atomicAdd(W.totals + 6, 1u);
+  const int r = int(__shfl_sync(0xffffffffu, ticket, 0));
+  if (r >= R) return;
   const unsigned lt = lanemask_lt();
   const int64_t sbase = int64_t(r) * P.cap;
   int nk = 0, nc = 0;
-  if (r < R) {
+  {
     const int ns = W.ray_ns[r];
     float T = 1.f;
     bool stop = false;
@@ -198,54 +195,45 @@ __global__ void __launch_bounds__(kMarchThreads)
       W.n_color[r] = nc;
     }
   }
-  if (lane == 0) wcnt[warp] = (uint64_t(nc) << 32) | uint64_t(uint32_t(nk));
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint64_t agg = 0;
-#pragma unroll
-    for (int q = 0; q < kMarchWarps; ++q) agg += wcnt[q];
-    volatile uint64_t* status = W.chain_status;
-    uint64_t excl = 0;
-    if (tile == 0) {
-      status[0] = kChainPrefix | agg;
-    } else {
-      status[tile] = kChainAgg | agg;
-      for (int t = tile - 1; t >= 0; --t) {
-        uint64_t v = status[t];
-        for (uint32_t it = 0; v == 0ull; ++it) {
-          if (it >= kChainSpinMax) {
-            atomicOr(W.totals + 3, 4u);
-            v = kChainPrefix;  // give up: offsets wrong, but the kernel ends
-            break;
-          }
-          v = status[t];
-        }
-        excl += v & kChainValue;
-        if (v & kChainPrefix) break;
+  // publish, then look back 32 rays at a time
+  const uint64_t agg = (uint64_t(nc) << 32) | uint64_t(uint32_t(nk));
+  volatile uint64_t* status = W.chain_status;
+  if (lane == 0) status[r] = (r == 0 ? kChainPrefix : kChainAgg) | agg;
+  uint32_t ex_k = 0, ex_c = 0;  // exclusive prefix (kept, colour)
+  for (int t = r - 1; t >= 0; t -= 32) {
+    const int j = t - lane;
+    uint64_t v = j >= 0 ? uint64_t(status[j]) : uint64_t(kChainPrefix);
+    for (uint32_t it = 0; __any_sync(0xffffffffu, v == 0ull); ++it) {
+      if (it >= kChainSpinMax) {
+        if (lane == 0) atomicOr(W.totals + 3, 4u);
+        v = v ? v : uint64_t(kChainPrefix);  // give up: offsets wrong, but the kernel ends
+        break;
       }
-      status[tile] = kChainPrefix | (excl + agg);
+      if (v == 0ull) v = status[j];
     }
-    base_s = excl;
-    if ((tile + 1) * kMarchWarps >= R) {
+    const unsigned pm = __ballot_sync(0xffffffffu, (v & kChainPrefix) != 0ull);
+    const int stop_lane = pm ? __ffs(pm) - 1 : 31;  // nearest ray with a prefix
+    const uint64_t val = lane <= stop_lane && j >= 0 ? (v & kChainValue) : 0ull;
+    ex_k += __reduce_add_sync(0xffffffffu, uint32_t(val));
+    ex_c += __reduce_add_sync(0xffffffffu, uint32_t(val >> 32));
+    if (pm) break;
+  }
+  const uint64_t excl = (uint64_t(ex_c) << 32) | ex_k;
+  if (lane == 0) {
+    if (r > 0) status[r] = kChainPrefix | (excl + agg);
+    W.kept_off[r] = ex_k;
+    W.color_off[r] = ex_c;
+    if (r == R - 1) {
       W.totals[0] = uint32_t(excl + agg);
       W.totals[1] = uint32_t((excl + agg) >> 32);
     }
-  }
-  __syncthreads();
-  if (r >= R) return;
-  uint64_t off = base_s;
-  for (int q = 0; q < warp; ++q) off += wcnt[q];
-  const uint32_t coff = uint32_t(off >> 32);
-  if (lane == 0) {
-    W.kept_off[r] = uint32_t(off);
-    W.color_off[r] = coff;
   }
   // colour rows: global row m = color_off + rank, the row record, k_row = m
   for (int i = lane; i < nk; i += 32) {
     const int64_t t = sbase + i;
     const int32_t rank = W.k_row[t];
     if (rank < 0) continue;
-    const int64_t m = int64_t(coff) + rank;
+    const int64_t m = int64_t(ex_c) + rank;
     W.r_w[m] = W.k_w[t];
     W.r_alpha[m] = W.k_alpha[t];
     W.r_ray[m] = r;
@@ -1054,7 +1042,7 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
   const size_t R = max_rays, S = size_t(m->slots);
   int rc;
   if ((rc = dev_alloc((void**)&w.ray_sd, R * 24)) || (rc = dev_alloc((void**)&w.ray_ns, R * 4)) ||
-      (rc = dev_alloc((void**)&w.chain_status, ((R + kMarchWarps - 1) / kMarchWarps) * 8)) ||
+      (rc = dev_alloc((void**)&w.chain_status, R * 8)) ||
       (rc = dev_alloc((void**)&w.T_last, R * 4)) || (rc = dev_alloc((void**)&w.n_kept, R * 4)) ||
       (rc = dev_alloc((void**)&w.n_color, R * 4)) ||
       (rc = dev_alloc((void**)&w.kept_off, R * 4)) ||

@@ -28,7 +28,7 @@ struct MarchW {
   // per ray
   float* ray_sd;  // [R*6] sample origin (rays_o + rays_d*t_min) and unit direction
   int32_t* ray_ns;  // [R] samples in the bbox (clamped to cap)
-  uint64_t* chain_status;  // [ceil(R/8)] k_march_chain tile counts / prefixes
+  uint64_t* chain_status;  // [R] k_march_chain ray counts / prefixes
   float* T_last;
   uint32_t* n_kept;
   uint32_t* n_color;
@@ -53,7 +53,7 @@ struct MarchW {
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 ray-offset look-back
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
-  // [6] k_march_chain tile counter, [7] train-step loss block counter
+  // [6] k_march_chain ray counter, [7] train-step loss block counter
   uint32_t* totals;
 };
 

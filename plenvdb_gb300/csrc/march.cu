@@ -476,36 +476,44 @@ __device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, in
     if (s[c] >= 0) touched[s[c] >> 9] = 1;
 }
 
-// Block (512 threads) per dense leaf with samples.
-__global__ void __launch_bounds__(kLeafVox)
+// Warp per dense leaf with samples: lane t scans cells 16t .. 16t+15 (four
+// 16-byte loads), the warp scans the lane totals.
+__global__ void __launch_bounds__(256)
     k_cell_offsets(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ leaf_cnt,
                    const uint32_t* __restrict__ leaf_off, int64_t nleaves, uint32_t* off) {
-  __shared__ uint32_t warp_sums[kLeafVox / 32];
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
-    if (leaf_cnt[l] == 0) continue;  // uniform over the block
-    const int64_t e = l * kLeafVox + t;
-    const uint32_t v = cnt[e];
-    uint32_t x = v;
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t l = w0; l < nleaves; l += nw) {
+    if (__ldg(leaf_cnt + l) == 0) continue;  // uniform over the warp
+    const uint4* src = reinterpret_cast<const uint4*>(cnt + l * kLeafVox) + lane * 4;
+    uint32_t v[16];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const uint4 q = src[b];
+      v[4 * b] = q.x; v[4 * b + 1] = q.y; v[4 * b + 2] = q.z; v[4 * b + 3] = q.w;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sum += v[q];
+    uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    if (lane == 31) warp_sums[w] = x;
-    __syncthreads();
-    if (w == 0) {
-      uint32_t s = lane < kLeafVox / 32 ? warp_sums[lane] : 0u;
+    uint32_t run = __ldg(leaf_off + l) + x - sum;
+    uint4* dst = reinterpret_cast<uint4*>(off + l * kLeafVox) + lane * 4;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += y;
+    for (int b = 0; b < 4; ++b) {
+      uint32_t o4[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        o4[e] = run;
+        run += v[4 * b + e];
       }
-      if (lane < kLeafVox / 32) warp_sums[lane] = s;
+      dst[b] = make_uint4(o4[0], o4[1], o4[2], o4[3]);
     }
-    __syncthreads();
-    off[e] = leaf_off[l] + (w ? warp_sums[w - 1] : 0u) + x - v;
-    __syncthreads();
   }
 }
 
@@ -572,16 +580,33 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
     const uint32_t key = skeys[i];
     if (i > 0 && skeys[i - 1] == key) continue;
     sort_segment(svals + i, cnt[key]);
+    const int off = int(key & 511u);
+    const int al = __ldg(gd.table + (key >> 9));  // the cell's own leaf, if allocated
+    const bool interior = al >= 0 && (off >> 6) != 7 && ((off >> 3) & 7) != 7 && (off & 7) != 7;
+    if (interior) {
+      // all 8 corners lie in the cell's own leaf
+      touched_d[al] = 1;
+      if (touched_c && k0_same) touched_c[al] = 1;
+    }
+    if (interior && (!touched_c || k0_same)) continue;
     int ci, cj, ck;
-    cell_decode(gd.ldim, key, ci, cj, ck);
-    int sl[8];
-    corner_slots(gd, ci, cj, ck, sl);
+    if (al >= 0) {
+      ci = __ldg(gd.origin + al * 3) + (off >> 6);
+      cj = __ldg(gd.origin + al * 3 + 1) + ((off >> 3) & 7);
+      ck = __ldg(gd.origin + al * 3 + 2) + (off & 7);
+    } else {
+      cell_decode(gd.ldim, key, ci, cj, ck);
+    }
+    if (!interior) {
+      int sl[8];
+      corner_slots(gd, ci, cj, ck, sl);
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (sl[c] >= 0) {
-        touched_d[sl[c] >> 9] = 1;
-        if (touched_c && k0_same) touched_c[sl[c] >> 9] = 1;
-      }
+      for (int c = 0; c < 8; ++c)
+        if (sl[c] >= 0) {
+          touched_d[sl[c] >> 9] = 1;
+          if (touched_c && k0_same) touched_c[sl[c] >> 9] = 1;
+        }
+    }
     if (touched_c && !k0_same) mark_corner_leaves(gc, ci, cj, ck, touched_c);
   }
 }
@@ -927,8 +952,8 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   rc = scan_exclusive_u32(m->leaf_cnt, m->leaf_off, nleaves, m->w.totals + 5, &m->scan_partial,
                           &m->scan_partial_cap, st);
   if (rc) return rc;
-  k_cell_offsets<<<int(std::min<int64_t>(nleaves, int64_t(num_sms()) * 4)), kLeafVox, 0, st>>>(
-      m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off);
+  k_cell_offsets<<<int(std::min<int64_t>(ceil_div(nleaves, 8), int64_t(stride_grid()))), 256, 0,
+                   st>>>(m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off);
   PVDB_CHECK_LAUNCH("k_cell_offsets");
   k_cell_place<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
   PVDB_CHECK_LAUNCH("k_cell_place");

@@ -353,6 +353,18 @@ def run_e2e(tr, ro, rd, vd, tgt, args, flush):
 #   voxel_gather    64 B record + 8 corner gradients (1 + C floats) per kept sample
 #   voxel_adam      28 B per visited voxel-channel (p, g, m, v read; p, m, v written)
 RGBNET_FWD_ROW, RGBNET_FWD_RAY, RGBNET_BWD_ROW = 36608.0, 6912.0, 122880.0
+# DRAM bytes (read + write) per launch of each stage's kernels at this workload,
+# from the ncu captures summarised in profiles/*_bf16_160cube_8192rays.md
+# (cold L2; the grids are L2-resident in the live step, so these are the
+# bytes a launch pulls from HBM, not the algorithmic bytes above)
+NCU_TRAFFIC = {
+    "march_fwd": 2.137e6 + 11.177e6,   # k_march_alpha + k_march_chain
+    "k0_gather": 13.279e6,             # k_march_k0_x
+    "rgbnet_fwd": 15.113e6,            # k_mlp_fwd_tc
+    "rgbnet_bwd": 19.026e6,            # k_mlp_bwd_tc
+    "march_bwd": 7.266e6,              # k_march_bwd
+    "voxel_gather": 27.686e6,          # k_voxel_gather
+}
 
 
 def stage_work(tr, R):
@@ -400,7 +412,9 @@ def roofline(stage_ms, tr, scfg, R=RAYS):
            "achieved": t["achieved"] if t else None,
            "peak": (hbm if (not t or t["bound"] == "hbm") else tflops),
            "unit": t["unit"] if t else "GB/s", "frac": t["frac"] if t else None,
-           "traffic": None, "peak_source": src, "avg_ms": stage_ms[name],
+           "traffic": NCU_TRAFFIC.get(name) if R == RAYS else None,
+           "traffic_source": f"ncu capture, profiles/ (stage {name})" if R == RAYS else None,
+           "peak_source": src, "avg_ms": stage_ms[name],
            "kept_samples": kept, "color_rows": rows, "evaluated_samples": evaluated,
            "stages": table}
     return out

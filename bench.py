@@ -71,6 +71,21 @@ def dist_info():
     return ws, rank, local
 
 
+def replica_throughput(step_ms_total, steps, world, device="cuda"):
+    """Whole-job it/s of `world` independent replicas (the path has no
+    cross-GPU exchange): every replica runs `steps` steps, the job's time is
+    the slowest replica's (max over ranks), value = world * steps / time.
+    Returns (value, ms_per_step of the slowest replica)."""
+    import torch
+    import torch.distributed as dist
+    t = float(step_ms_total)
+    if world > 1:
+        x = torch.tensor([t], device=device, dtype=torch.float64)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return world * steps / (t / 1e3), t / steps
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled during the timed region."""
@@ -209,12 +224,7 @@ def run_ours(args):
     launches = lib.pvdb_launch_count() - launches0
     clk = clocks.stop()
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
-    if ws_ > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    ms_per_step = step_ms / args.steps
-    value = ws_ * args.steps / (step_ms / 1e3)
+    value, ms_per_step = replica_throughput(step_ms, args.steps, ws_)
     stage_ms = stage_profile(tr, dev, nb, flush, args)
     # ---------------- the FP32 plain method on the same workload, same timing
     plain = None

@@ -472,6 +472,96 @@ int pvdb_renderer_output(pvdb_renderer r, float* out, int32_t mem, pvdb_stream s
  * (device scalar). */
 int pvdb_renderer_views(pvdb_renderer r, float** image, int32_t** n_samples_total);
 
+/* ------------------------------------------------------- grid lifecycle
+ * The steps of the DVGO schedule around the training step (run.py:430-512):
+ * merged-row compression for the renderer, progressive rescaling, the
+ * occupancy (mask-cache) builds, near-camera masking, per-voxel view counts,
+ * and the training-ray generation of the in-mask-cache sampler. Device
+ * buffers only. Calls that return a count synchronise the stream.            */
+
+/* Number of nonzero bytes of mask [n] (the N of vdb_compression.py:27-29). */
+int pvdb_merge_count(const uint8_t* mask, int64_t n, int64_t* n_active, pvdb_stream s);
+
+/* vdb_compression.py:19-59 without the file I/O: the voxels with a nonzero
+ * mask byte (mask [rx*ry*rz], C order) get row ids 1..N in C order, written
+ * to index [rx*ry*rz] (0 = empty); row 0 of den_rows [N+1] and col_rows
+ * [(N+1)*C] is zero, row r holds the voxel's density and its C colour
+ * channels (copyToArray values: the background outside allocated leaves).
+ * row_dtype 0 = FP32, 1 = FP16 (the reference's mergeddata.npz). density or
+ * color may be NULL (then its rows are not written). n_rows must be N+1; it
+ * is checked before anything is written. Synchronises. */
+int pvdb_merge_build(pvdb_grid density, pvdb_grid color, const uint8_t* mask, int32_t* index,
+                     void* den_rows, void* col_rows, int64_t n_rows, int32_t row_dtype,
+                     pvdb_stream s);
+
+/* Stable compaction of up to four [n,3] float arrays by keep [n] (nonzero =
+ * kept): dst[k] receives the kept rows of src[k] in order. cap is the row
+ * capacity of every dst (checked before writing); *n_kept the kept count.
+ * Synchronises. */
+int pvdb_compact_rows(const uint8_t* keep, int64_t n, const float* const* src, float* const* dst,
+                      int32_t n_arrays, int64_t cap, int64_t* n_kept, pvdb_stream s);
+
+/* VDBGrid.scale_volume_grid (lib/grid.py:91-102): every voxel of dst's
+ * allocated leaves inside its resolution gets F.interpolate(trilinear,
+ * align_corners=True) of src's dense values (background outside src's
+ * leaves). src and dst have the same channel count. */
+int pvdb_grid_resample(pvdb_grid src, pvdb_grid dst, pvdb_stream s);
+
+/* Occupancy (mask-cache) builds over the density grid, mask [shape] bytes:
+ *  mode 0  update_occupancy_cache (lib/dvgo.py:200-210): density trilinear at
+ *          the linspace(xyz_min, xyz_max, shape) points, raw2alpha, 3^3 max
+ *          pool, mask &= pooled > thres (fast_color_thres); any shape;
+ *  mode 1  the rebuild after scale_volume_grid (lib/dvgo.py:186-197): shape
+ *          = grid resolution; raw2alpha of the voxel values, 3^3 max pool,
+ *          mask = old_mask lookup at the new grid points & pooled > thres
+ *          (old_mask [old_shape], NULL = all true);
+ *  mode 2  MaskGrid from a checkpoint (lib/grid.py:214-221): shape = grid
+ *          resolution; 3^3 max pool of the voxel values, then
+ *          mask = 1 - exp(-softplus(pooled + act_shift) * interval) >= thres.
+ * Values outside [0, shape) are the pool's padding (ignored). */
+int pvdb_occupancy(pvdb_grid density, int32_t mode, uint8_t* mask, const int32_t shape[3],
+                   const float xyz_min[3], const float xyz_max[3], float act_shift,
+                   float interval, float thres, const uint8_t* old_mask,
+                   const int32_t old_shape[3], pvdb_stream s);
+
+/* maskout_near_cam_vox (lib/dvgo.py:163-175): active voxels whose grid point
+ * (linspace over the resolution) lies within near_clip of any of the camera
+ * centres cam_o [n_cams,3] get `value` (-100 in the reference). */
+int pvdb_grid_maskout_near_cams(pvdb_grid g, const float* cam_o, int32_t n_cams,
+                                const float xyz_min[3], const float xyz_max[3], float near_clip,
+                                float value, pvdb_stream s);
+
+/* voxel_count_views for one view (lib/dvgo.py:212-243): every ray takes
+ * n_samples points t_min + stepdist*k/|d| (stepdist = stepsize*voxel_size),
+ * each point adds its trilinear weights to the voxels it touches (zero
+ * padding), and count [reso] += (sum > 1). acc [reso] is uint64 scratch that
+ * must be zero on entry and is zero again on return (32.32 fixed-point sums:
+ * exact and independent of the order of the atomics). */
+int pvdb_count_views(const float* rays_o, const float* rays_d, int64_t n_rays,
+                     const int32_t reso[3], const float xyz_min[3], const float xyz_max[3],
+                     float near_, float stepdist, int32_t n_samples, uint64_t* acc, float* count,
+                     pvdb_stream s);
+
+/* get_rays_of_a_view (lib/dvgo.py:471-521): rays_o, rays_d, viewdirs [H*W,3]
+ * of a pinhole view, pixels in row-major (h, w) order. K [9] row-major (the
+ * reference's float64 intrinsics), c2w [16] row-major 4x4 (host). mode 0 =
+ * 'center', 1 = 'lefttop', 2 = 'random' with jitter [2][H*W] (device) holding
+ * the uniform offsets of i then j before the flips. ndc applies ndc_rays with
+ * near 1 and focal K[0] to rays_o/rays_d (viewdirs stay those of the pinhole
+ * rays). */
+int pvdb_get_rays(int32_t H, int32_t W, const double K[9], const float c2w[16], int32_t ndc,
+                  int32_t inverse_y, int32_t flip_x, int32_t flip_y, int32_t mode,
+                  const float* jitter, float* rays_o, float* rays_d, float* viewdirs,
+                  pvdb_stream s);
+
+/* hit_coarse_geo (lib/dvgo.py:258-270): hit[r] = 1 when a sample of
+ * sample_pts_on_rays (far = 1e9) inside the bbox lands in a nonzero voxel of
+ * the mask cache mask [shape] (nearest lookup, MaskGrid scale/shift). */
+int pvdb_rays_hit_mask(const float* rays_o, const float* rays_d, int64_t n,
+                       const float xyz_min[3], const float xyz_max[3], float near_,
+                       float stepdist, const uint8_t* mask, const int32_t shape[3], uint8_t* hit,
+                       pvdb_stream s);
+
 #ifdef __cplusplus
 }
 #endif

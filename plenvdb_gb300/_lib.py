@@ -157,6 +157,17 @@ _SIGS = {
     "pvdb_renderer_render": (C.c_int, [vp, i32, vp]),
     "pvdb_renderer_output": (C.c_int, [vp, vp, i32, vp]),
     "pvdb_renderer_views": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    "pvdb_merge_count": (C.c_int, [vp, i64, C.POINTER(i64), vp]),
+    "pvdb_merge_build": (C.c_int, [vp, vp, vp, vp, vp, vp, i64, i32, vp]),
+    "pvdb_compact_rows": (C.c_int, [vp, i64, vp, vp, i32, i64, C.POINTER(i64), vp]),
+    "pvdb_grid_resample": (C.c_int, [vp, vp, vp]),
+    "pvdb_occupancy": (C.c_int, [vp, i32, vp, P_i32, P_f32, P_f32, f32, f32, f32, vp, P_i32,
+                                 vp]),
+    "pvdb_grid_maskout_near_cams": (C.c_int, [vp, vp, i32, P_f32, P_f32, f32, f32, vp]),
+    "pvdb_count_views": (C.c_int, [vp, vp, i64, P_i32, P_f32, P_f32, f32, f32, i32, vp, vp, vp]),
+    "pvdb_get_rays": (C.c_int, [i32, i32, C.POINTER(C.c_double), P_f32, i32, i32, i32, i32, i32,
+                                vp, vp, vp, vp, vp]),
+    "pvdb_rays_hit_mask": (C.c_int, [vp, vp, i64, P_f32, P_f32, f32, f32, vp, P_i32, vp, vp]),
 }
 
 _lib = None
@@ -217,6 +228,14 @@ def i32arr(vals) -> C.Array:
 
 def f32arr(vals) -> C.Array:
     return (C.c_float * len(vals))(*[float(v) for v in vals])
+
+
+def f64arr(vals) -> C.Array:
+    return (C.c_double * len(vals))(*[float(v) for v in vals])
+
+
+def ptrarr(ptrs) -> C.Array:
+    return (C.c_void_p * max(len(ptrs), 1))(*ptrs)
 
 
 def is_cuda(x) -> bool:

@@ -93,6 +93,30 @@ def _grid_info(h):
     return list(reso), ch.value, nleaf.value, nact.value, bg.value
 
 
+def _device_arrays(h, owner):
+    """Zero-copy torch views of a grid handle's device arrays."""
+    d, g, m, t, o = (C.c_void_p() for _ in range(5))
+    ld = (C.c_int32 * 3)()
+    L.call("pvdb_grid_device_views", h, C.byref(d), C.byref(g), C.byref(m), C.byref(t),
+           C.byref(o), ld)
+    _, ch, nleaf, _, _ = _grid_info(h)
+    return {"data": device_view(d.value, (nleaf * 512 * ch,), "float32", owner),
+            "mask": device_view(m.value, (nleaf * 8,), "uint64", owner),
+            "table": device_view(t.value, (ld[0] * ld[1] * ld[2],), "int32", owner),
+            "origin": device_view(o.value, (nleaf * 3,), "int32", owner)}
+
+
+def _same_topology(h0, h1) -> bool:
+    import torch
+    r0, c0, n0, _, _ = _grid_info(h0)
+    r1, c1, n1, _, _ = _grid_info(h1)
+    if (r0, c0, n0) != (r1, c1, n1):
+        return False
+    a, b = _device_arrays(h0, None), _device_arrays(h1, None)
+    return (torch.equal(a["mask"].view(torch.int64), b["mask"].view(torch.int64))
+            and all(torch.equal(a[k], b[k]) for k in ("table", "origin")))
+
+
 class BaseVDB:
     """Common part of DensityVDB / ColorVDB (plenvdb.h:389-429)."""
 
@@ -249,13 +273,29 @@ class BaseVDB:
         L.call("pvdb_grid_zero_grad", self.handle, L.stream_of())
 
     def load_from(self, path: str):
+        """Load values (and topology) saved by save_to. When the file has this
+        grid's topology the values are copied in place, so optimisers created
+        on this grid stay attached (the reference replaces the grid inside the
+        same C++ object, plenvdb.h:143-148); a different topology replaces the
+        grid and is refused while an optimiser holds it."""
         out = C.c_void_p()
         L.call("pvdb_grid_load", str(path).encode(), C.byref(out))
-        reso, ch, _, _, _ = _grid_info(out)
+        new = _GridHandle(out.value)
+        reso, ch, nleaf, _, _ = _grid_info(new.h)
         if ch != self.ndim:
-            L.load().pvdb_grid_destroy(out)
             raise ValueError(f"{path} holds {ch} channels, this grid has {self.ndim}")
-        self._g = _GridHandle(out.value)
+        if reso == self.reso and _same_topology(self.handle, new.h):
+            import torch
+            src = _device_arrays(new.h, new)
+            dst = _device_arrays(self.handle, self)
+            dst["data"].copy_(src["data"])
+            torch.cuda.synchronize()
+            self.mark_written(L.WHICH_DATA)
+            return
+        if any(o() is not None for o in getattr(self, "_opts", [])):
+            raise ValueError(f"{path} has another topology than this grid and an optimiser is "
+                             "attached to it: create the optimiser after loading")
+        self._g = new
         self.reso = reso
 
     def save_to(self, path: str):
@@ -315,6 +355,10 @@ class _BaseOpt:
 
     def __init__(self, vdb: BaseVDB, lr: float, eps: float, beta0: float, beta1: float):
         self.vdb = vdb  # keeps the grid alive (the reference relies on the caller)
+        import weakref
+        if not hasattr(vdb, "_opts"):
+            vdb._opts = []
+        vdb._opts.append(weakref.ref(self))
         out = C.c_void_p()
         L.call("pvdb_opt_create", vdb.handle, float(lr), float(eps), float(beta0), float(beta1),
                C.byref(out))

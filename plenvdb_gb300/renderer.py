@@ -3,6 +3,7 @@ names (plenvdb.h:933-1068, bound at plenvdb.cpp:135-170)."""
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -31,10 +32,16 @@ class MGRenderer:
 
     def load_data(self, den, col, index, N, reso=None, storage: int = 0):
         """load_data(den [N], col [N*dcol], index, N): `index` is a dense int array of
-        row ids [rx,ry,rz] (0 = empty). The reference reads an OpenVDB index grid
-        from a .vdb path here; that format is not supported."""
-        if isinstance(index, (str, bytes)):
-            raise ValueError("an OpenVDB .vdb index path is not supported: pass the dense row-id array")
+        row ids [rx,ry,rz] (0 = empty) or the path of a mergedidxs.npz written by
+        lifecycle.save_merged. The reference reads an OpenVDB index grid from a
+        .vdb path here; that format is not supported."""
+        if isinstance(index, (str, bytes, os.PathLike)):
+            path = os.fsdecode(index)
+            if not path.endswith(".npz"):
+                raise ValueError("OpenVDB .vdb index grids are not supported: pass the dense "
+                                 "row-id array or a mergedidxs.npz from lifecycle.save_merged")
+            from .lifecycle import load_merged_index
+            index = load_merged_index(path)
         idx = np.ascontiguousarray(np.asarray(index), np.int32)
         reso = list(idx.shape) if reso is None else [int(r) for r in reso]
         den = np.ascontiguousarray(np.asarray(den, np.float32).reshape(-1))

@@ -120,3 +120,63 @@ class FineStageTrainer:
         self.ws.n_rays = n
         self.ws.generation += 1
         return self.loss
+
+    # ------------------------------------------------------- checkpoints
+    def save_checkpoint(self, prefix: str, global_step: int = 0) -> str:
+        """Everything a resumed run needs, as run.py:612-630 + VDBAdam.save_to
+        (masked_adam.py:82-95) lay it out beside ``prefix`` (e.g. ``<dir>/fine``):
+        ``<prefix>_last.npz`` (model kwargs, rgbnet parameters, Adam moments and
+        scalars, the voxel optimisers' scalars, global_step),
+        ``<prefix>density.pvdb`` / ``<prefix>color.pvdb`` (the grids) and
+        ``<prefix>density_exp_avg.vdb`` ... (the voxel-Adam moments). Returns
+        the path of the ``_last.npz`` file."""
+        torch.cuda.synchronize()
+        cfg = self.cfg
+        path = prefix + "_last.npz"
+        scal = {}
+        for tag, o in (("d", self.dopt), ("c", self.kopt)):
+            scal.update({tag + "step": o.getStep(), tag + "lr": o.getLr(), tag + "eps": o.getEps(),
+                         tag + "beta0": o.getBeta0(), tag + "beta1": o.getBeta1()})
+        np.savez(path, global_step=np.int64(global_step),
+                 xyz_min=np.array(cfg.xyz_min, np.float32),
+                 xyz_max=np.array(cfg.xyz_max, np.float32),
+                 act_shift=np.float32(cfg.act_shift), voxel_size_ratio=np.float32(cfg.interval),
+                 world_size=np.array(self.density.reso, np.int32),
+                 params=self.params.cpu().numpy(), exp_avg=self.exp_avg.cpu().numpy(),
+                 exp_avg_sq=self.exp_avg_sq.cpu().numpy(), rgbnet_step=np.int32(self._step.value),
+                 rgbnet_lr=np.float32(self._lr.value),
+                 **{k: np.asarray(v) for k, v in scal.items()})
+        self.density.save_to(prefix + "density.pvdb")
+        self.k0.save_to(prefix + "color.pvdb")
+        self.dopt.save_to(prefix + "density_")
+        self.kopt.save_to(prefix + "color_")
+        return path
+
+    def load_checkpoint(self, prefix: str) -> int:
+        """Restores a checkpoint written by save_checkpoint into this trainer
+        (same grid topology and rgbnet shape; values are copied in place, so the
+        captured step graph stays valid). Returns the saved global_step."""
+        st = np.load(prefix + "_last.npz")
+        if st["params"].size != self.params.numel():
+            raise ValueError("the checkpoint's rgbnet has another shape")
+        self.density.load_from(prefix + "density.pvdb")
+        self.k0.load_from(prefix + "color.pvdb")
+        self.dopt.load_from(prefix + "density_")
+        self.kopt.load_from(prefix + "color_")
+        for tag, o in (("d", self.dopt), ("c", self.kopt)):
+            o.setStep(int(st[tag + "step"]))
+            o.setLr(float(st[tag + "lr"]))
+            o.setEps(float(st[tag + "eps"]))
+            o.setBeta0(float(st[tag + "beta0"]))
+            o.setBeta1(float(st[tag + "beta1"]))
+        for t, key in ((self.params, "params"), (self.exp_avg, "exp_avg"),
+                       (self.exp_avg_sq, "exp_avg_sq")):
+            t.copy_(torch.from_numpy(st[key]).to(t.device))
+        self._step.value = int(st["rgbnet_step"])
+        self._lr.value = float(st["rgbnet_lr"])
+        # gradients restart clean, as after a step
+        self.density.zero_grad()
+        self.k0.zero_grad()
+        self.grads.zero_()
+        torch.cuda.synchronize()
+        return int(st["global_step"])

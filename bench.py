@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 320^3 / 65536-ray training measurement")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-lifecycle", action="store_true",
+                    help="skip the timings of the steps around the training step")
+    ap.add_argument("--lifecycle-only", action="store_true",
+                    help="only the lifecycle timings (for profiling their kernels)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the fused step eagerly instead of replaying a CUDA graph")
@@ -257,6 +261,8 @@ def run_ours(args):
     render = None if args.no_render else run_render(scfg, cfg, cam, tr, args)
     # ---------------- BF16 vs FP32 quality after training from one seed
     psnr = run_psnr(scfg, cfg, cam, args.psnr_iters) if args.psnr_iters > 0 else None
+    # ---------------- the steps around the training step (lifecycle)
+    life = None if args.no_lifecycle else run_lifecycle(scfg, cfg, cam, tr)
     # ---------------- 320^3 grid, 65536 rays per step
     large = None if args.no_large else run_large(args)
     out = None
@@ -284,6 +290,8 @@ def run_ours(args):
             out["psnr"] = psnr
         if large:
             out["large"] = large
+        if life:
+            out["lifecycle"] = life
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(scfg, cfg, ro, rd, vd, tgt)
         print(json.dumps(out), flush=True)
@@ -637,6 +645,162 @@ def cpu_baseline(scfg, cfg, ro, rd, vd, tgt, budget_s=20.0):
                       f"to one {RAYS}-ray iteration"}
 
 
+def _hbm_peak():
+    import json as _json
+    try:
+        return float(_json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), \
+            "MEASURED_PEAKS.json (of measured)"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _time_op(fn, reps=5, warmup=2):
+    """Mean device time (ms) of fn() over reps calls, CUDA events on the
+    current stream after warm-up calls."""
+    import torch
+    st = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        fn()
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def _cpu_ms(fn, budget_s=3.0):
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        fn()
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 5:
+            break
+    return (time.perf_counter() - t0) / n * 1e3
+
+
+def run_lifecycle(scfg, cfg, cam, tr):
+    """The steps around the training step at the 160^3 workload: device time
+    of each (CUDA events, mean of 5 after 2 warm-up calls), its algorithmic
+    bytes and the fraction of the measured HBM bandwidth, and the oracle's CPU
+    time on the same input (or a stated sample)."""
+    import torch
+
+    from oracle import lifecycle as OL
+    from oracle import oracle as O
+    from plenvdb_gb300 import _lib as L
+    from plenvdb_gb300 import lifecycle as LC
+    from plenvdb_gb300 import rays as RY
+    from plenvdb_gb300.plenvdb import ColorVDB, DensityVDB
+    from plenvdb_gb300.scene import scene_mask, sphere_poses
+    peak, peak_src = _hbm_peak()
+    R = scfg.reso
+    nvox = R ** 3
+    res = {"peak_gbs": peak, "peak_source": peak_src}
+
+    def entry(ms, nbytes, cpu_ms=None, sample=None, extra=None):
+        e = {"ms": ms, "bytes": int(nbytes), "gbs": nbytes / ms / 1e6,
+             "frac": nbytes / ms / 1e6 / peak}
+        if cpu_ms is not None:
+            e["cpu_ms"] = cpu_ms
+            e["cpu_sample"] = sample
+        e.update(extra or {})
+        return e
+
+    mask_np = scene_mask(scfg).astype(bool)
+    mask = torch.from_numpy(mask_np).cuda()
+    # merged compression (FP16 rows), vdb_compression.py
+    n_rows = int(mask_np.sum()) + 1
+    ms = _time_op(lambda: LC.merge_compress(tr.density, tr.k0, mask))
+    dd = tr.density.get_dense_grid().reshape(R, R, R)
+    kd = tr.k0.get_dense_grid().reshape(R, R, R, 12)
+    cms = _cpu_ms(lambda: OL.merge(dd, kd, mask_np))
+    res["merge_compress"] = entry(ms, nvox * (1 + 4) + (n_rows - 1) * (4 + 48 + 2 + 24), cms,
+                                  "the whole grid (numpy, 1 thread)",
+                                  {"rows": n_rows, "note": "three mask passes (count, "
+                                   "rank+write, the caller's count); bytes count one"})
+    # progressive rescaling 80^3 -> 160^3 (scale_volume_grid), density and k0
+    half = R // 2
+    rng = np.random.default_rng(0)
+    for C, name in ((1, "rescale_density"), (12, "rescale_k0")):
+        src = DensityVDB([half] * 3, 1) if C == 1 else ColorVDB([half] * 3, C)
+        vals = rng.normal(0, 1, half ** 3 * C).astype(np.float32)
+        src.copyFromDense(vals)
+        dst = DensityVDB([R] * 3, 1) if C == 1 else ColorVDB([R] * 3, C)
+        ms = _time_op(lambda: L.call("pvdb_grid_resample", src.handle, dst.handle,
+                                     L.stream_of()))
+        if C == 1:
+            cms = _cpu_ms(lambda: OL.resample(vals.reshape(half, half, half, 1), [R] * 3))
+            sample = "the whole grid (numpy, 1 thread)"
+        else:
+            cms = _cpu_ms(lambda: OL.resample(vals.reshape(half, half, half, C)[..., :1],
+                                              [R] * 3)) * C
+            sample = "one of the 12 channels (numpy, 1 thread), time x12"
+        res[name] = entry(ms, (nvox + half ** 3) * C * 4, cms, sample)
+        del src, dst
+    # update_occupancy_cache on the 160^3 mask cache
+    mc = LC.MaskGrid(mask=mask.clone(), xyz_min=cfg.xyz_min, xyz_max=cfg.xyz_max)
+    ms = _time_op(lambda: LC.update_occupancy_cache(mc, tr.density, cfg.act_shift, cfg.interval,
+                                                    cfg.fast_color_thres))
+    og = O.OGridData((R,) * 3, dd.astype(np.float64), mask_np.astype(np.uint8),
+                     background=scfg.background)
+    cms = _cpu_ms(lambda: OL.occupancy(0, og, (R,) * 3, cfg.xyz_min, cfg.xyz_max, cfg.act_shift,
+                                       cfg.interval, cfg.fast_color_thres, mask=mask_np),
+                  budget_s=1.0)
+    res["occupancy_update"] = entry(ms, nvox * (4 + 1 + 1), cms,
+                                    "the whole grid (trilinear in the C oracle, OpenMP; "
+                                    "pooling in numpy)")
+    # rays of an 800x800 view, the in-mask-cache hit test and the compaction
+    pose = sphere_poses(1, cam.radius, seed=5)[0]
+    K = np.asarray(cam.K, np.float64)
+    H, W = cam.H, cam.W
+    ms = _time_op(lambda: RY.get_rays_of_a_view(H, W, K, pose, False, False, False, False))
+    cms = _cpu_ms(lambda: OL.get_rays(H, W, K, pose, False, False, False))
+    res["get_rays"] = entry(ms, H * W * 36, cms, "the whole view (numpy, 1 thread)",
+                            {"rays_per_s": H * W / ms * 1e3})
+    o, d, v = RY.get_rays_of_a_view(H, W, K, pose, False, False, False, False)
+    model = {"xyz_min": cfg.xyz_min, "xyz_max": cfg.xyz_max, "voxel_size": cfg.voxel_size}
+    ms = _time_op(lambda: RY.hit_coarse_geo(o, d, cam.near, 1e9, cfg.stepsize, mask_cache=mc,
+                                            **model))
+    on, dn = o.cpu().numpy().reshape(-1, 3), d.cpu().numpy().reshape(-1, 3)
+    n_cpu = 20000
+    stepdist = float(np.float32(cfg.stepsize) * np.float32(cfg.voxel_size))
+    cms = _cpu_ms(lambda: OL.hit_coarse_geo(on[:n_cpu], dn[:n_cpu], cfg.xyz_min, cfg.xyz_max,
+                                            cam.near, stepdist, mc.mask.cpu().numpy()),
+                  budget_s=2.0) * (H * W / n_cpu)
+    hit = RY.hit_coarse_geo(o, d, cam.near, 1e9, cfg.stepsize, mask_cache=mc, **model)
+    res["hit_coarse_geo"] = entry(ms, H * W * 25, cms,
+                                  f"{n_cpu} of the {H * W} rays (C oracle), time scaled",
+                                  {"rays_per_s": H * W / ms * 1e3,
+                                   "hit_fraction": float(hit.float().mean())})
+    rgb = torch.rand(H * W, 3, device="cuda")
+    ms = _time_op(lambda: RY._compact(hit, [o, d, v, rgb], H * W))
+    kept = int(hit.sum())
+    res["compact_rays"] = entry(ms, H * W + kept * 4 * 12 * 2)
+    # voxel_count_views: one view at 200x200 rays (downrate 4)
+    ro4 = o[::4, ::4].contiguous()
+    rd4 = d[::4, ::4].contiguous()
+    ws = [R] * 3
+    ms = _time_op(lambda: LC.voxel_count_views(ro4[None], rd4[None], [1], cam.near, 1e9,
+                                               cfg.stepsize, ws, cfg.voxel_size, cfg.xyz_min,
+                                               cfg.xyz_max), reps=3, warmup=1)
+    n_samples = int(np.linalg.norm(np.array(ws) + 1) / cfg.stepsize) + 1
+    pts = ro4.shape[0] * ro4.shape[1] * n_samples
+    ro_np, rd_np = ro4.cpu().numpy().reshape(-1, 3), rd4.cpu().numpy().reshape(-1, 3)
+    n_cpu = 500
+    cms = _cpu_ms(lambda: OL.view_weight_sums(ro_np[:n_cpu], rd_np[:n_cpu], ws, cfg.xyz_min,
+                                              cfg.xyz_max, cam.near, stepdist, n_samples),
+                  budget_s=2.0) * (ro_np.shape[0] / n_cpu)
+    res["count_views"] = entry(ms, nvox * 8 * 2 + nvox * 4 * 2, cms,
+                               f"{n_cpu} of the {ro_np.shape[0]} rays (numpy), time scaled",
+                               {"points_per_s": pts / ms * 1e3, "points": pts,
+                                "bound": "atomics: 8 per point"})
+    return res
+
+
 def run_reference(args):
     ws_, rank, local = dist_info()
     if rank != 0:
@@ -685,6 +849,20 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.lifecycle_only:
+        import torch
+
+        from plenvdb_gb300 import _lib as L
+        from plenvdb_gb300.scene import CameraConfig, SceneConfig, build_grids
+        from plenvdb_gb300.trainer import FineStageConfig
+        L.load()
+        scfg = SceneConfig(reso=RESO, n_ellipsoids=8, seed=0)
+        cfg = FineStageConfig(reso=RESO)
+        dg, kg = build_grids(scfg)
+        grids = type("Grids", (), {"density": dg, "k0": kg})()
+        print(json.dumps({"lifecycle": run_lifecycle(scfg, cfg, CameraConfig(), grids)}),
+              flush=True)
+        torch.cuda.synchronize()
     else:
         run_ours(args)
 

@@ -12,6 +12,7 @@
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "ray_ops.cuh"
 
@@ -67,13 +68,57 @@ struct MergeArgs {
   int32_t* index;
   void* den_rows;
   void* col_rows;
-  int dtype;  // 0 FP32 rows, 1 FP16 rows
-  int vec;    // mask and index are 16-byte aligned
+  int dtype;    // 0 FP32 rows, 1 FP16 rows
+  int vec;      // mask and index are 16-byte aligned
+  int col_vec;  // colour rows aligned for whole-row vector stores
 };
 
 __device__ __forceinline__ void put_row(void* rows, int64_t i, int dtype, float v) {
   if (dtype == 1) reinterpret_cast<__half*>(rows)[i] = __float2half_rn(v);
   else reinterpret_cast<float*>(rows)[i] = v;
+}
+
+// Row r of the colour rows: the voxel's C channels (background outside the
+// leaves). C == 12 with aligned rows moves 16-byte loads and 16-/8-byte stores.
+__device__ __forceinline__ void put_col_row(const MergeArgs& a, int64_t r, int x, int y, int z) {
+  const int s = slot_of(a.col, x, y, z);
+  const int C = a.col.C;
+  if (C == 12 && a.col_vec) {
+    float v[12];
+    if (s < 0) {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) v[c] = a.col.background;
+    } else {
+      const float4* src = reinterpret_cast<const float4*>(a.col.data + int64_t(s) * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float4 w = __ldg(src + b);
+        v[4 * b] = w.x;
+        v[4 * b + 1] = w.y;
+        v[4 * b + 2] = w.z;
+        v[4 * b + 3] = w.w;
+      }
+    }
+    if (a.dtype == 1) {
+      uint2* dst = reinterpret_cast<uint2*>(reinterpret_cast<__half*>(a.col_rows) + r * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const __half2 lo = __floats2half2_rn(v[4 * b], v[4 * b + 1]);
+        const __half2 hi = __floats2half2_rn(v[4 * b + 2], v[4 * b + 3]);
+        dst[b] = make_uint2(*reinterpret_cast<const uint32_t*>(&lo),
+                            *reinterpret_cast<const uint32_t*>(&hi));
+      }
+    } else {
+      float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(a.col_rows) + r * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        dst[b] = make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
+    }
+    return;
+  }
+  for (int ch = 0; ch < C; ++ch)
+    put_row(a.col_rows, r * C + ch, a.dtype,
+            s < 0 ? a.col.background : __ldg(a.col.data + int64_t(s) * C + ch));
 }
 
 // Rank of this thread's first flagged voxel among all flagged voxels (block
@@ -122,24 +167,26 @@ __global__ void __launch_bounds__(kMergeThreads)
       for (int ch = 0; ch < a.col.C; ++ch) put_row(a.col_rows, ch, a.dtype, 0.f);
   }
   if (!f) return;
+  // coordinates of the chunk's first voxel, then stepped along z (C order)
   const int64_t yz = int64_t(a.reso[1]) * a.reso[2];
+  int x = int(base / yz);
+  const int64_t rem = base - int64_t(x) * yz;
+  int y = int(rem / a.reso[2]);
+  int z = int(rem - int64_t(y) * a.reso[2]);
   r = row0;
   for (int q = 0; q < kMergeVox; ++q) {
-    if (!((f >> q) & 1u)) continue;
-    const int64_t v = base + q;
-    const int x = int(v / yz);
-    const int64_t rem = v - int64_t(x) * yz;
-    const int y = int(rem / a.reso[2]);
-    const int z = int(rem - int64_t(y) * a.reso[2]);
-    if (a.has_den) put_row(a.den_rows, r, a.dtype, value1(a.den, x, y, z));
-    if (a.has_col) {
-      const int s = slot_of(a.col, x, y, z);
-      const int C = a.col.C;
-      for (int ch = 0; ch < C; ++ch)
-        put_row(a.col_rows, r * C + ch, a.dtype,
-                s < 0 ? a.col.background : __ldg(a.col.data + int64_t(s) * C + ch));
+    if ((f >> q) & 1u) {
+      if (a.has_den) put_row(a.den_rows, r, a.dtype, value1(a.den, x, y, z));
+      if (a.has_col) put_col_row(a, r, x, y, z);
+      ++r;
     }
-    ++r;
+    if (++z == a.reso[2]) {
+      z = 0;
+      if (++y == a.reso[1]) {
+        y = 0;
+        ++x;
+      }
+    }
   }
 }
 
@@ -211,9 +258,44 @@ __global__ void k_resample(GridView src, GridView dst, AxisMap m) {
   axis_weights(m.scale[1], m.in[1], y, yi[0], yi[1], yw[0], yw[1]);
   axis_weights(m.scale[2], m.in[2], z, zi[0], zi[1], zw[0], zw[1]);
   int s[8];
+  if ((xi[0] >> 3) == (xi[1] >> 3) && (yi[0] >> 3) == (yi[1] >> 3) &&
+      (zi[0] >> 3) == (zi[1] >> 3)) {
+    // all 8 corners in the low corner's leaf: one table lookup
+    const int l = leaf_of(src, xi[0], yi[0], zi[0]);
+    const int b = l < 0 ? -1 : ((l << 9) | vox_offset(xi[0], yi[0], zi[0]));
+    const int dx = (xi[1] - xi[0]) << 6, dy = (yi[1] - yi[0]) << 3, dz = zi[1] - zi[0];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) s[c] = slot_of(src, xi[c >> 2], yi[(c >> 1) & 1], zi[c & 1]);
+    for (int c = 0; c < 8; ++c)
+      s[c] = b < 0 ? -1 : b + ((c >> 2) ? dx : 0) + (((c >> 1) & 1) ? dy : 0) + ((c & 1) ? dz : 0);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s[c] = slot_of(src, xi[c >> 2], yi[(c >> 1) & 1], zi[c & 1]);
+  }
   const int C = dst.C;
+  if ((C & 3) == 0) {
+    float4* out = reinterpret_cast<float4*>(dst.data + slot * C);
+    const float4 bg = make_float4(src.background, src.background, src.background, src.background);
+    for (int q = 0; q < C / 4; ++q) {
+      float4 v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        v[c] = s[c] < 0 ? bg : __ldg(reinterpret_cast<const float4*>(src.data + int64_t(s[c]) * C) + q);
+      float r[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        float w[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) w[c] = e == 0 ? v[c].x : e == 1 ? v[c].y : e == 2 ? v[c].z : v[c].w;
+        const float y0 = lerp2(lerp2(w[0], zw[0], w[1], zw[1]), yw[0],
+                               lerp2(w[2], zw[0], w[3], zw[1]), yw[1]);
+        const float y1 = lerp2(lerp2(w[4], zw[0], w[5], zw[1]), yw[0],
+                               lerp2(w[6], zw[0], w[7], zw[1]), yw[1]);
+        r[e] = lerp2(y0, xw[0], y1, xw[1]);
+      }
+      out[q] = make_float4(r[0], r[1], r[2], r[3]);
+    }
+    return;
+  }
   float* out = dst.data + slot * C;
   for (int ch = 0; ch < C; ++ch) {
     float v[8];
@@ -225,6 +307,62 @@ __global__ void k_resample(GridView src, GridView dst, AxisMap m) {
     const float y1 = lerp2(lerp2(v[4], zw[0], v[5], zw[1]), yw[0], lerp2(v[6], zw[0], v[7], zw[1]),
                            yw[1]);
     out[ch] = lerp2(y0, xw[0], y1, xw[1]);
+  }
+}
+
+// Scalar grids: one thread per 8-voxel z column of a destination leaf. The
+// x/y weights and the table rows of the four (x, y) source corners are formed
+// once per column; per z only the z weights, one table load per corner and
+// the values remain.
+__global__ void __launch_bounds__(256) k_resample_col(GridView src, GridView dst, AxisMap m) {
+  const int64_t col = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (col >= int64_t(dst.nleaf) * 64) return;
+  const int l = int(col >> 6), xy = int(col & 63);
+  const int x = __ldg(dst.origin + 3 * l) + (xy >> 3);
+  const int y = __ldg(dst.origin + 3 * l + 1) + (xy & 7);
+  const int zb = __ldg(dst.origin + 3 * l + 2);
+  if (x >= dst.reso[0] || y >= dst.reso[1]) return;
+  int xi[2], yi[2];
+  float xw[2], yw[2];
+  axis_weights(m.scale[0], m.in[0], x, xi[0], xi[1], xw[0], xw[1]);
+  axis_weights(m.scale[1], m.in[1], y, yi[0], yi[1], yw[0], yw[1]);
+  // per (x, y) corner: the table row (-1 outside the table) and the in-leaf offset
+  int trow[4], xyoff[4];
+  const int lx = src.ldim[0] << 3, ly = src.ldim[1] << 3;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int i = xi[c >> 1], j = yi[c & 1];
+    trow[c] = ((unsigned)i < (unsigned)lx && (unsigned)j < (unsigned)ly)
+                  ? ((i >> 3) * src.ldim[1] + (j >> 3)) * src.ldim[2]
+                  : -1;
+    xyoff[c] = ((i & 7) << 6) | ((j & 7) << 3);
+  }
+  const int lz = src.ldim[2] << 3;
+  float* out = dst.data + ((int64_t(l) << 9) | (xy << 3));
+  for (int dz = 0; dz < 8; ++dz) {
+    const int z = zb + dz;
+    if (z >= dst.reso[2]) break;
+    int zi[2];
+    float zw[2];
+    axis_weights(m.scale[2], m.in[2], z, zi[0], zi[1], zw[0], zw[1]);
+    int sl[8];  // corner c = 4*xbit + 2*ybit + zbit
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int k = zi[e];
+        int leaf = -1;
+        if (trow[c] >= 0 && (unsigned)k < (unsigned)lz) leaf = __ldg(src.table + trow[c] + (k >> 3));
+        sl[2 * c + e] = leaf < 0 ? -1 : ((leaf << 9) | xyoff[c] | (k & 7));
+      }
+    float v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = sl[c] < 0 ? src.background : __ldg(src.data + sl[c]);
+    const float y0 = lerp2(lerp2(v[0], zw[0], v[1], zw[1]), yw[0],
+                           lerp2(v[2], zw[0], v[3], zw[1]), yw[1]);
+    const float y1 = lerp2(lerp2(v[4], zw[0], v[5], zw[1]), yw[0],
+                           lerp2(v[6], zw[0], v[7], zw[1]), yw[1]);
+    out[dz] = lerp2(y0, xw[0], y1, xw[1]);
   }
 }
 
@@ -269,32 +407,54 @@ __global__ void __launch_bounds__(512) k_occupancy(OccArgs a) {
   const int tz = blockIdx.x % tiles_z, ty = (blockIdx.x / tiles_z) % tiles_y,
             tx = blockIdx.x / (tiles_z * tiles_y);
   const int x0 = tx * kOccTile - 1, y0 = ty * kOccTile - 1, z0 = tz * kOccTile - 1;
+  const int lx = threadIdx.x >> 6, ly = (threadIdx.x >> 3) & 7, lz = threadIdx.x & 7;
+  const int i = x0 + 1 + lx, j = y0 + 1 + ly, k = z0 + 1 + lz;
+  const bool inside = i < a.shape[0] && j < a.shape[1] && k < a.shape[2];
+  const int64_t o = (int64_t(i) * a.shape[1] + j) * a.shape[2] + k;
+  // the pooled value only matters where the other operand of the & is set:
+  // mode 0 the mask itself, mode 1 the old mask at the grid point
+  bool need = inside;
+  if (inside && a.mode == 0) {
+    need = a.out[o] != 0;
+  } else if (inside && a.mode == 1 && a.old_mask) {
+    const float p[3] = {linspace_at(a.lin_start[0], a.lin_end[0], a.lin_step[0], a.shape[0], i),
+                        linspace_at(a.lin_start[1], a.lin_end[1], a.lin_step[1], a.shape[1], j),
+                        linspace_at(a.lin_start[2], a.lin_end[2], a.lin_step[2], a.shape[2], k)};
+    need = mask_lookup(a.old_mask, a.old_shape, p, a.old_scale, a.old_shift);
+  }
+  if (!__syncthreads_or(need)) {
+    if (inside && a.mode == 1) a.out[o] = 0;  // mode 0 leaves the zeros as they are
+    return;
+  }
   for (int e = threadIdx.x; e < kOccHalo * kOccHalo * kOccHalo; e += blockDim.x) {
     const int hx = e / (kOccHalo * kOccHalo), hy = (e / kOccHalo) % kOccHalo, hz = e % kOccHalo;
-    const int i = x0 + hx, j = y0 + hy, k = z0 + hz;
+    const int ii = x0 + hx, jj = y0 + hy, kk = z0 + hz;
     float v = -INFINITY;
-    if (i >= 0 && j >= 0 && k >= 0 && i < a.shape[0] && j < a.shape[1] && k < a.shape[2]) {
+    if (ii >= 0 && jj >= 0 && kk >= 0 && ii < a.shape[0] && jj < a.shape[1] && kk < a.shape[2]) {
       if (a.mode == 0) {
-        const float p[3] = {linspace_at(a.lin_start[0], a.lin_end[0], a.lin_step[0], a.shape[0], i),
-                            linspace_at(a.lin_start[1], a.lin_end[1], a.lin_step[1], a.shape[1], j),
-                            linspace_at(a.lin_start[2], a.lin_end[2], a.lin_step[2], a.shape[2], k)};
+        const float p[3] = {
+            linspace_at(a.lin_start[0], a.lin_end[0], a.lin_step[0], a.shape[0], ii),
+            linspace_at(a.lin_start[1], a.lin_end[1], a.lin_step[1], a.shape[1], jj),
+            linspace_at(a.lin_start[2], a.lin_end[2], a.lin_step[2], a.shape[2], kk)};
         float idx[3];
         world_to_index(p, a.lin_start, a.ext, a.wsm1, idx);
         float e_;
         v = raw2alpha(trilinear1(a.den, idx[0], idx[1], idx[2]), a.shift, a.interval, e_);
       } else if (a.mode == 1) {
         float e_;
-        v = raw2alpha(value1(a.den, i, j, k), a.shift, a.interval, e_);
+        v = raw2alpha(value1(a.den, ii, jj, kk), a.shift, a.interval, e_);
       } else {
-        v = value1(a.den, i, j, k);
+        v = value1(a.den, ii, jj, kk);
       }
     }
     val[e] = v;
   }
   __syncthreads();
-  const int lx = threadIdx.x >> 6, ly = (threadIdx.x >> 3) & 7, lz = threadIdx.x & 7;
-  const int i = x0 + 1 + lx, j = y0 + 1 + ly, k = z0 + 1 + lz;
-  if (i >= a.shape[0] || j >= a.shape[1] || k >= a.shape[2]) return;
+  if (!inside) return;
+  if (!need) {
+    if (a.mode == 1) a.out[o] = 0;
+    return;
+  }
   float m = -INFINITY;
 #pragma unroll
   for (int dx = 0; dx < 3; ++dx)
@@ -303,22 +463,9 @@ __global__ void __launch_bounds__(512) k_occupancy(OccArgs a) {
 #pragma unroll
       for (int dz = 0; dz < 3; ++dz)
         m = fmaxf(m, val[((lx + dx) * kOccHalo + (ly + dy)) * kOccHalo + (lz + dz)]);
-  const int64_t o = (int64_t(i) * a.shape[1] + j) * a.shape[2] + k;
   uint8_t r;
-  if (a.mode == 0) {
-    r = (a.out[o] != 0) & (m > a.thres);
-  } else if (a.mode == 1) {
-    bool keep = m > a.thres;
-    if (keep && a.old_mask) {
-      const float p[3] = {linspace_at(a.lin_start[0], a.lin_end[0], a.lin_step[0], a.shape[0], i),
-                          linspace_at(a.lin_start[1], a.lin_end[1], a.lin_step[1], a.shape[1], j),
-                          linspace_at(a.lin_start[2], a.lin_end[2], a.lin_step[2], a.shape[2], k)};
-      keep = mask_lookup(a.old_mask, a.old_shape, p, a.old_scale, a.old_shift);
-    }
-    r = keep;
-  } else {
-    r = softplus_alpha(m + a.shift, a.interval) >= a.thres;
-  }
+  if (a.mode == 0 || a.mode == 1) r = m > a.thres;
+  else r = softplus_alpha(m + a.shift, a.interval) >= a.thres;
   a.out[o] = r;
 }
 
@@ -445,29 +592,49 @@ void linspace_params(const float mn[3], const float mx[3], const int shape[3], f
   }
 }
 
-int merge_counts(const uint8_t* mask, int64_t n, int vec, uint32_t** cnt, uint32_t** off,
-                 uint32_t** total, uint32_t** partial, size_t* partial_cap, int64_t* nblocks,
-                 cudaStream_t st) {
-  *nblocks = (n + kMergeBlockVox - 1) / kMergeBlockVox;
-  int rc = dev_alloc((void**)cnt, size_t(*nblocks) * 4);
-  if (!rc) rc = dev_alloc((void**)off, size_t(*nblocks) * 4);
-  if (!rc) rc = dev_alloc((void**)total, 4);
-  if (rc) return rc;
-  k_merge_count<<<int(*nblocks), kMergeThreads, 0, st>>>(mask, n, vec, *cnt);
-  PVDB_CHECK_LAUNCH("k_merge_count");
-  return scan_exclusive_u32(*cnt, *off, *nblocks, *total, partial, partial_cap, st);
+// Scratch of the counting passes, kept for the process (grown, never shrunk):
+// every call that uses it synchronises its stream before returning and holds
+// the lock meanwhile, so calls from several threads take turns.
+struct MergeScratch {
+  std::mutex mu;
+  int device = -1;
+  uint32_t *cnt = nullptr, *off = nullptr, *total = nullptr, *partial = nullptr;
+  size_t cnt_cap = 0, off_cap = 0, total_cap = 0, partial_cap = 0;
+};
+
+MergeScratch& merge_scratch() {
+  static MergeScratch* s = new MergeScratch();
+  return *s;
 }
 
-struct MergeScratch {
-  uint32_t *cnt = nullptr, *off = nullptr, *total = nullptr, *partial = nullptr;
-  size_t partial_cap = 0;
-  ~MergeScratch() {
-    dev_free(cnt);
-    dev_free(off);
-    dev_free(total);
-    dev_free(partial);
+// Counts and block offsets of mask (device scalar total), in the scratch.
+int merge_pass(MergeScratch& m, const uint8_t* mask, int64_t n, int vec, int64_t* nblocks,
+               cudaStream_t st) {
+  int dev = 0;
+  PVDB_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev != m.device) {
+    for (uint32_t** p : {&m.cnt, &m.off, &m.total, &m.partial}) {
+      dev_free(*p);
+      *p = nullptr;
+    }
+    m.cnt_cap = m.off_cap = m.total_cap = m.partial_cap = 0;
+    m.device = dev;
   }
-};
+  *nblocks = (n + kMergeBlockVox - 1) / kMergeBlockVox;
+  int rc = dev_reserve((void**)&m.cnt, &m.cnt_cap, size_t(*nblocks) * 4);
+  if (!rc) rc = dev_reserve((void**)&m.off, &m.off_cap, size_t(*nblocks) * 4);
+  if (!rc) rc = dev_reserve((void**)&m.total, &m.total_cap, 4);
+  if (rc) return rc;
+  k_merge_count<<<int(*nblocks), kMergeThreads, 0, st>>>(mask, n, vec, m.cnt);
+  PVDB_CHECK_LAUNCH("k_merge_count");
+  return scan_exclusive_u32(m.cnt, m.off, *nblocks, m.total, &m.partial, &m.partial_cap, st);
+}
+
+int merge_total(MergeScratch& m, cudaStream_t st, uint32_t* h) {
+  PVDB_CHECK_CUDA(cudaMemcpyAsync(h, m.total, 4, cudaMemcpyDeviceToHost, st));
+  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  return PVDB_OK;
+}
 
 }  // namespace
 
@@ -480,15 +647,14 @@ int pvdb_merge_count(const uint8_t* mask, int64_t n, int64_t* n_active, pvdb_str
   if (!n) return PVDB_OK;
   PVDB_REQUIRE(mask, "null mask");
   cudaStream_t st = as_stream(s);
-  MergeScratch m;
+  MergeScratch& m = merge_scratch();
+  std::lock_guard<std::mutex> lk(m.mu);
   int64_t nb = 0;
   const int vec = (reinterpret_cast<uintptr_t>(mask) & 15) == 0;
-  int rc = merge_counts(mask, n, vec, &m.cnt, &m.off, &m.total, &m.partial, &m.partial_cap, &nb,
-                        st);
-  if (rc) return rc;
+  int rc = merge_pass(m, mask, n, vec, &nb, st);
   uint32_t h = 0;
-  PVDB_CHECK_CUDA(cudaMemcpyAsync(&h, m.total, 4, cudaMemcpyDeviceToHost, st));
-  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (!rc) rc = merge_total(m, st, &h);
+  if (rc) return rc;
   *n_active = h;
   return PVDB_OK;
 }
@@ -508,16 +674,15 @@ int pvdb_merge_build(pvdb_grid density, pvdb_grid color, const uint8_t* mask, in
       PVDB_REQUIRE(density->reso[q] == color->reso[q], "density and color resolutions differ");
   const int64_t n = int64_t(ref->reso[0]) * ref->reso[1] * ref->reso[2];
   cudaStream_t st = as_stream(s);
-  MergeScratch m;
+  MergeScratch& m = merge_scratch();
+  std::lock_guard<std::mutex> lk(m.mu);
   int64_t nb = 0;
   const int vec = (reinterpret_cast<uintptr_t>(mask) & 15) == 0 &&
                   (reinterpret_cast<uintptr_t>(index) & 15) == 0;
-  int rc = merge_counts(mask, n, vec, &m.cnt, &m.off, &m.total, &m.partial, &m.partial_cap, &nb,
-                        st);
-  if (rc) return rc;
+  int rc = merge_pass(m, mask, n, vec, &nb, st);
   uint32_t h = 0;
-  PVDB_CHECK_CUDA(cudaMemcpyAsync(&h, m.total, 4, cudaMemcpyDeviceToHost, st));
-  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (!rc) rc = merge_total(m, st, &h);
+  if (rc) return rc;
   // the row buffers are sized by the caller: check before anything is written
   PVDB_REQUIRE(n_rows == int64_t(h) + 1, "n_rows must be the number of masked voxels + 1");
   MergeArgs a;
@@ -532,6 +697,7 @@ int pvdb_merge_build(pvdb_grid density, pvdb_grid color, const uint8_t* mask, in
   a.col_rows = col_rows;
   a.dtype = row_dtype;
   a.vec = vec;
+  a.col_vec = (reinterpret_cast<uintptr_t>(col_rows) & (row_dtype == 1 ? 7 : 15)) == 0;
   k_merge_write<<<int(nb), kMergeThreads, 0, st>>>(mask, n, m.off, a);
   PVDB_CHECK_LAUNCH("k_merge_write");
   PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -555,14 +721,13 @@ int pvdb_compact_rows(const uint8_t* keep, int64_t n, const float* const* src, f
   }
   a.vec = (reinterpret_cast<uintptr_t>(keep) & 15) == 0;
   cudaStream_t st = as_stream(s);
-  MergeScratch m;
+  MergeScratch& m = merge_scratch();
+  std::lock_guard<std::mutex> lk(m.mu);
   int64_t nb = 0;
-  int rc = merge_counts(keep, n, a.vec, &m.cnt, &m.off, &m.total, &m.partial, &m.partial_cap, &nb,
-                        st);
-  if (rc) return rc;
+  int rc = merge_pass(m, keep, n, a.vec, &nb, st);
   uint32_t h = 0;
-  PVDB_CHECK_CUDA(cudaMemcpyAsync(&h, m.total, 4, cudaMemcpyDeviceToHost, st));
-  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (!rc) rc = merge_total(m, st, &h);
+  if (rc) return rc;
   // the destination rows are sized by the caller: check before anything is written
   PVDB_REQUIRE(int64_t(h) <= cap, "destination arrays hold fewer rows than the kept count");
   *n_kept = h;
@@ -585,7 +750,14 @@ int pvdb_grid_resample(pvdb_grid src, pvdb_grid dst, pvdb_stream s) {
   }
   const int64_t n = dst->nslots();
   if (n) {
-    k_resample<<<ceil_div(n, 256), 256, 0, as_stream(s)>>>(src->view(), dst->view(), m);
+    const int64_t cols = int64_t(dst->nleaf) * 64;
+    // one channel: a thread per z column; wider voxels: a thread per voxel
+    // (per-thread columns of 48-byte rows lose memory parallelism)
+    if (dst->C == 1) {
+      k_resample_col<<<ceil_div(cols, 256), 256, 0, as_stream(s)>>>(src->view(), dst->view(), m);
+    } else {
+      k_resample<<<ceil_div(n, 256), 256, 0, as_stream(s)>>>(src->view(), dst->view(), m);
+    }
     PVDB_CHECK_LAUNCH("k_resample");
   }
   dst->bmax_valid = false;

@@ -635,6 +635,49 @@ __device__ __forceinline__ float corner_scale(float u, float v, float w, int c) 
 // Thread per voxel of the listed (touched) leaves of grid g; adds the density
 // sum to grad_d and/or the k0 sums to grad_c (C channels). NQ = the number of
 // float4 chunks of the k0 gradient (0 = density only).
+// A kept sample's k0-gradient row (NQ float4), zero when it has none.
+template <int NQ>
+__device__ __forceinline__ void gather_row(const float* __restrict__ gk0, int32_t row, int C,
+                                           int vec, float4* q) {
+#pragma unroll
+  for (int b = 0; b < NQ; ++b) {
+    if (row < 0) {
+      q[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    const float* gr = gk0 + int64_t(row) * C;
+    if (vec) {
+      q[b] = __ldg(reinterpret_cast<const float4*>(gr) + b);
+    } else {
+      q[b].x = __ldg(gr + 4 * b);
+      q[b].y = 4 * b + 1 < C ? __ldg(gr + 4 * b + 1) : 0.f;
+      q[b].z = 4 * b + 2 < C ? __ldg(gr + 4 * b + 2) : 0.f;
+      q[b].w = 4 * b + 3 < C ? __ldg(gr + 4 * b + 3) : 0.f;
+    }
+  }
+}
+
+// Adds one sample's contribution to corner c of its cell: the density term
+// (when the grid takes one and the sample's dL/dsigma is nonzero) and the
+// k0 row scaled by the corner weight (when the sample has a colour row).
+template <int NQ>
+__device__ __forceinline__ void gather_add(const float4 p, const float4* q, bool has_row,
+                                           bool want_d, int c, float& pd, float4* pk) {
+  const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
+              w = p.z - float(ifloor(p.z));
+  if (want_d && p.w != 0.f) pd = __fadd_rn(pd, density_corner_term(p.w, u, v, w, c));
+  if (has_row) {
+    const float sce = corner_scale(u, v, w, c);
+#pragma unroll
+    for (int b = 0; b < NQ; ++b) {
+      pk[b].x = __fadd_rn(pk[b].x, __fmul_rn(q[b].x, sce));
+      pk[b].y = __fadd_rn(pk[b].y, __fmul_rn(q[b].y, sce));
+      pk[b].z = __fadd_rn(pk[b].z, __fmul_rn(q[b].z, sce));
+      pk[b].w = __fadd_rn(pk[b].w, __fmul_rn(q[b].w, sce));
+    }
+  }
+}
+
 template <int NQ>
 __global__ void __launch_bounds__(256)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
@@ -642,60 +685,51 @@ __global__ void __launch_bounds__(256)
                    const uint32_t* __restrict__ svals, const float4* __restrict__ rec,
                    const int32_t* __restrict__ brow, const float* __restrict__ gk0, int gk0_vec,
                    float* grad_d, float* grad_c, int C) {
+  constexpr int NB = NQ > 0 ? NQ : 1;
   const int64_t nv = int64_t(*count) * kLeafVox;
+  const bool want_d = grad_d != nullptr, want_c = NQ && grad_c;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nv;
        i += int64_t(gridDim.x) * blockDim.x) {
     const int leaf = list[i >> 9];
     const int vox = int(i & 511);
     const int vi = g.origin[leaf * 3] + (vox >> 6), vj = g.origin[leaf * 3 + 1] + ((vox >> 3) & 7),
               vk = g.origin[leaf * 3 + 2] + (vox & 7);
-    bool any = false;
-    float sum_d = 0.f;
-    float4 acc[NQ > 0 ? NQ : 1];
-#pragma unroll
-    for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-    // the up to 8 cells that have this voxel as corner c, in corner order
+    // the up to 8 cells that have this voxel as corner c, in corner order:
+    // the counts are loaded together (a cell outside the lattice reads entry
+    // 0 and counts as empty), so the loads of idle voxels overlap
+    uint32_t len[8], key[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       int di, dj, dk;
       corner_delta(c, di, dj, dk);
-      const uint32_t key = cell_key(g.ldim, vi - di, vj - dj, vk - dk);
-      if (key == kInvalidKey) continue;
-      const uint32_t len = __ldg(cnt + key);
-      if (len == 0) continue;
-      const uint32_t h = __ldg(off + key);
-      any = true;
+      const uint32_t k = cell_key(g.ldim, vi - di, vj - dj, vk - dk);
+      key[c] = k == kInvalidKey ? 0u : k;
+      len[c] = __ldg(cnt + key[c]);
+      if (k == kInvalidKey) len[c] = 0;
+    }
+    uint32_t any = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) any |= len[c];
+    if (!any) continue;
+    float sum_d = 0.f;
+    float4 acc[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) acc[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      if (!len[c]) continue;
       float pd = 0.f;
-      float4 pk[NQ > 0 ? NQ : 1];
+      float4 pk[NB];
 #pragma unroll
-      for (int b = 0; b < (NQ > 0 ? NQ : 1); ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (uint32_t j = h; j < h + len; ++j) {
-        const uint32_t smp = svals[j];
-        const float4 p = rec[smp];
-        const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
-                    w = p.z - float(ifloor(p.z));
-        if (grad_d && p.w != 0.f) pd = __fadd_rn(pd, density_corner_term(p.w, u, v, w, c));
-        const int32_t row = NQ && grad_c ? brow[smp] : -1;
-        if (row >= 0) {  // a sample without a colour row adds nothing to k0
-          const float sce = corner_scale(u, v, w, c);
-          const float* gr = gk0 + int64_t(row) * C;
-#pragma unroll
-          for (int b = 0; b < NQ; ++b) {
-            float4 q;
-            if (gk0_vec) {
-              q = __ldg(reinterpret_cast<const float4*>(gr) + b);
-            } else {
-              q.x = __ldg(gr + 4 * b);
-              q.y = 4 * b + 1 < C ? __ldg(gr + 4 * b + 1) : 0.f;
-              q.z = 4 * b + 2 < C ? __ldg(gr + 4 * b + 2) : 0.f;
-              q.w = 4 * b + 3 < C ? __ldg(gr + 4 * b + 3) : 0.f;
-            }
-            pk[b].x = __fadd_rn(pk[b].x, __fmul_rn(q.x, sce));
-            pk[b].y = __fadd_rn(pk[b].y, __fmul_rn(q.y, sce));
-            pk[b].z = __fadd_rn(pk[b].z, __fmul_rn(q.z, sce));
-            pk[b].w = __fadd_rn(pk[b].w, __fmul_rn(q.w, sce));
-          }
-        }
+      for (int b = 0; b < NB; ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const uint32_t h = __ldg(off + key[c]);
+      for (uint32_t j = h; j < h + len[c]; ++j) {
+        const uint32_t s0 = svals[j];
+        const float4 p0 = rec[s0];
+        const int32_t r0 = want_c ? brow[s0] : -1;
+        float4 q0[NB];
+        gather_row<NQ>(gk0, r0, C, gk0_vec, q0);
+        gather_add<NQ>(p0, q0, r0 >= 0, want_d, c, pd, pk);
       }
       sum_d = __fadd_rn(sum_d, pd);
 #pragma unroll
@@ -706,10 +740,9 @@ __global__ void __launch_bounds__(256)
         acc[b].w = __fadd_rn(acc[b].w, pk[b].w);
       }
     }
-    if (!any) continue;
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
-    if (grad_d) grad_d[slot] = __fadd_rn(grad_d[slot], sum_d);
-    if (NQ && grad_c) {
+    if (want_d) grad_d[slot] = __fadd_rn(grad_d[slot], sum_d);
+    if (want_c) {
       float* dst = grad_c + slot * C;
 #pragma unroll
       for (int b = 0; b < NQ; ++b) {

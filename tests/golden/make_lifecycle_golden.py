@@ -27,6 +27,7 @@ import ast
 import os
 import shutil
 import sys
+import tempfile
 import textwrap
 import types
 
@@ -157,7 +158,7 @@ def compression_case(out):
 
     vdb.readAll = readAll
     vdb.write = lambda path, grids: None
-    work = os.path.join(ROOT, "_work", "golden_compression")
+    work = tempfile.mkdtemp(prefix="compression_", dir=HERE)  # removed below
     os.makedirs(os.path.join(work, "vdb_synth"), exist_ok=True)
     argv, tload = sys.argv, torch.load
     try:

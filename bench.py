@@ -11,9 +11,14 @@ Beside the headline line's step timing the JSON carries: per-stage times and
 rooflines, the end-to-end number through the public API with host buffers,
 the merged-VDB render of 200 800x800 frames (FP32 plain and BF16), the PSNR
 of FP32- and BF16-trained models after 2000 iterations on 8 held-out 800x800
-views, and the 320^3 / 65536-ray BF16 training step.
+views, the 320^3 / 65536-ray BF16 training step, and `lifecycle`: the steps
+around the training step (merged compression, 80^3 -> 160^3 rescaling, the
+mask-cache update, rays of a view, the in-mask-cache hit test, ray
+compaction, per-view voxel counts) with device time, algorithmic bytes,
+fraction of the measured HBM bandwidth and the oracle's CPU time.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --lifecycle-only      # just the lifecycle timings
 
 Prints one JSON line (rank 0). Under torchrun every rank runs an independent
 replica (the path has no cross-GPU exchange in this build) and the time is the

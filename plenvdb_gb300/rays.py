@@ -103,7 +103,11 @@ def _compact(keep, srcs, cap):
 @torch.no_grad()
 def get_training_rays(rgb_tr, train_poses, HW, Ks, ndc, inverse_y, flip_x, flip_y):
     """(rgb_tr, rays_o_tr, rays_d_tr, viewdirs_tr, imsz) with [n,H,W,3] rays (lib/dvgo.py:524-548)."""
+    # one image size and one camera for all views, as the reference asserts
     assert len(np.unique(np.asarray(HW), axis=0)) == 1
+    Kn = np.stack([np.asarray(k.cpu() if torch.is_tensor(k) else k, np.float64) for k in Ks])
+    assert len(np.unique(Kn.reshape(len(Kn), -1), axis=0)) == 1
+    assert len(rgb_tr) == len(train_poses) == len(Ks) == len(HW)
     H, W = (int(v) for v in np.asarray(HW)[0])
     K = Ks[0]
     n = len(rgb_tr)
@@ -121,6 +125,7 @@ def get_training_rays(rgb_tr, train_poses, HW, Ks, ndc, inverse_y, flip_x, flip_
 @torch.no_grad()
 def get_training_rays_flatten(rgb_tr_ori, train_poses, HW, Ks, ndc, inverse_y, flip_x, flip_y):
     """Flattened [N,3] rays of all views (lib/dvgo.py:551-579)."""
+    assert len(rgb_tr_ori) == len(train_poses) == len(Ks) == len(HW)
     N = sum(im.shape[0] * im.shape[1] for im in rgb_tr_ori)
     rgb_tr = torch.zeros([N, 3], device="cuda")
     rays_o_tr = torch.zeros_like(rgb_tr)
@@ -128,6 +133,7 @@ def get_training_rays_flatten(rgb_tr_ori, train_poses, HW, Ks, ndc, inverse_y, f
     viewdirs_tr = torch.zeros_like(rgb_tr)
     imsz, top = [], 0
     for c2w, img, (H, W), K in zip(train_poses, rgb_tr_ori, HW, Ks):
+        assert tuple(img.shape[:2]) == (int(H), int(W))
         o, d, v = get_rays_of_a_view(int(H), int(W), K, c2w, ndc, inverse_y, flip_x, flip_y)
         n = int(H) * int(W)
         rgb_tr[top:top + n].copy_(torch.as_tensor(img).reshape(-1, 3))
@@ -145,6 +151,7 @@ def get_training_rays_in_maskcache_sampling(rgb_tr_ori, train_poses, HW, Ks, ndc
     """Rays of all views that hit the coarse geometry, in view and pixel order
     (lib/dvgo.py:582-624): per view the rays, the hit test and an
     order-preserving compaction, all on the device."""
+    assert len(rgb_tr_ori) == len(train_poses) == len(Ks) == len(HW)
     N = sum(im.shape[0] * im.shape[1] for im in rgb_tr_ori)
     rgb_tr = torch.zeros([N, 3], device="cuda")
     rays_o_tr = torch.zeros_like(rgb_tr)
@@ -152,6 +159,7 @@ def get_training_rays_in_maskcache_sampling(rgb_tr_ori, train_poses, HW, Ks, ndc
     viewdirs_tr = torch.zeros_like(rgb_tr)
     imsz, top = [], 0
     for c2w, img, (H, W), K in zip(train_poses, rgb_tr_ori, HW, Ks):
+        assert tuple(img.shape[:2]) == (int(H), int(W))
         o, d, v = get_rays_of_a_view(int(H), int(W), K, c2w, ndc, inverse_y, flip_x, flip_y)
         hit = hit_coarse_geo(o, d, render_kwargs["near"], render_kwargs.get("far", 1e9),
                              render_kwargs["stepsize"], xyz_min=model.xyz_min,

@@ -379,3 +379,36 @@ def test_checkpoint_resume_is_bitwise(lib, tmp_path):
     from plenvdb_gb300 import lifecycle as LC
     mg = LC.MaskGrid(path=str(tmp_path / "fine_last.npz"), mask_cache_thres=1e-3)
     assert mg.shape == (48, 48, 48) and 0 < int(mg.mask.sum()) < 48 ** 3
+
+
+def test_merge_one_grid_only(lib):
+    """Density-only and colour-only compression (the other rows not written)."""
+    import torch
+    from plenvdb_gb300 import lifecycle as LC
+    R = (19, 23, 17)
+    dg, dd, _ = _sparse(R, 11)
+    kg, kd, _ = _sparse(R, 12, C=12, bg=0.0)
+    mask = np.random.default_rng(13).random(R) < 0.3
+    m = torch.from_numpy(mask).cuda()
+    a = LC.merge_compress(dg, None, m, row_dtype="float32")
+    b = LC.merge_compress(None, kg, m, row_dtype="float32")
+    idx, den, col = OL.merge(dd, kd, mask, dtype=np.float32)
+    assert a["col"] is None and b["den"] is None
+    np.testing.assert_array_equal(a["index"].cpu().numpy(), idx)
+    np.testing.assert_array_equal(b["index"].cpu().numpy(), idx)
+    np.testing.assert_array_equal(a["den"].cpu().numpy(), den)
+    np.testing.assert_array_equal(b["col"].cpu().numpy(), col)
+
+
+def test_rescaled_mask_cache_without_old_cache(lib):
+    """The rebuild after rescaling with no previous mask cache: only the pooled
+    alpha decides (the old-cache lookup counts as all set)."""
+    from plenvdb_gb300 import lifecycle as LC
+    R = (21, 18, 26)
+    g, dense, active = _sparse(R, 14, bg=-10.0, p=0.25)
+    og = O.OGridData(R, dense.astype(np.float64), active, background=-10.0)
+    mn, mx = [-1.5] * 3, [1.5] * 3
+    new = LC.rescaled_mask_cache(None, g, mn, mx, -4.6, 0.5, 1e-3)
+    ref, margin = OL.occupancy(1, og, R, mn, mx, -4.6, 0.5, 1e-3)
+    _assert_mask(new.mask.cpu().numpy().astype(bool), margin, ref, 1e-3)
+    assert ref.any() and not ref.all()

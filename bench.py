@@ -97,23 +97,35 @@ def replica_throughput(step_ms_total, steps, world, device="cuda"):
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    nvidia-smi starts before the warm-up steps and polls every 200 ms with its
+    output line-buffered (stdbuf, where present); every sample carries
+    nvidia-smi's timestamp. begin() and end() mark the timed region on the
+    same clock, and the summary keeps the samples taken inside it plus the
+    first one after it (which covers the region's tail), so a region shorter
+    than one interval still gets the sample that spans it."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 200
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
+        import shutil
+        cmd = ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+               "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)]
+        if shutil.which("stdbuf"):
+            cmd = ["stdbuf", "-oL"] + cmd
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except Exception:
@@ -123,31 +135,70 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_ready(self, timeout: float = 10.0):
+        """Until nvidia-smi has printed its first sample (it takes a moment to start)."""
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.01)
+
+    def begin(self):
+        import datetime
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        import datetime
+        self.t1 = datetime.datetime.now()
+
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text.strip(), "%Y/%m/%d %H:%M:%S.%f")
+        except ValueError:
+            return None
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # wait for the first sample after the region (it covers the region's tail)
+        t_wait = time.time()
+        while time.time() - t_wait < 2.0:
+            last = self._stamp(self.lines[-1].split(",")[0]) if self.lines else None
+            if last is not None and self.t1 is not None and last > self.t1:
+                break
+            time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
+            ts = self._stamp(parts[0])
+            if ts is None:
+                continue
+            rows.append((ts, parts))
+        inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+        after = [r for r in rows if r[0] > self.t1]
+        picked = inside + after[:1]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for _, parts in picked:
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                sm.append(float(parts[2]))
+                smax.append(float(parts[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            for n, v in zip(names, parts[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "samples_inside": len(inside), "interval_ms": self.INTERVAL_MS}
 
 
 # ------------------------------------------------------------------ setup
@@ -210,18 +261,20 @@ def run_ours(args):
            for b in range(nb)]
     flush = torch.zeros(128 * 1024 * 1024, device="cuda")
     st = torch.cuda.current_stream()
+    clocks = ClockSampler(local)
+    clocks.start()
     for i in range(args.warmup):
         tr.step(*dev[i % nb])
     torch.cuda.synchronize()
+    clocks.wait_ready()
     # ---------------- timed region (device-resident inputs)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
-    clocks = ClockSampler(local)
-    clocks.start()
     launches0 = lib.pvdb_launch_count()
     if ws_ > 1:
         dist.barrier()
     torch.cuda.synchronize()
+    clocks.begin()
     t_wall = time.perf_counter()
     for i in range(args.steps):
         flush_l2(flush)
@@ -230,6 +283,7 @@ def run_ours(args):
         evs[i][1].record(st)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
+    clocks.end()
     launches = lib.pvdb_launch_count() - launches0
     clk = clocks.stop()
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))

@@ -33,8 +33,9 @@ def norm3_f32(v):
 
 
 def linspace_f32(start, end, n):
-    """torch.linspace on the CPU in float32: start + step*i for the first
-    half, end - step*(n-1-i) for the second."""
+    """torch.linspace in float32 by ATen's scalar two-sided formula: start +
+    step*i for the first half, end - step*(n-1-i) for the second (ATen's
+    vectorised CPU path can differ by one ulp of the range)."""
     start, end = f32(start), f32(end)
     if n == 1:
         return np.array([start], f32)
@@ -84,7 +85,9 @@ def resample(values, new_ws):
     """F.interpolate(mode='trilinear', align_corners=True) of values
     [X,Y,Z,C] (ATen upsample_trilinear3d): the z interpolation nested in y
     nested in x, each a*w0 + b*w1 evaluated as fma(a, w0, b*w1) like ATen's
-    CPU build (the fma emulated in float64: the exact sum rounded once)."""
+    CPU build does for 1- and 3-channel volumes (some wider shapes take
+    another ATen order, a few ulps apart). The fma is emulated in float64:
+    the exact sum rounded once."""
     v = np.asarray(values, f32)
     ax = [_axis(v.shape[a], int(new_ws[a])) for a in range(3)]
     (x0, x1, wx0, wx1), (y0, y1, wy0, wy1), (z0, z1, wz0, wz1) = ax
@@ -129,7 +132,8 @@ def raw2alpha_f32(d, shift, interval):
 
 
 def softplus_alpha(x, interval):
-    """1 - exp(-softplus(x) * interval), torch softplus threshold 20."""
+    """1 - exp(-softplus(x) * interval), softplus = log1p(exp(x)) with torch's
+    threshold 20 (torch's vectorised CPU kernel uses log(exp(x) + 1))."""
     x = np.asarray(x, f32)
     sp = np.where(x > 20, x, np.log1p(np.exp(np.minimum(x, f32(20))))).astype(f32)
     return (f32(1) - np.exp(-(sp * f32(interval)))).astype(f32)

@@ -220,7 +220,9 @@ __global__ void __launch_bounds__(kMergeThreads)
 
 // --------------------------------------------------------------- rescale
 // F.interpolate(mode='trilinear', align_corners=True) on the dense values
-// (grid.py:92, ATen upsample_trilinear3d): per axis src = scale*o with
+// (grid.py:92, ATen upsample_trilinear3d, as its CPU build evaluates 1- and
+// 3-channel volumes; some wider shapes take another ATen order, a few ulps
+// apart): per axis src = scale*o with
 // scale = (in-1)/(out-1), i0 = min(floor(src), in-1), i1 = i0 + (i0 < in-1),
 // l1 = clamp(src - i0, 0, 1), l0 = 1 - l1; the value nests z inside y inside
 // x: ((v[..z0]*l0z + v[..z1]*l1z)*l0y + (...)*l1y)*l0x + (...)*l1x, each
@@ -386,15 +388,19 @@ struct OccArgs {
   uint8_t* out;
 };
 
-// torch.linspace(start, end, n)[i] on the CPU: start + step*i in the first
-// half, end - step*(n-1-i) in the second (ATen RangeFactoriesKernel).
+// torch.linspace(start, end, n)[i] by the two-sided formula of ATen's scalar
+// path: start + step*i in the first half, end - step*(n-1-i) in the second
+// (ATen RangeFactoriesKernel). ATen's vectorised path, which depends on the
+// CPU, can round differently by up to one ulp of the range.
 __device__ __forceinline__ float linspace_at(float start, float end, float step, int n, int i) {
   if (n == 1) return start;
   return i < n / 2 ? __fadd_rn(start, __fmul_rn(step, float(i)))
                    : __fsub_rn(end, __fmul_rn(step, float(n - 1 - i)));
 }
 
-// 1 - exp(-softplus(x) * interval), softplus with torch's threshold 20.
+// 1 - exp(-softplus(x) * interval), softplus as log1p(exp(x)) with torch's
+// threshold 20 (torch's vectorised CPU kernel forms log(exp(x) + 1): within
+// 2e-5 relative).
 __device__ __forceinline__ float softplus_alpha(float x, float interval) {
   const float sp = x > 20.f ? x : log1pf(expf(x));
   return 1.f - expf(-__fmul_rn(sp, interval));

@@ -61,13 +61,15 @@ def merge(den, col, mask, dtype=np.float16):
     n = int(mask.sum())
     index = np.zeros(mask.shape, np.int32)
     index[mask] = np.arange(1, n + 1, dtype=np.int32)
-    den_rows = None if den is None else np.concatenate(
-        [[0.0], np.asarray(den, np.float32)[mask]]).astype(np.float32).astype(dtype)
-    col_rows = None
-    if col is not None:
-        col = np.asarray(col, np.float32)
-        col_rows = np.concatenate([np.zeros((1, col.shape[-1]), np.float32), col[mask]]).astype(
-            dtype)
+    # values beyond the FP16 range become inf, as torch's .half() makes them
+    with np.errstate(over="ignore"):
+        den_rows = None if den is None else np.concatenate(
+            [[0.0], np.asarray(den, np.float32)[mask]]).astype(np.float32).astype(dtype)
+        col_rows = None
+        if col is not None:
+            col = np.asarray(col, np.float32)
+            col_rows = np.concatenate([np.zeros((1, col.shape[-1]), np.float32),
+                                       col[mask]]).astype(dtype)
     return index, den_rows, col_rows
 
 

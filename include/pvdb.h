@@ -57,6 +57,14 @@ int pvdb_last_error(char* buf, size_t len);
 /* Test hook: makes the next `count` device allocations made by the library fail
  * with PVDB_ERR_NOMEM (host-side injection; no device call is made for them). */
 int pvdb_debug_fail_next_allocs(int count);
+/* Test hook of the bounded device-side waits (no counterpart in the
+ * reference): spins > 0 replaces the built-in spin limit of the look-back
+ * waits (radix sort, march ray offsets; 0 restores it); hold_first != 0 makes
+ * the first publisher of each look-back chain withhold its count, so that the
+ * waits behind it run out and the call reports PVDB_ERR_TIMEOUT. Applies to
+ * launches made after the call (a captured train-step graph keeps the values
+ * it was captured with). */
+int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first);
 
 /* Stage profiler. Between begin and end, pvdb_train_step and
  * pvdb_renderer_render record CUDA events on their stream at stage boundaries
@@ -131,7 +139,11 @@ int pvdb_grid_sample(pvdb_grid g, const float* xs, const float* ys, const float*
  * colorvdb.cu:28-37, :130-175): adds grad_out[n,channels] x trilinear weight
  * into the gradient of every corner voxel that lies in an allocated leaf (the
  * active mask is ignored, as in the reference). The sum is a deterministic
- * leaf-sorted segmented reduction (bitwise reproducible), not float atomics. */
+ * leaf-sorted segmented reduction (bitwise reproducible), not float atomics.
+ * The call waits for its stream to finish, as the reference's backward does
+ * (plenvdb.h:468-485 ends in a device synchronisation): a bounded wait of the
+ * sort that gave up is reported as PVDB_ERR_TIMEOUT, with the gradient left
+ * unchanged. */
 int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys, const float* zs,
                               const float* grad_out, int64_t n, int32_t mem, pvdb_stream s);
 
@@ -141,11 +153,15 @@ int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys, con
  * memory budget, and callers that cannot afford the device-wide
  * synchronisation of cudaMalloc/cudaFree. No counterpart in the reference.
  * The call allocates nothing: its scratch is one fixed file-scope device array
- * (about 5.3 MB, held on every GPU that loads the library until exit) that
- * limits a call to n <= 32768 points (PVDB_ERR_ARG beyond that). The first
- * call on a device looks up that array's address (cudaGetSymbolAddress); make
- * it before any stream capture. All calls share the array, so calls that
- * overlap on the GPU (e.g. on two streams) race. */
+ * (about 5.3 MB) that limits a call to n <= 32768 points (PVDB_ERR_ARG beyond
+ * that). The array exists on a GPU once the library's module is loaded there
+ * and is held until exit; under CUDA's lazy module loading (the default) the
+ * first call on a device loads it and looks up its address
+ * (cudaGetSymbolAddress), so make that first call before reserving a memory
+ * pool or capturing a stream. All calls share the array, so calls that
+ * overlap on the GPU (e.g. on two streams) race: serialise them on one stream
+ * per device. Like pvdb_grid_sample_backward, the call waits for its stream
+ * and reports a sort wait that gave up as PVDB_ERR_TIMEOUT. */
 int pvdb_grid_sample_backward_noalloc(pvdb_grid g, const float* xs, const float* ys,
                                       const float* zs, const float* grad_out, int64_t n,
                                       pvdb_stream s);
@@ -171,6 +187,12 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
  * densityvdb.cu:353-368, color_zero_grad_kernel colorvdb.cu:355-371). */
 int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s);
 
+/* Number of leaves in the grid's touched-leaf list as last built (by TV or
+ * mode-1 Adam over the leaves a backward touched), 0 if none was built: the
+ * leaves whose voxels those passes visit. A measurement aid with no
+ * counterpart in the reference; waits for the stream. */
+int pvdb_grid_touched_leaves(pvdb_grid g, int64_t* n, pvdb_stream s);
+
 /* Device views of the leaf store (for zero-copy use by a host framework).
  * data/grad: float[nleaf*512*channels] (voxel-major, channel innermost);
  * mask: uint64[nleaf*8]; leaf_table: int32[ldim0*ldim1*ldim2] (-1 = no leaf);
@@ -182,9 +204,10 @@ int pvdb_grid_device_views(pvdb_grid g, void** data, void** grad, void** mask,
                            void** leaf_table, void** leaf_origin, int32_t ldim[3]);
 
 /* Report writes through device views: which = PVDB_WHICH_DATA drops the
- * values' derived bounds (rebuilt by the next march), PVDB_WHICH_GRAD makes
- * every leaf count as possibly holding a gradient. No reference counterpart
- * (the reference copies host arrays in and out on every call). */
+ * values' derived data (the brick bound, rebuilt by the next march, and the
+ * BF16 feature shadow, rebuilt by the next BF16 train step), PVDB_WHICH_GRAD
+ * makes every leaf count as possibly holding a gradient. No reference
+ * counterpart (the reference copies host arrays in and out on every call). */
 int pvdb_grid_mark_written(pvdb_grid g, int32_t which);
 
 /* save_to / load_from (plenvdb.h:143-148, :126-142, :269-276, :211-240).

@@ -158,11 +158,31 @@ def adam(g: OGridData, grad_pad, m_pad, v_pad, perlr_pad, stepsz, eps, b0, b1, m
     return data
 
 
-def tv(g: OGridData, grad_pad, wx, wy, wz, dense_mode):
-    """TV gradient with weights already divided by 6, added into grad_pad."""
+def tv(g: OGridData, grad_pad, wx, wy, wz, dense_mode, fp32=False):
+    """TV gradient with weights already divided by 6, added into grad_pad
+    (fp32: the reference's float arithmetic)."""
     lib().oracle_tv(g.ref, _p(grad_pad), C.c_float(wx), C.c_float(wy), C.c_float(wz),
-                    int(dense_mode))
+                    int(dense_mode), int(fp32))
     return grad_pad
+
+
+def adam_step_size(lr, beta1, beta2, step):
+    """Host-side Adam step size of adam_upd_kernel.cu:72 (float)."""
+    f = lib().oracle_adam_step_size
+    f.restype = C.c_float
+    return float(f(C.c_float(lr), C.c_float(beta1), C.c_float(beta2), int(step)))
+
+
+def adam_dense(p, g, m, v, perlr, step, beta1, beta2, lr, eps, mode, fp32=False):
+    """One dense Adam step (MaskedAdam's kernels) on float64 copies; returns
+    (p, m, v)."""
+    p, m, v = (np.array(x, np.float64) for x in (p, m, v))
+    g = np.ascontiguousarray(g, np.float64)
+    pl = None if perlr is None else np.ascontiguousarray(perlr, np.float64)
+    lib().oracle_adam_dense(_p(p), _p(g), _p(m), _p(v), _p(pl), C.c_int64(p.size), int(step),
+                            C.c_float(beta1), C.c_float(beta2), C.c_float(lr), C.c_float(eps),
+                            int(mode), int(fp32))
+    return p, m, v
 
 
 def raw2alpha(d, shift, interval, fp32=False):
@@ -415,6 +435,15 @@ class CPUTrainer:
         return lib().oracle_train_step_fp32(C.byref(self.g), C.byref(self.n), _p(ro), _p(rd), _p(vd),
                                             _p(tg), int(R), C.byref(params), C.c_float(w_main),
                                             C.c_float(w_ent), C.c_float(w_per), C.c_float(tv_w))
+
+
+    def density_step(self, rays_o, rays_d, target_alpha, params):
+        """Density-only FP32 forward + backward with the alpha-MSE loss
+        (oracle_density_step_fp32); the gradient accumulates into self.gd."""
+        ro, rd, ta = (np.ascontiguousarray(a, np.float32) for a in (rays_o, rays_d, target_alpha))
+        f = lib().oracle_density_step_fp32
+        f.restype = C.c_double
+        return f(C.byref(self.g), _p(ro), _p(rd), _p(ta), int(ro.shape[0]), C.byref(params))
 
 
 class _RenderParams(C.Structure):

@@ -115,7 +115,9 @@ struct Ray {
 };
 
 // infer_t_minmax / infer_n_samples / infer_ray_start_dir
-// (render_utils_kernel.cu:12-78); |d| = sqrt(fma(dz,dz,fma(dy,dy,dx*dx))).
+// (render_utils_kernel.cu:12-78); |d| = sqrt(fma(dz,dz,fma(dx,dx,dy*dy))),
+// nvcc's contraction of dx*dx + dy*dy + dz*dz (pinned by the golden vectors
+// of the reference's own kernel).
 void ray_setup(const float* o, const float* d, const omarch_params& p, Ray& r) {
   const float vx = d[0] == 0.f ? float(1e-6) : d[0];
   const float vy = d[1] == 0.f ? float(1e-6) : d[1];
@@ -126,7 +128,7 @@ void ray_setup(const float* o, const float* d, const omarch_params& p, Ray& r) {
               bz = (p.xyz_min[2] - o[2]) / vz;
   r.t_min = std::max(std::min(std::max(std::max(std::min(ax, bx), std::min(ay, by)), std::min(az, bz)), p.far_), p.near_);
   r.t_max = std::max(std::min(std::min(std::min(std::max(ax, bx), std::max(ay, by)), std::max(az, bz)), p.far_), p.near_);
-  const float rn = std::sqrt(std::fma(d[2], d[2], std::fma(d[1], d[1], d[0] * d[0])));
+  const float rn = std::sqrt(std::fma(d[2], d[2], std::fma(d[0], d[0], d[1] * d[1])));
   const float q = ((r.t_max - r.t_min) * rn) / p.stepdist;
   r.n_steps = int64_t(std::max(double(std::ceil(q)), 1.0));
   for (int a = 0; a < 3; ++a) {
@@ -471,11 +473,19 @@ void oracle_adam(const ogrid* g, double* data, const double* grad, double* m, do
 
 // TV (total_variation_kernel.cu:13-35) with weights already divided by 6;
 // neighbours inside [0, reso); values through the leaf rules; every active
-// voxel (dense_mode) or those with a nonzero gradient.
-void oracle_tv(const ogrid* g, double* grad, float wx, float wy, float wz, int dense_mode) {
+// voxel (dense_mode) or those with a nonzero gradient. The six terms are taken
+// in the reference's order (k-1, k+1, j-1, j+1, i-1, i+1). fp32 mimics the
+// reference's float arithmetic: each term w * clamp(p - q) is rounded, then
+// added to the running float sum (the conditional around each term keeps nvcc
+// from fusing them), and the sum is added to the gradient last. The i axis is weighted by wx (the
+// reference writes wz there, :31-32; its callers pass wx == wz, dvgo.py:245-251).
+void oracle_tv(const ogrid* g, double* grad, float wx, float wy, float wz, int dense_mode,
+               int fp32) {
   const int64_t nvox = int64_t(g->pad[0]) * g->pad[1] * g->pad[2];
   std::vector<double> add(size_t(nvox) * g->C, 0.0);
+  std::vector<uint8_t> has(size_t(nvox) * g->C, 0);
   auto cl = [](double x) { return std::min(std::max(x, -1.0), 1.0); };
+  auto clf = [](float x) { return std::min(std::max(x, -1.f), 1.f); };
   for (int i = 0; i < g->reso[0]; ++i)
     for (int j = 0; j < g->reso[1]; ++j)
       for (int k = 0; k < g->reso[2]; ++k) {
@@ -483,18 +493,71 @@ void oracle_tv(const ogrid* g, double* grad, float wx, float wy, float wz, int d
         if (!allocated(*g, i, j, k) || !g->active[q]) continue;
         for (int ch = 0; ch < g->C; ++ch) {
           if (!dense_mode && grad[q * g->C + ch] == 0) continue;
-          const double p = value(*g, i, j, k, ch);
-          double s = 0;
-          if (k > 0) s += wz * cl(p - value(*g, i, j, k - 1, ch));
-          if (k < g->reso[2] - 1) s += wz * cl(p - value(*g, i, j, k + 1, ch));
-          if (j > 0) s += wy * cl(p - value(*g, i, j - 1, k, ch));
-          if (j < g->reso[1] - 1) s += wy * cl(p - value(*g, i, j + 1, k, ch));
-          if (i > 0) s += wx * cl(p - value(*g, i - 1, j, k, ch));
-          if (i < g->reso[0] - 1) s += wx * cl(p - value(*g, i + 1, j, k, ch));
-          add[q * g->C + ch] = s;
+          const bool in[6] = {k > 0, k < g->reso[2] - 1, j > 0, j < g->reso[1] - 1, i > 0,
+                              i < g->reso[0] - 1};
+          const int nb[6][3] = {{i, j, k - 1}, {i, j, k + 1}, {i, j - 1, k},
+                                {i, j + 1, k}, {i - 1, j, k}, {i + 1, j, k}};
+          const float w[6] = {wz, wz, wy, wy, wx, wx};
+          if (fp32) {
+            const float p = float(value(*g, i, j, k, ch));
+            float s = 0.f;
+            for (int t = 0; t < 6; ++t)
+              if (in[t]) {
+                const float term = w[t] * clf(p - float(value(*g, nb[t][0], nb[t][1], nb[t][2], ch)));
+                s = s + term;
+              }
+            add[q * g->C + ch] = s;
+          } else {
+            const double p = value(*g, i, j, k, ch);
+            double s = 0;
+            for (int t = 0; t < 6; ++t)
+              if (in[t]) s += w[t] * cl(p - value(*g, nb[t][0], nb[t][1], nb[t][2], ch));
+            add[q * g->C + ch] = s;
+          }
+          has[q * g->C + ch] = 1;
         }
       }
-  for (int64_t q = 0; q < nvox * g->C; ++q) grad[q] += add[q];
+  for (int64_t q = 0; q < nvox * g->C; ++q) {
+    if (!has[q]) continue;
+    grad[q] = fp32 ? double(float(grad[q]) + float(add[q])) : grad[q] + add[q];
+  }
+}
+
+// Dense Adam of MaskedAdam (masked_adam.py:105-158 -> adam_upd_kernel.cu):
+// mode 0 adam_upd (:8-23), 1 masked_adam_upd (skip g == 0, :25-41), 2
+// adam_upd_with_perlr (:43-58). The step size is the host's
+// lr * sqrt(1 - beta2^step) / (1 - beta1^step) in float (:72). fp32 mimics
+// the float kernel: each moment is one fused multiply-add of the decayed
+// moment onto the rounded gradient term (nvcc's contraction of
+// `beta * m + (1 - beta) * g`).
+float oracle_adam_step_size(float lr, float beta1, float beta2, int step) {
+  return lr * std::sqrt(1.f - std::pow(beta2, float(step))) / (1.f - std::pow(beta1, float(step)));
+}
+
+void oracle_adam_dense(double* p, const double* g, double* m, double* v, const double* perlr,
+                       int64_t n, int step, float beta1, float beta2, float lr, float eps,
+                       int mode, int fp32) {
+  const float ss = oracle_adam_step_size(lr, beta1, beta2, step);
+  for (int64_t i = 0; i < n; ++i) {
+    if (mode == 1 && g[i] == 0) continue;
+    if (fp32) {
+      const float gi = float(g[i]);
+      const float mn = std::fma(beta1, float(m[i]), (1.f - beta1) * gi);
+      const float vn = std::fma(beta2, float(v[i]), (1.f - beta2) * gi * gi);
+      m[i] = mn;
+      v[i] = vn;
+      const float num = mode == 2 ? ss * float(perlr[i]) * mn : ss * mn;
+      p[i] = float(p[i]) - num / (std::sqrt(vn) + eps);
+    } else {
+      const double b1 = beta1, b2 = beta2;
+      const double mn = b1 * m[i] + (1 - b1) * g[i];
+      const double vn = b2 * v[i] + (1 - b2) * g[i] * g[i];
+      m[i] = mn;
+      v[i] = vn;
+      const double num = double(ss) * (mode == 2 ? perlr[i] : 1.0) * mn;
+      p[i] = p[i] - num / (std::sqrt(vn) + double(eps));
+    }
+  }
 }
 
 // raw2alpha / raw2alpha_backward (render_utils_kernel.cu:430-552)
@@ -1168,6 +1231,79 @@ double oracle_train_step_fp32(otrain_grids* G, otrain_net* N, const float* ro, c
     N->params[q] -= sn * N->m[q] / (std::sqrt(N->v[q]) + 1e-8f);
   }
   N->lr *= float(std::pow(0.1, 1.0 / 20000.0));
+  return loss;
+}
+
+// Density-only forward + backward in FP32 on the host cores (the plain
+// density-only configuration): the march of dvgo.py:296-335 without colour
+// (density trilinear, raw2alpha, alpha2weight with the T < t_stop stop), the
+// composited alpha 1 - alphainv_last, the loss mean((alpha - target)^2) over
+// the rays, and its gradient through alpha2weight_backward (:653-677),
+// raw2alpha_backward (:506-517) and the density scatter (densityvdb.cu:16-27,
+// 143-167; float atomics as the reference's kernel) into G->gdens. No
+// optimiser step. Returns the loss.
+double oracle_density_step_fp32(otrain_grids* G, const float* ro, const float* rd,
+                                const float* target_alpha, int R, const omarch_params* p) {
+  const int P1 = G->pad[1], P2 = G->pad[2];
+  auto alloc_at = [&](int i, int j, int k) {
+    if (i < 0 || j < 0 || k < 0 || i >= G->pad[0] || j >= P1 || k >= P2) return false;
+    return G->alloc[((i >> 3) * (P1 / 8) + (j >> 3)) * (P2 / 8) + (k >> 3)] != 0;
+  };
+  auto vid = [&](int i, int j, int k) { return (int64_t(i) * P1 + j) * P2 + k; };
+  auto dval = [&](int i, int j, int k) { return alloc_at(i, j, k) ? G->dens[vid(i, j, k)] : G->background; };
+  double loss = 0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : loss)
+  for (int r = 0; r < R; ++r) {
+    Ray ray;
+    ray_setup(ro + 3 * r, rd + 3 * r, *p, ray);
+    std::vector<float> ka, kT, ksig;
+    std::vector<std::array<float, 3>> kidx;
+    float Tc = 1.f;
+    for (int64_t k = 0; k < ray.n_steps; ++k) {
+      float pt[3], idx[3];
+      ray_point(ray, p->stepdist, k, pt);
+      if (out_of_bbox(pt, *p)) continue;
+      world_to_index(pt, *p, G->reso, idx);
+      const int i = int(std::floor(idx[0])), j = int(std::floor(idx[1])), kk = int(std::floor(idx[2]));
+      const float u = idx[0] - float(i), v = idx[1] - float(j), w = idx[2] - float(kk);
+      float sig = 0.f;
+      for (int c = 0; c < 8; ++c) {
+        const int* d = kCorner[c];
+        const float a = d[0] ? u : 1.f - u, b = d[1] ? v : 1.f - v, cc = d[2] ? w : 1.f - w;
+        sig = sig + ((dval(i + d[0], j + d[1], kk + d[2]) * a) * b) * cc;
+      }
+      float e;
+      const float alpha = raw2alpha<float>(sig, p->act_shift, p->interval, e);
+      if (!(alpha > p->fast_color_thres)) continue;
+      ka.push_back(alpha);
+      kT.push_back(Tc);
+      ksig.push_back(sig);
+      kidx.push_back({idx[0], idx[1], idx[2]});
+      Tc = trans_step<float>(Tc, alpha);
+      if (Tc < p->t_stop) break;
+    }
+    const float err = (1.f - Tc) - target_alpha[r];
+    loss += double(err) * err / R;
+    // d loss / d alphainv_last; the weights carry no gradient
+    float back = (-2.f * err / float(R)) * Tc;
+    for (int q = int(ka.size()) - 1; q >= 0; --q) {
+      const float ga = alpha_grad<float>(0.f, kT[q], back, ka[q]);
+      float e;
+      (void)raw2alpha<float>(ksig[q], p->act_shift, p->interval, e);
+      const float gs = raw2alpha_grad<float>(e, p->interval, ga);
+      const auto& id3 = kidx[q];
+      const int i = int(std::floor(id3[0])), j = int(std::floor(id3[1])), kk = int(std::floor(id3[2]));
+      const float u = id3[0] - float(i), v = id3[1] - float(j), w = id3[2] - float(kk);
+      for (int c = 0; c < 8; ++c) {
+        const int* d = kCorner[c];
+        const int ci = i + d[0], cj = j + d[1], ck = kk + d[2];
+        if (!alloc_at(ci, cj, ck)) continue;
+        const float a = d[0] ? u : 1.f - u, b = d[1] ? v : 1.f - v, cc = d[2] ? w : 1.f - w;
+#pragma omp atomic
+        G->gdens[vid(ci, cj, ck)] += ((gs * a) * b) * cc;
+      }
+    }
+  }
   return loss;
 }
 

@@ -11,6 +11,7 @@
 #include <numeric>
 
 #include "pvdb_internal.cuh"
+#include "tc.cuh"
 
 namespace pvdb {
 
@@ -228,7 +229,9 @@ __global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
           add += 0.f;
         } else {
           const float vn = nb[q] < 0 ? g.background : g.data[int64_t(nb[q]) * g.C + ch];
-          add += wt[q] * tv_clamp(p - vn);
+          // each term rounded, then added (the reference's conditional terms
+          // are not fused, total_variation_kernel.cu:27-32)
+          add = __fadd_rn(add, __fmul_rn(wt[q], tv_clamp(p - vn)));
         }
       }
       g.grad[t0 + ch] = gcur + add;
@@ -313,7 +316,8 @@ __global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mod
         }
       }
 #pragma unroll
-      for (int ch = 0; ch < 12; ++ch) add[ch] += wt[q] * tv_clamp(p[ch] - vn[ch]);
+      for (int ch = 0; ch < 12; ++ch)
+        add[ch] = __fadd_rn(add[ch], __fmul_rn(wt[q], tv_clamp(p[ch] - vn[ch])));
     }
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
@@ -451,6 +455,39 @@ int bmax_ensure(pvdb_grid_s* g, cudaStream_t st) {
   return PVDB_OK;
 }
 
+// BF16 copy of every stored value (round to nearest even), 8 values a thread.
+__global__ void k_half_build(const float* __restrict__ src, __nv_bfloat16* dst, int64_t n) {
+  const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) * 8;
+  if (i + 8 <= n) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(src + i));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(src + i + 4));
+    uint4 o;
+    o.x = tc::pack_bf16(a.x, a.y);
+    o.y = tc::pack_bf16(a.z, a.w);
+    o.z = tc::pack_bf16(b.x, b.y);
+    o.w = tc::pack_bf16(b.z, b.w);
+    *reinterpret_cast<uint4*>(dst + i) = o;
+  } else {
+    for (int64_t q = i; q < n; ++q) dst[q] = __float2bfloat16_rn(src[q]);
+  }
+}
+
+int half_ensure(pvdb_grid_s* g, cudaStream_t st) {
+  const int64_t n = g->nslots() * g->C;
+  if (!g->d_half) {
+    int rc = dev_alloc((void**)&g->d_half, size_t(std::max<int64_t>(n, 8)) * 2);
+    if (rc) return rc;
+    g->half_valid = false;
+  }
+  if (g->half_valid) return PVDB_OK;
+  if (n) {
+    k_half_build<<<ceil_div((n + 7) / 8, 256), 256, 0, st>>>(g->d_data, g->d_half, n);
+    PVDB_CHECK_LAUNCH("k_half_build");
+  }
+  g->half_valid = true;
+  return PVDB_OK;
+}
+
 }  // namespace pvdb
 
 using namespace pvdb;
@@ -578,6 +615,7 @@ int pvdb_grid_destroy(pvdb_grid g) {
   dev_free(g->d_tlist);
   dev_free(g->d_tcount);
   dev_free(g->d_bmax);
+  dev_free(g->d_half);
   dev_free(g->d_stage);
   free_scratch(g->red);
   delete g;
@@ -629,7 +667,7 @@ int pvdb_grid_copy_from_dense(pvdb_grid g, int32_t which, const float* arr, int6
         g->reso[1], g->reso[2]);
   PVDB_CHECK_LAUNCH("k_copy_from_dense");
   if (which == PVDB_WHICH_GRAD) g->all_touched = true;
-  if (which == PVDB_WHICH_DATA) g->bmax_valid = false;
+  if (which == PVDB_WHICH_DATA) data_written(g);
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
   return PVDB_OK;
 }
@@ -681,7 +719,7 @@ int pvdb_grid_set_values_by_mask(pvdb_grid g, const uint8_t* mask, int64_t n, fl
     k_set_by_mask<<<ceil_div(ns, 256), 256, 0, st>>>(g->view(), m, val, g->reso[0], g->reso[1],
                                                      g->reso[2]);
   PVDB_CHECK_LAUNCH("k_set_by_mask");
-  g->bmax_valid = false;
+  data_written(g);
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
   return PVDB_OK;
 }
@@ -780,6 +818,19 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
 
 
 
+int pvdb_grid_touched_leaves(pvdb_grid g, int64_t* n, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(g && n, "null argument");
+  *n = 0;
+  if (!g->d_tcount) return PVDB_OK;
+  uint32_t c = 0;
+  cudaStream_t st = as_stream(s);
+  PVDB_CHECK_CUDA(cudaMemcpyAsync(&c, g->d_tcount, 4, cudaMemcpyDeviceToHost, st));
+  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  *n = std::min<int64_t>(c, g->nleaf);
+  return PVDB_OK;
+}
+
 int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
   clear_error();
   PVDB_REQUIRE(g, "null grid");
@@ -801,7 +852,7 @@ int pvdb_grid_mark_written(pvdb_grid g, int32_t which) {
   clear_error();
   PVDB_REQUIRE(g, "null grid");
   PVDB_REQUIRE(which == PVDB_WHICH_DATA || which == PVDB_WHICH_GRAD, "bad `which`");
-  if (which == PVDB_WHICH_DATA) g->bmax_valid = false;
+  if (which == PVDB_WHICH_DATA) data_written(g);
   else g->all_touched = true;
   return PVDB_OK;
 }
@@ -812,7 +863,7 @@ int pvdb_grid_device_views(pvdb_grid g, void** data, void** grad, void** mask, v
   PVDB_REQUIRE(g, "null grid");
   if (data) {
     *data = g->d_data;
-    g->bmax_valid = false;  // the caller may write values we cannot track
+    data_written(g);  // the caller may write values we cannot track
   }
   if (grad) {
     *grad = g->d_grad;

@@ -543,7 +543,7 @@ __global__ void k_count_views_acc(const float* __restrict__ ro, const float* __r
                                           fminf(ta[2], tb[2])),
                                     a.near_),
                               1e9f);
-    const float dn = ray_norm(d[0], d[1], d[2]);  // rays_d.norm(dim=-1) (fma form)
+    const float dn = torch_norm3(d[0], d[1], d[2]);  // rays_d.norm(dim=-1)
     const float tk = __fadd_rn(t_min, __fdiv_rn(__fmul_rn(a.stepdist, float(k)), dn));
     float g[3];
     int g0[3];
@@ -766,7 +766,7 @@ int pvdb_grid_resample(pvdb_grid src, pvdb_grid dst, pvdb_stream s) {
     }
     PVDB_CHECK_LAUNCH("k_resample");
   }
-  dst->bmax_valid = false;
+  data_written(dst);
   return PVDB_OK;
 }
 
@@ -832,7 +832,7 @@ int pvdb_grid_maskout_near_cams(pvdb_grid g, const float* cam_o, int32_t n_cams,
     k_near_cams<<<ceil_div(n, 256), 256, 0, as_stream(s)>>>(a);
     PVDB_CHECK_LAUNCH("k_near_cams");
   }
-  g->bmax_valid = false;
+  data_written(g);
   return PVDB_OK;
 }
 

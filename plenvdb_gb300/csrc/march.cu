@@ -132,7 +132,7 @@ constexpr uint64_t kChainValue = kChainAgg - 1;
 constexpr uint32_t kChainSpinMax = 1u << 24;
 
 __global__ void __launch_bounds__(kMarchThreads)
-    k_march_chain(int R, MarchP P, MarchW W) {
+    k_march_chain(int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
   const int lane = threadIdx.x & 31;
   uint32_t ticket = 0;
   if (lane == 0) ticket = atomicAdd(W.totals + 6, 1u);
@@ -198,13 +198,14 @@ __global__ void __launch_bounds__(kMarchThreads)
   // publish, then look back 32 rays at a time
   const uint64_t agg = (uint64_t(nc) << 32) | uint64_t(uint32_t(nk));
   volatile uint64_t* status = W.chain_status;
-  if (lane == 0) status[r] = (r == 0 ? kChainPrefix : kChainAgg) | agg;
+  // (hold_first: the test hook of the bounded waits withholds ray 0's counts)
+  if (lane == 0 && !(hold_first && r == 0)) status[r] = (r == 0 ? kChainPrefix : kChainAgg) | agg;
   uint32_t ex_k = 0, ex_c = 0;  // exclusive prefix (kept, colour)
   for (int t = r - 1; t >= 0; t -= 32) {
     const int j = t - lane;
     uint64_t v = j >= 0 ? uint64_t(status[j]) : uint64_t(kChainPrefix);
     for (uint32_t it = 0; __any_sync(0xffffffffu, v == 0ull); ++it) {
-      if (it >= kChainSpinMax) {
+      if (it >= spin_max) {
         if (lane == 0) atomicOr(W.totals + 3, 4u);
         v = v ? v : uint64_t(kChainPrefix);  // give up: offsets wrong, but the kernel ends
         break;
@@ -292,6 +293,51 @@ __device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[
   }
 }
 
+// The 12-channel trilinear from the grid's BF16 shadow (the BF16 train step):
+// 24 bytes per corner in three 8-byte loads, FP32 interpolation in the order of
+// k0_trilinear.
+__device__ __forceinline__ void k0_trilinear_half(const GridView& g,
+                                                  const __nv_bfloat16* __restrict__ half,
+                                                  const float idx[3], float* out) {
+  const int i = ifloor(idx[0]), j = ifloor(idx[1]), k = ifloor(idx[2]);
+  float sc[8];
+  corner_scales(idx[0] - float(i), idx[1] - float(j), idx[2] - float(k), sc);
+  int slots[8];
+  corner_slots(g, i, j, k, slots);
+  uint2 raw[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    if (slots[c] >= 0) {
+      const uint2* src = reinterpret_cast<const uint2*>(half + int64_t(slots[c]) * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) raw[c][b] = __ldg(src + b);
+    }
+  }
+  float acc[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) acc[q] = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    float v[12];
+    if (slots[c] >= 0) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        v[4 * b] = __uint_as_float(raw[c][b].x << 16);
+        v[4 * b + 1] = __uint_as_float(raw[c][b].x & 0xFFFF0000u);
+        v[4 * b + 2] = __uint_as_float(raw[c][b].y << 16);
+        v[4 * b + 3] = __uint_as_float(raw[c][b].y & 0xFFFF0000u);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 12; ++q) v[q] = g.background;
+    }
+#pragma unroll
+    for (int q = 0; q < 12; ++q) acc[q] = __fadd_rn(acc[q], __fmul_rn(v[q], sc[c]));
+  }
+#pragma unroll
+  for (int q = 0; q < 12; ++q) out[q] = acc[q];
+}
+
 // k_march_k0 (thread per colour row): the k0 trilinear at the row's position
 // (colorvdb.cu:81-111).
 __global__ void __launch_bounds__(256)
@@ -315,7 +361,7 @@ __global__ void __launch_bounds__(256)
 // The padding rows of the last tile are zero.
 __global__ void __launch_bounds__(256)
     k_march_k0_x(GridView gk, MarchP P, MarchW W, const float* __restrict__ pe, int pe_stride,
-                 int dpe, uint8_t* xt) {
+                 int dpe, uint8_t* xt, const __nv_bfloat16* __restrict__ half) {
   const int64_t M = W.totals[1];
   const int64_t Mpad = (M + 127) / 128 * 128;
   const int C = gk.C, din = C + dpe;
@@ -330,7 +376,10 @@ __global__ void __launch_bounds__(256)
       float p[3], idx[3];
       ray_point(rs, P.stepdist, W.r_step[m], p);
       world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-      k0_trilinear(gk, idx, k0v);
+      if (half)
+        k0_trilinear_half(gk, half, idx, k0v);
+      else
+        k0_trilinear(gk, idx, k0v);
     }
     uint8_t* tile = xt + (m >> 7) * int64_t(kRgbXTile);
     const int row = int(m & 127);
@@ -905,7 +954,8 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     PVDB_CHECK_LAUNCH("k_march_setup");
     k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_alpha");
-    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w);
+    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w, debug_spin_limit(kChainSpinMax),
+                                                debug_hold_first());
     PVDB_CHECK_LAUNCH("k_march_chain");
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
@@ -927,14 +977,16 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
 // the rgbnet backward produces the k0-row gradients. with_k0: the k0 grid gets
 // gradients (its touched leaves are flagged too).
 // The fused k0 + X-tile pass (after a forward run with skip_k0); xt must hold
-// ceil(slots / 128) tiles.
+// ceil(slots / 128) tiles; half: the k0 grid's BF16 shadow to gather from
+// (NULL: the FP32 values).
 int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t* xt,
-               cudaStream_t st) {
+               cudaStream_t st, const __nv_bfloat16* half) {
   if (m->n_rays == 0 || !m->k0) return PVDB_OK;
+  PVDB_REQUIRE(!half || m->k0->C == 12, "the BF16 feature shadow is kept for 12 channels");
   PVDB_REQUIRE(m->k0->C <= 16 && m->k0->C + dpe + 1 <= kRgbXK,
                "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   const int grid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16));
-  k_march_k0_x<<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt);
+  k_march_k0_x<<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt, half);
   PVDB_CHECK_LAUNCH("k_march_k0_x");
   if (m->prof) prof_mark(st, 2);
   return PVDB_OK;
@@ -1113,7 +1165,11 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
     pvdb_march_destroy(m);
     return rc;
   }
+  // totals, and the row records' ray and step indices: rows that a forward
+  // does not write (after a look-back wait gave up) keep in-range values
   cudaError_t e = cudaMemset(w.totals, 0, 64);
+  if (e == cudaSuccess) e = cudaMemset(w.r_ray, 0, S * 4);
+  if (e == cudaSuccess) e = cudaMemset(w.r_step, 0, S * 4);
   if (e != cudaSuccess) {
     pvdb_march_destroy(m);
     return cuda_error(e, "cudaMemset");

@@ -429,7 +429,7 @@ static int mlp_reserve(pvdb_march_s* m, int din) {
 }
 
 int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* b1,
-                const float* w2, const float* b2, int c0, int dpe, int with_bwd, void** blob,
+                const float* w2, const float* b2, int c0, int dpe, void** blob,
                 size_t* blob_cap, cudaStream_t st);
 int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const float* b1,
                         const float* w2, const float* b2, int c0, int dpe, const float* k0rows,
@@ -452,7 +452,7 @@ int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R,
                                                  precision == 1 ? nullptr : m->hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
-    return mlp_tc_pack(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, 1, &m->mlp_packed,
+    return mlp_tc_pack(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, &m->mlp_packed,
                        &m->mlp_packed_cap, st);
   return PVDB_OK;
 }

@@ -34,10 +34,6 @@ constexpr uint32_t kOffW0 = 0;                             // W0f  [128 n][48 q]
 constexpr uint32_t kOffW1 = kOffW0 + 128 * kXK * 2;        // W1   [128 n][128 k]   12288
 constexpr uint32_t kOffW2 = kOffW1 + 128 * 128 * 2;        // W2p  [16 c][128 k]    45056
 constexpr uint32_t kPackFwdBytes = kOffW2 + 16 * 128 * 2;  // 49152
-constexpr uint32_t kOffW1T = kPackFwdBytes;                // W1T  [128 k][128 n]
-constexpr uint32_t kOffW0T = kOffW1T + 128 * 128 * 2;      // W0kT [16 q][128 n]    81920
-constexpr uint32_t kOffW2T = kOffW0T + 16 * 128 * 2;       // W2T  [128 n][16 c]    86016
-constexpr uint32_t kPackAllBytes = kOffW2T + 128 * 16 * 2;  // 90112
 // shared-memory layout of the forward kernel
 constexpr uint32_t kXTile = kRgbXTile;                // 12288 B: one X tile
 constexpr uint32_t kSmX = kPackFwdBytes;              // two X tiles [128 x 48] bf16
@@ -60,9 +56,9 @@ struct MlpArgsTc {
 };
 
 // FP32 nn.Linear weights -> BF16 canonical K-major tiles (one thread per
-// element). The forward uses the first kPackFwdBytes; the backward adds the
-// transposed tiles W1T [k][n], W0kT [q][n] and W2T [n][c].
-__global__ void k_pack(MlpArgsTc a, uint8_t* blob, int with_bwd) {
+// element). The backward reads the same tiles, transposed through MN-major
+// descriptors.
+__global__ void k_pack(MlpArgsTc a, uint8_t* blob) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   __nv_bfloat16* w0 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0);
   __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1);
@@ -79,22 +75,6 @@ __global__ void k_pack(MlpArgsTc a, uint8_t* blob, int with_bwd) {
   if (t < 16 * 128) {
     const int n = t / 128, k = t % 128;
     w2[tc::kmaj(n, k, 128) / 2] = __float2bfloat16_rn(n < 3 ? a.w2[n * 128 + k] : 0.f);
-  }
-  if (!with_bwd) return;
-  __nv_bfloat16* w1t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1T);
-  __nv_bfloat16* w0t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0T);
-  __nv_bfloat16* w2t = reinterpret_cast<__nv_bfloat16*>(blob + kOffW2T);
-  if (t < 128 * 128) {  // W1T[k][n] = w1[n][k]
-    const int k = t / 128, n = t % 128;
-    w1t[tc::kmaj(k, n, 128) / 2] = __float2bfloat16_rn(a.w1[n * 128 + k]);
-  }
-  if (t < 16 * 128) {  // W0kT[q][n] = w0[n][q] for q < c0
-    const int q = t / 128, n = t % 128;
-    w0t[tc::kmaj(q, n, 128) / 2] = __float2bfloat16_rn(q < a.c0 ? a.w0[n * a.din + q] : 0.f);
-  }
-  if (t < 128 * 16) {  // W2T[n][c] = w2[c][n] for c < 3
-    const int n = t / 16, c = t % 16;
-    w2t[tc::kmaj(n, c, 16) / 2] = __float2bfloat16_rn(c < 3 ? a.w2[c * 128 + n] : 0.f);
   }
 }
 
@@ -309,51 +289,63 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 }
 
 // ---------------------------------------------------------------- backward
-// Per 128-row tile (one CTA per SM, persistent, all 512 TMEM columns):
+// Per 128-row tile:
 //   recompute  Z0 = X.W0f^T -> H0 = relu(Z0);  Z1 = H0.W1^T -> H1 = relu(Z1 + b1)
 //   dl   = grad_rgb * y (1 - y)                       [128 x 3] (sigmoid backward)
-//   dZ1  = (dl . W2) * [H1 > 0]                       MMA K=16 (W2T)
-//   dZ0  = (dZ1 . W1) * [H0 > 0]                      MMA K=128 (W1T)
-//   gk0  = dZ0 . W0k                                  MMA N=16 (W0kT)
+//   dZ1  = (dl . W2) * [H1 > 0]
+//   dZ0  = (dZ1 . W1) * [H0 > 0]
+//   gk0  = dZ0 . W0k
 //   dW2 += H1^T . dl      dW1|db1 += dZ1^T . [H0|1]   dW0|db0 += dZ0^T . X
-// The three weight-gradient accumulators stay in TMEM across all tiles of the
-// CTA (a ones column in H0 and in X turns the bias sums into one more MMA
-// column); the transposed operands are the same shared-memory tiles read
-// through MN-major descriptors. db2 is a per-thread FP32 sum. At the end the
-// CTA writes its partial gradients in the flat parameter layout; the partials
-// are summed over CTAs in a fixed order, so the result is deterministic.
-//
-// Shared memory (bytes). The tiles read through MN-major descriptors come
-// first and the weights (86016 B) last. dZ0 reuses H1's buffer: H1's last
-// readers (the dW2 MMA and the dZ1 mask) are done before dZ0 is written.
-constexpr uint32_t kBdZ1 = 0;                        // dZ1 [128 r][128 n]
-constexpr uint32_t kBH1 = kBdZ1 + 128 * 128 * 2;     // H1, later dZ0 [128 r][128 n]
-constexpr uint32_t kBdZ0 = kBH1;
-constexpr uint32_t kBH0 = kBH1 + 128 * 128 * 2;      // H0  [128 r][144 k], col 128 = 1
-constexpr uint32_t kBX = kBH0 + 128 * 144 * 2;       // X x 2 [128 r][48 q]: k0 | PE | 1 | 0
-constexpr uint32_t kBDl = kBX + 2 * kXTile;          // dl  [128 r][16 c]
-constexpr uint32_t kBW = kBDl + 128 * 16 * 2;        // weights
-constexpr uint32_t kBW0f = kBW;                      // W0f  [128 n][48 q]
-constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;     // W1   [128 n][128 k]
-constexpr uint32_t kBW1T = kBW1 + 128 * 128 * 2;     // W1T  [128 k][128 n]
-constexpr uint32_t kBW0T = kBW1T + 128 * 128 * 2;    // W0kT [16 q][128 n]
-constexpr uint32_t kBW2T = kBW0T + 16 * 128 * 2;     // W2T  [128 n][16 c]
-constexpr uint32_t kBB1 = kBW2T + 128 * 16 * 2;      // b1 f32[128]
-constexpr uint32_t kBBar = kBB1 + 128 * 4;          // mbarriers: MMA, X0, X1, layer 0
-constexpr uint32_t kBTmem = kBBar + 32;
+// One persistent CTA per SM keeps two tiles in flight, in two slots with their
+// own shared-memory tiles and TMEM columns: while the four epilogue warps of
+// one slot drain TMEM and write the next operand, the tensor cores run the
+// other slot's MMAs. One elected thread of a ninth warp issues every MMA, in a
+// fixed order (stage k of slot 0, then stage k of slot 1, tile pair after tile
+// pair), so the weight-gradient accumulators, resident in TMEM across all the
+// CTA's tiles, sum in an order fixed by the data: bitwise reproducible.
+//   stage  MMAs (issuer)                                   epilogue (the slot's warps)
+//   S0     Z0 = X.W0f^T                -> A                E0  H0 = relu(Z0)
+//   S1     Z1 = H0.W1^T                -> A                E1  H1 = relu(Z1 + b1), dl
+//   S2     dZ1' = dl.W2 -> A;  dW2 += H1^T.dl              E2  dZ1 = dZ1'*[H1 > 0], over H1
+//   S3     dH0 = dZ1.W1 -> A;  dW1|db1 += dZ1^T.[H0|1]     E3  dZ0 = dH0*[H0 > 0], over dZ1
+//   S4     gk0 = dZ0.W0k -> G; dW0|db0 += dZ0^T.X          E4  gk0 -> global
+// A ones column in H0 and in X turns the bias sums into one more MMA column.
+// The backward's operands W2, W1 and W0k are the forward's K-major weight tiles
+// read through MN-major descriptors (no transposed copies). An epilogue
+// signals the issuer through its slot's mbarrier (128 arrivals) after a
+// proxy fence (its shared-memory writes feed the next MMAs) and a tcgen05
+// fence (its TMEM reads precede the next MMA into those columns); E4 instead
+// starts the bulk copy of the slot's next X tile, whose arrival releases S0.
+// At the end the CTA writes its partial weight gradients in the flat parameter
+// layout; the partials are summed over CTAs in a fixed order.
+constexpr int kBwdEpiWarps = 8;             // per slot: 4 lane quarters x 2 column halves
+constexpr int kBwdThreads = (2 * kBwdEpiWarps + 1) * 32;  // + the issuer warp: 544
+constexpr int kBwdIssuer = 2 * kBwdEpiWarps;  // warp index of the issuer
+constexpr uint32_t kSlH0 = 0;               // H0 [128 r][144 k], col 128 = 1
+constexpr uint32_t kSlH1 = kSlH0 + 128 * 144 * 2;  // H1, then dZ1, then dZ0 [128 r][128 n]
+constexpr uint32_t kSlX = kSlH1 + 128 * 128 * 2;   // X [128 r][48 q]: k0 | PE | 1 | 0
+constexpr uint32_t kSlDl = kSlX + kXTile;          // dl [128 r][16 c]
+constexpr uint32_t kSlot = kSlDl + 128 * 16 * 2;   // 86016 B per slot
+constexpr uint32_t kBW0f = 2 * kSlot;              // W0f [128 n][48 q]
+constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;   // W1  [128 n][128 k]
+constexpr uint32_t kBW2 = kBW1 + 128 * 128 * 2;    // W2p [16 c][128 k]
+constexpr uint32_t kBB1 = kBW2 + 16 * 128 * 2;     // b1 f32[128]
+constexpr uint32_t kBBar = kBB1 + 128 * 4;         // mma[2], epi[2], x[2], drain, weights
+constexpr uint32_t kBTmem = kBBar + 64;
 constexpr uint32_t kBFlag = kBTmem + 4;
-constexpr uint32_t kSmBwdBytes = kBFlag + 12;
-static_assert(kSmBwdBytes <= 232448, "backward tile exceeds 227 KB of shared memory");
-static_assert(kBW2T + 128 * 16 * 2 - kBW == (kOffW2 - kOffW0) + (kPackAllBytes - kOffW1T),
-              "backward weight region must hold W0f, W1, W1T, W0kT, W2T");
-// TMEM columns
-constexpr uint32_t kTA = 0;      // Z0, then dZ1 (pre-mask)
-constexpr uint32_t kTB = 128;    // Z1, then dH0
-constexpr uint32_t kTG = 256;    // grad k0 [128 x 16]
-constexpr uint32_t kTW2 = 272;   // dW2 [128 n x 16 c]
-constexpr uint32_t kTW0 = 288;   // dW0|db0 [128 n x 48 q]
-constexpr uint32_t kTW1 = 336;   // dW1|db1 [128 n x 144 k]
+constexpr uint32_t kBXIssued = kBFlag + 4;         // X copies started, per slot
+constexpr uint32_t kSmBwdBytes = kBXIssued + 8;
+static_assert(kSlot % 1024 == 0, "slot tiles keep their alignment");
+static_assert(kBW2 + 16 * 128 * 2 - kBW0f == kPackFwdBytes, "weight region = the forward blob");
+static_assert(kSmBwdBytes <= 232448, "backward CTA exceeds 227 KB of shared memory");
+// TMEM columns: per slot A (128) and G (16); the resident weight-gradient sums
+constexpr uint32_t kTA0 = 0;     // slot s: kTA0 + 128*s  (Z0, Z1, dZ1', dH0)
+constexpr uint32_t kTG0 = 256;   // slot s: kTG0 + 16*s   (grad k0)
+constexpr uint32_t kTW2 = 288;   // dW2 [128 n x 16 c]
+constexpr uint32_t kTW0 = 304;   // dW0|db0 [128 n x 48 q]
+constexpr uint32_t kTW1 = 352;   // dW1|db1 [128 n x 144 k]
 constexpr uint32_t kTmemBwdCols = 512;
+static_assert(kTW1 + 144 <= kTmemBwdCols, "TMEM columns");
 
 __device__ __forceinline__ bool bf16_pos(uint32_t bits16) { return (bits16 & 0x7FFFu) != 0u; }
 
@@ -374,10 +366,32 @@ __device__ __forceinline__ uint4 mask_pack(const float* v, uint4 h) {
   return pk;
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+// Bounded wait that also gives up as soon as another role has (flag set).
+__device__ __forceinline__ bool bwait(uint64_t* bar, uint32_t parity, uint32_t* flag,
+                                      uint32_t* err, uint32_t spin_max) {
+  for (uint32_t i = 0; i < spin_max; ++i) {
+    if (tc::mbar_try(bar, parity)) return true;
+    if ((i & 31u) == 31u && *((volatile uint32_t*)flag)) return false;
+  }
+  atomicOr(flag, 1u);
+  if (err) atomicOr(err, 2u);
+  return false;
+}
+
+// The slot's epilogue threads: results written to shared memory are made
+// visible to the tensor cores, TMEM reads are ordered before the next MMA,
+// then the thread arrives on the slot's epilogue barrier.
+__device__ __forceinline__ void epi_done(uint64_t* bar) {
+  tc::fence_async_smem();
+  tc::fence_before();
+  tc::mbar_arrive(bar);
+}
+
+__global__ void __launch_bounds__(kBwdThreads, 1)
     k_mlp_bwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const uint8_t* __restrict__ xt,
                  const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
-                 const float* __restrict__ grad_rgb, float* grad_k0, float* wpart, uint32_t* err) {
+                 const float* __restrict__ grad_rgb, float* grad_k0, float* wpart, uint32_t* err,
+                 uint32_t spin_max, int hold) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
   const int64_t ntiles = (M + 127) / 128;
@@ -390,39 +404,48 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   float* pw2 = pb1 + kW;
   float* pb2 = pw2 + 3 * kW;
   if (blockIdx.x >= ntiles) {
-    for (int64_t i = tid; i < P; i += kTcThreads) pw0[i] = 0.f;
+    for (int64_t i = tid; i < P; i += kBwdThreads) pw0[i] = 0.f;
     return;
   }
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kBBar);
+  // this CTA's tiles: t_j = blockIdx.x + j * gridDim.x, j < nj; tile j goes to slot j & 1
+  const int nj = int((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kBBar);  // [2] MMA stage done
+  uint64_t* ebar = mbar + 2;                                  // [2] epilogue done
+  uint64_t* xbar = mbar + 4;                                  // [2] X tile landed
+  uint64_t* dbar = mbar + 6;                                  // drain
+  uint64_t* wbar = mbar + 7;                                  // weight tiles landed
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kBTmem);
   uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kBFlag);
+  uint32_t* xissued = reinterpret_cast<uint32_t*>(sm + kBXIssued);
   float* b1s = reinterpret_cast<float*>(sm + kBB1);
-  {
-    const int4* src = reinterpret_cast<const int4*>(blob);
-    int4* dst = reinterpret_cast<int4*>(sm + kBW);
-    // W0f, W1 (blob 0..45056) and W1T, W0kT, W2T (blob 49152..90112)
-    for (int i = tid; i < int(kOffW2 / 16); i += kTcThreads) dst[i] = __ldg(src + i);
-    for (int i = tid; i < int((kPackAllBytes - kOffW1T) / 16); i += kTcThreads)
-      dst[kOffW2 / 16 + i] = __ldg(src + kOffW1T / 16 + i);
+  if (tid < 128) b1s[tid] = a.b1[tid];
+  if (tid < 256) {
+    // H0 columns 128..143 of both slots: [1, 0 x 15] for every row
+    const int s = tid >> 7, r = tid & 127;
+    uint8_t* h0 = sm + s * kSlot + kSlH0;
+    *reinterpret_cast<uint4*>(h0 + tc::kmaj(r, 128, 144)) =
+        make_uint4(tc::pack_bf16(1.f, 0.f), 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(h0 + tc::kmaj(r, 136, 144)) = make_uint4(0u, 0u, 0u, 0u);
   }
-  if (tid < 128) {
-    b1s[tid] = a.b1[tid];
-    // H0 columns 128..143: [1, 0 x 15] for every row
-    uint4 one = make_uint4(tc::pack_bf16(1.f, 0.f), 0u, 0u, 0u);
-    *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 128, 144)) = one;
-    *reinterpret_cast<uint4*>(sm + kBH0 + tc::kmaj(tid, 136, 144)) = make_uint4(0u, 0u, 0u, 0u);
-  }
-  uint64_t* xbar = bar + 1;  // X tile barriers, one per buffer
-  uint64_t* lbar = bar + 3;  // layer-0 MMA of a tile, issued during the previous tile
-  if (tid == 0) {
+  if (tid == kBwdIssuer * 32) {
     *flag = 0;
-    tc::mbar_init(bar, 1);
+    tc::mbar_init(mbar, 1);
+    tc::mbar_init(mbar + 1, 1);
+    tc::mbar_init(ebar, 32 * kBwdEpiWarps);
+    tc::mbar_init(ebar + 1, 32 * kBwdEpiWarps);
     tc::mbar_init(xbar, 1);
     tc::mbar_init(xbar + 1, 1);
-    tc::mbar_init(lbar, 1);
-    x_fetch(sm + kBX, xt, blockIdx.x, xbar);
+    tc::mbar_init(dbar, 1);
+    tc::mbar_init(wbar, 1);
+    // the weight tiles (the forward's blob) in one bulk copy
+    tc::mbar_expect_tx(wbar, kPackFwdBytes);
+    tc::bulk_g2s(sm + kBW0f, blob, kPackFwdBytes, wbar);
+    for (int s = 0; s < 2; ++s) {
+      xissued[s] = s < nj ? 1u : 0u;
+      if (s < nj) x_fetch(sm + s * kSlot + kSlX, xt, blockIdx.x + int64_t(s) * gridDim.x, xbar + s);
+    }
   }
-  if (warp == 0) {
+  if (warp == kBwdIssuer) {
     tc::tmem_alloc(tmem_slot, kTmemBwdCols);
     tc::tmem_relinquish();
   }
@@ -431,223 +454,249 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc::fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t sb = tc::smem_addr(sm);
-  const uint32_t id_r128 = tc::idesc_bf16(128, 128);              // K-major A and B
-  const uint32_t id_r16 = tc::idesc_bf16(128, 16);                // grad k0
-  const uint32_t id_w2 = tc::idesc_bf16(128, 16, true, true);     // H1^T . dl
-  const uint32_t id_w1 = tc::idesc_bf16(128, 144, true, true);    // dZ1^T . H0
-  const uint32_t id_w0 = tc::idesc_bf16(128, 48, true, true);     // dZ0^T . X
-  const int q4 = warp & 3, half = warp >> 2;
-  const int row = 32 * q4 + lane;
-  const uint32_t t_lane = tmem + (uint32_t(32 * q4) << 16);
   float db2[3] = {0.f, 0.f, 0.f};
-  uint32_t phase = 0, lph = 0, xph[2] = {0u, 0u};
-  bool ok = true, first = true;
-  // layer 0 of tile t into TMEM columns kTA (free once the previous tile's
-  // dZ1 has been read); issued by thread 0 after its X tile has landed
-  auto issue_l0 = [&](int buf) {
-    if (!tc::mbar_wait(xbar + buf, xph[buf], kWaitIters)) {
-      atomicOr(flag, 1u);
-      if (err) atomicOr(err, 2u);
-      return;
-    }
-    tc::fence_after();
-#pragma unroll
-    for (int s = 0; s < 3; ++s)
-      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBX + uint32_t(buf) * kXTile + 256 * s, 128, 768),
-                   tc::make_desc(sb + kBW0f + 256 * s, 128, 768), id_r128, s > 0);
-    tc::mma_commit(lbar);
-  };
-  int it = 0;
-  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
-    const int64_t row0 = t * 128;
-    const int64_t mrow = row0 + row;
-    const int xb = it & 1;
-    const uint32_t kBXt = kBX + uint32_t(xb) * kXTile;  // this tile's X buffer
-    // sigmoid inputs of this thread's row (warps 0-3), read early
-    float yv[3] = {0.f, 0.f, 0.f}, gv[3] = {0.f, 0.f, 0.f};
-    if (half == 0 && mrow < M) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        yv[c] = __ldg(rgb + mrow * 3 + c);
-        gv[c] = __ldg(grad_rgb + mrow * 3 + c);
+  uint32_t xwaits[2] = {0u, 0u};  // X arrivals the issuer consumed, per slot
+  bool wdone = false;             // the issuer saw the weight copy land
+
+  if (warp == kBwdIssuer) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0 && !hold) {
+      const uint32_t id_kk = tc::idesc_bf16(128, 128);               // A, B K-major
+      const uint32_t id_kn = tc::idesc_bf16(128, 128, false, true);  // B MN-major
+      const uint32_t id_g = tc::idesc_bf16(128, 16, false, true);    // grad k0
+      const uint32_t id_w2 = tc::idesc_bf16(128, 16, true, true);    // H1^T . dl
+      const uint32_t id_w1 = tc::idesc_bf16(128, 144, true, true);   // dZ1^T . [H0|1]
+      const uint32_t id_w0 = tc::idesc_bf16(128, 48, true, true);    // dZ0^T . X
+      uint32_t eph[2] = {0u, 0u}, xph[2] = {0u, 0u};
+      bool w2_on = false, w1_on = false, w0_on = false;
+      bool ok = wdone = bwait(wbar, 0, flag, err, spin_max);
+      for (int pair = 0; ok && 2 * pair < nj; ++pair) {
+        for (int k = 0; ok && k < 5; ++k) {
+          for (int s = 0; ok && s < 2; ++s) {
+            if (2 * pair + s >= nj) continue;
+            if (k == 0) {
+              ok = bwait(xbar + s, xph[s], flag, err, spin_max);
+              if (ok) {
+                xph[s] ^= 1u;
+                xwaits[s]++;
+              }
+            } else {
+              ok = bwait(ebar + s, eph[s], flag, err, spin_max);
+              eph[s] ^= 1u;
+            }
+            if (!ok) break;
+            tc::fence_after();
+            // descriptors advance by (byte step >> 4) in their address field;
+            // the loops stay rolled so the single issuing thread keeps few
+            // registers live
+            const uint32_t sl = sb + uint32_t(s) * kSlot;
+            const uint32_t tA = tmem + kTA0 + 128u * uint32_t(s);
+            if (k == 0) {  // Z0 = X . W0f^T
+              uint64_t da = tc::make_desc(sl + kSlX, 128, 768);
+              uint64_t db = tc::make_desc(sb + kBW0f, 128, 768);
+#pragma unroll 1
+              for (int q = 0; q < 3; ++q, da += 256 >> 4, db += 256 >> 4)
+                tc::mma_bf16(tA, da, db, id_kk, q > 0);
+            } else if (k == 1) {  // Z1 = H0 . W1^T
+              uint64_t da = tc::make_desc(sl + kSlH0, 128, 2304);
+              uint64_t db = tc::make_desc(sb + kBW1, 128, 2048);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 256 >> 4)
+                tc::mma_bf16(tA, da, db, id_kk, q > 0);
+            } else if (k == 2) {  // dZ1' = dl . W2;  dW2 += H1^T . dl
+              tc::mma_bf16(tA, tc::make_desc(sl + kSlDl, 128, 256),
+                           tc::make_desc(sb + kBW2, 2048, 128), id_kn, 0);
+              uint64_t da = tc::make_desc(sl + kSlH1, 2048, 128);
+              uint64_t db = tc::make_desc(sl + kSlDl, 256, 128);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 4096 >> 4, db += 512 >> 4)
+                tc::mma_bf16(tmem + kTW2, da, db, id_w2, (w2_on || q > 0) ? 1u : 0u);
+              w2_on = true;
+            } else if (k == 3) {  // dH0 = dZ1 . W1;  dW1|db1 += dZ1^T . [H0|1]
+              uint64_t da = tc::make_desc(sl + kSlH1, 128, 2048);
+              uint64_t db = tc::make_desc(sb + kBW1, 2048, 128);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 4096 >> 4)
+                tc::mma_bf16(tA, da, db, id_kn, q > 0);
+              da = tc::make_desc(sl + kSlH1, 2048, 128);
+              db = tc::make_desc(sl + kSlH0, 2304, 128);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 4096 >> 4, db += 4608 >> 4)
+                tc::mma_bf16(tmem + kTW1, da, db, id_w1, (w1_on || q > 0) ? 1u : 0u);
+              w1_on = true;
+            } else {  // grad k0 = dZ0 . W0k;  dW0|db0 += dZ0^T . X
+              const uint32_t tG = tmem + kTG0 + 16u * uint32_t(s);
+              uint64_t da = tc::make_desc(sl + kSlH1, 128, 2048);
+              uint64_t db = tc::make_desc(sb + kBW0f, 768, 128);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 1536 >> 4)
+                tc::mma_bf16(tG, da, db, id_g, q > 0);
+              da = tc::make_desc(sl + kSlH1, 2048, 128);
+              db = tc::make_desc(sl + kSlX, 768, 128);
+#pragma unroll 1
+              for (int q = 0; q < 8; ++q, da += 4096 >> 4, db += 1536 >> 4)
+                tc::mma_bf16(tmem + kTW0, da, db, id_w0, (w0_on || q > 0) ? 1u : 0u);
+              w0_on = true;
+            }
+            tc::mma_commit(mbar + s);
+          }
+        }
       }
     }
-    const bool has_next = t + gridDim.x < ntiles;
-    // the next tile's X travels while this tile computes (its buffer was last
-    // read by the previous tile's dW0 MMA, complete)
-    if (tid == 0 && has_next)
-      x_fetch(sm + kBX + uint32_t(xb ^ 1) * kXTile, xt, t + gridDim.x, xbar + (xb ^ 1));
-    if (it == 0) {
-      if (tid == 0) issue_l0(xb);
-      xph[xb] ^= 1u;
-    }
-    ok = wait_or_flag(lbar, lph, flag, err);
-    lph ^= 1u;
-    if (!ok) break;
-    tc::fence_after();
-    // ---- H0 = relu(Z0)
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      float v[32];
-      tc::tmem_ld32(t_lane + kTA + uint32_t(64 * half + 32 * j), v);
-      store_relu32(sm + kBH0, row, 64 * half + 32 * j, 144, v, nullptr);
-    }
-    tc::fence_before();
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTB, tc::make_desc(sb + kBH0 + 256 * s, 128, 2304),
-                     tc::make_desc(sb + kBW1 + 256 * s, 128, 2048), id_r128, s > 0);
-      tc::mma_commit(bar);
-    }
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
-    if (!ok) break;
-    tc::fence_after();
-    // ---- H1 = relu(Z1 + b1); dl = grad_rgb * y * (1 - y)
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      float v[32];
-      tc::tmem_ld32(t_lane + kTB + uint32_t(64 * half + 32 * j), v);
-      store_relu32(sm + kBH1, row, 64 * half + 32 * j, 128, v, b1s);
-    }
-    if (half == 0) {
-      float d[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        d[c] = gv[c] * (1.f - yv[c]) * yv[c];
-        db2[c] += d[c];
-      }
-      *reinterpret_cast<uint4*>(sm + kBDl + tc::kmaj(row, 0, 16)) =
-          make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
-      *reinterpret_cast<uint4*>(sm + kBDl + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
-    }
-    tc::fence_before();
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      // dZ1 (pre-mask) = dl . W2
-      tc::mma_bf16(tmem + kTA, tc::make_desc(sb + kBDl, 128, 256),
-                   tc::make_desc(sb + kBW2T, 128, 256), id_r128, 0);
-      // dW2 += H1^T . dl  (A: H1 MN-major, B: dl MN-major; K = rows)
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTW2, tc::make_desc(sb + kBH1 + 4096 * s, 2048, 128),
-                     tc::make_desc(sb + kBDl + 512 * s, 256, 128), id_w2, (!first || s > 0));
-      tc::mma_commit(bar);
-    }
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
-    if (!ok) break;
-    tc::fence_after();
-    // ---- dZ1 = (dl . W2) * [H1 > 0]
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      float v[32];
-      const int cb = 64 * half + 32 * j;
-      tc::tmem_ld32(t_lane + kTA + uint32_t(cb), v);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const uint32_t off = tc::kmaj(row, cb + 8 * c, 128);
-        const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH1 + off);
-        *reinterpret_cast<uint4*>(sm + kBdZ1 + off) = mask_pack(v + 8 * c, h);
-      }
-    }
-    tc::fence_before();
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      // dH0 = dZ1 . W1
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTB, tc::make_desc(sb + kBdZ1 + 256 * s, 128, 2048),
-                     tc::make_desc(sb + kBW1T + 256 * s, 128, 2048), id_r128, s > 0);
-      // dW1|db1 += dZ1^T . [H0 | 1]
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTW1, tc::make_desc(sb + kBdZ1 + 4096 * s, 2048, 128),
-                     tc::make_desc(sb + kBH0 + 4608 * s, 2304, 128), id_w1, (!first || s > 0));
-      tc::mma_commit(bar);
-      // the next tile's layer 0 runs behind these on the tensor pipe
-      if (has_next) issue_l0(xb ^ 1);
-    }
-    if (has_next) xph[xb ^ 1] ^= 1u;
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
-    if (!ok) break;
-    tc::fence_after();
-    // ---- dZ0 = dH0 * [H0 > 0]  (into H1's buffer)
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      float v[32];
-      const int cb = 64 * half + 32 * j;
-      tc::tmem_ld32(t_lane + kTB + uint32_t(cb), v);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const uint4 h = *reinterpret_cast<const uint4*>(sm + kBH0 + tc::kmaj(row, cb + 8 * c, 144));
-        *reinterpret_cast<uint4*>(sm + kBdZ0 + tc::kmaj(row, cb + 8 * c, 128)) = mask_pack(v + 8 * c, h);
-      }
-    }
-    tc::fence_before();
-    tc::fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      // grad k0 = dZ0 . W0k
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTG, tc::make_desc(sb + kBdZ0 + 256 * s, 128, 2048),
-                     tc::make_desc(sb + kBW0T + 256 * s, 128, 2048), id_r16, s > 0);
-      // dW0|db0 += dZ0^T . X
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        tc::mma_bf16(tmem + kTW0, tc::make_desc(sb + kBdZ0 + 4096 * s, 2048, 128),
-                     tc::make_desc(sb + kBXt + 1536 * s, 768, 128), id_w0, (!first || s > 0));
-      tc::mma_commit(bar);
-    }
-    ok = wait_or_flag(bar, phase, flag, err);
-    phase ^= 1;
-    if (!ok) break;
-    tc::fence_after();
-    if (half == 0) {
-      float v[16];
-      tc::tmem_ld16(t_lane + kTG, v);
-      if (mrow < M) {
-#pragma unroll
-        for (int qq = 0; qq < 16; ++qq)
-          if (qq < a.c0) grad_k0[mrow * a.c0 + qq] = v[qq];
-      }
-    }
-    first = false;
-    tc::fence_before();
-    __syncthreads();
-  }
-  if (!ok) {
-    // a wait gave up: one more bounded wait for the MMAs and X copies in
-    // flight before their TMEM and shared memory are released
-    tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
-    tc::mbar_wait(lbar, lph, kWaitIters);
-    tc::mbar_wait(xbar, xph[0], kWaitIters);
-    tc::mbar_wait(xbar + 1, xph[1], kWaitIters);
-    __syncthreads();
-    for (int64_t i = tid; i < P; i += kTcThreads) pw0[i] = 0.f;
+    __syncwarp();
   } else {
+    // ------------------------------------------------- epilogues of slot s
+    // warp (s, q4, half): TMEM lanes / tile rows 32*q4.., columns 64*half..
+    const int s = warp / kBwdEpiWarps, w8 = warp % kBwdEpiWarps;
+    const int q4 = w8 & 3, half = w8 >> 2;
+    const int row = 32 * q4 + lane;
+    const int c0 = 64 * half;
+    const uint32_t tl = tmem + (uint32_t(32 * q4) << 16);
+    const uint32_t tA = tl + kTA0 + 128u * uint32_t(s) + uint32_t(c0);
+    const uint32_t tG = tl + kTG0 + 16u * uint32_t(s);
+    uint8_t* h0 = sm + s * kSlot + kSlH0;
+    uint8_t* h1 = sm + s * kSlot + kSlH1;
+    uint8_t* dl = sm + s * kSlot + kSlDl;
+    const bool vec_k0 = (a.c0 & 3) == 0;
+    uint32_t mph = 0;
+    bool ok = true;
+    for (int j = s; ok && j < nj; j += 2) {
+      const int64_t mrow = (int64_t(blockIdx.x) + int64_t(j) * gridDim.x) * 128 + row;
+      // sigmoid inputs of this row, read before the first wait (column half 0)
+      float yv[3] = {0.f, 0.f, 0.f}, gv[3] = {0.f, 0.f, 0.f};
+      if (half == 0 && mrow < M) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          yv[c] = __ldg(rgb + mrow * 3 + c);
+          gv[c] = __ldg(grad_rgb + mrow * 3 + c);
+        }
+      }
+      // ---- E0: H0 = relu(Z0)
+      if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
+      mph ^= 1u;
+      tc::fence_after();
+#pragma unroll
+      for (int cb = 0; cb < 64; cb += 32) {
+        float v[32];
+        tc::tmem_ld32(tA + uint32_t(cb), v);
+        store_relu32(h0, row, c0 + cb, 144, v, nullptr);
+      }
+      epi_done(ebar + s);
+      // ---- E1: H1 = relu(Z1 + b1); dl = grad_rgb * y * (1 - y)
+      if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
+      mph ^= 1u;
+      tc::fence_after();
+#pragma unroll
+      for (int cb = 0; cb < 64; cb += 32) {
+        float v[32];
+        tc::tmem_ld32(tA + uint32_t(cb), v);
+        store_relu32(h1, row, c0 + cb, 128, v, b1s);
+      }
+      if (half == 0) {
+        float d[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          d[c] = gv[c] * (1.f - yv[c]) * yv[c];
+          db2[c] += d[c];
+        }
+        *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 0, 16)) =
+            make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
+        *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+      }
+      epi_done(ebar + s);
+      // ---- E2: dZ1 = (dl . W2) * [H1 > 0], in place over H1
+      if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
+      mph ^= 1u;
+      tc::fence_after();
+#pragma unroll
+      for (int cb = 0; cb < 64; cb += 32) {
+        float v[32];
+        tc::tmem_ld32(tA + uint32_t(cb), v);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint4* p = reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128));
+          *p = mask_pack(v + 8 * c, *p);
+        }
+      }
+      epi_done(ebar + s);
+      // ---- E3: dZ0 = dH0 * [H0 > 0], over dZ1
+      if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
+      mph ^= 1u;
+      tc::fence_after();
+#pragma unroll
+      for (int cb = 0; cb < 64; cb += 32) {
+        float v[32];
+        tc::tmem_ld32(tA + uint32_t(cb), v);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const uint4 h =
+              *reinterpret_cast<const uint4*>(h0 + tc::kmaj(row, c0 + cb + 8 * c, 144));
+          *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128)) =
+              mask_pack(v + 8 * c, h);
+        }
+      }
+      epi_done(ebar + s);
+      // ---- E4: grad k0; the slot's X buffer is free again (S4 is done)
+      if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
+      mph ^= 1u;
+      tc::fence_after();
+      if (w8 == 0 && lane == 0 && j + 2 < nj) {
+        xissued[s] += 1u;
+        x_fetch(sm + s * kSlot + kSlX, xt, blockIdx.x + int64_t(j + 2) * gridDim.x, xbar + s);
+      }
+      if (half == 0) {
+        float v[16];
+        tc::tmem_ld16(tG, v);
+        if (mrow < M) {
+          float* dst = grad_k0 + mrow * a.c0;
+          if (vec_k0) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+              if (4 * b < a.c0)
+                reinterpret_cast<float4*>(dst)[b] =
+                    make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
+          } else {
+#pragma unroll
+            for (int qq = 0; qq < 16; ++qq)
+              if (qq < a.c0) dst[qq] = v[qq];
+          }
+        }
+      }
+      tc::fence_before();
+    }
+  }
+  // ---------------------------------------------------------------- teardown
+  __syncthreads();
+  const bool failed = *((volatile uint32_t*)flag) != 0;
+  if (warp == kBwdIssuer && lane == 0) {
+    // every MMA this thread issued completes before TMEM is released; copies
+    // still in flight (a wait gave up) land before shared memory is released
+    if (!hold) {
+      tc::mma_commit(dbar);
+      tc::mbar_wait(dbar, 0, spin_max);
+    }
+    if (!wdone) tc::mbar_wait(wbar, 0, spin_max);
+    for (int s = 0; s < 2; ++s)  // at most one copy per slot is outstanding
+      if (xissued[s] > xwaits[s]) tc::mbar_wait(xbar + s, xwaits[s] & 1u, spin_max);
+  }
+  __syncthreads();
+  if (failed) {
+    for (int64_t i = tid; i < P; i += kBwdThreads) pw0[i] = 0.f;
+  } else if (warp < 8) {
     tc::fence_after();
     // partial gradients of this CTA: thread (q4, lane) holds row n = 32*q4 + lane
-    const int n = row;
+    const int q4 = warp & 3, half = warp >> 2;
+    const int n = 32 * q4 + lane;
+    const uint32_t tl = tmem + (uint32_t(32 * q4) << 16);
+    float v[16];
+    float4* w1row = reinterpret_cast<float4*>(pw1 + n * kW);  // 512 B per row, aligned
     if (half == 0) {
-      float v[16];
-      tc::tmem_ld16(t_lane + kTW2, v);
+      tc::tmem_ld16(tl + kTW2, v);
 #pragma unroll
       for (int c = 0; c < 3; ++c) pw2[c * kW + n] = v[c];
 #pragma unroll
       for (int j = 0; j < 2; ++j) {  // dW0|db0 columns 0..31
-        tc::tmem_ld16(t_lane + kTW0 + 16 * j, v);
+        tc::tmem_ld16(tl + kTW0 + 16 * j, v);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int qq = 16 * j + i;
@@ -657,15 +706,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {  // dW1 columns 0..63
-        tc::tmem_ld16(t_lane + kTW1 + 16 * j, v);
+        tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) pw1[n * kW + 16 * j + i] = v[i];
+        for (int b = 0; b < 4; ++b)
+          w1row[4 * j + b] = make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
       }
-      tc::tmem_ld16(t_lane + kTW1 + 128, v);  // db1
+      tc::tmem_ld16(tl + kTW1 + 128, v);  // db1
       pb1[n] = v[0];
     } else {
-      float v[16];
-      tc::tmem_ld16(t_lane + kTW0 + 32, v);  // dW0|db0 columns 32..47
+      tc::tmem_ld16(tl + kTW0 + 32, v);  // dW0|db0 columns 32..47
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int qq = 32 + i;
@@ -674,42 +723,47 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
 #pragma unroll
       for (int j = 4; j < 8; ++j) {  // dW1 columns 64..127
-        tc::tmem_ld16(t_lane + kTW1 + 16 * j, v);
+        tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) pw1[n * kW + 16 * j + i] = v[i];
+        for (int b = 0; b < 4; ++b)
+          w1row[4 * j + b] = make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
       }
     }
-    // db2: fixed-order block sum of the per-row partials (X tile as scratch)
-    float* red = reinterpret_cast<float*>(sm + kBX);
-    __syncthreads();
-    if (half == 0)
-      for (int c = 0; c < 3; ++c) red[c * 128 + row] = db2[c];
+  }
+  if (!failed) {
+    // db2: fixed-order sum of the per-row partials of both slots (slot 0's X
+    // buffer as scratch: no copy or MMA touches it any more)
+    float* red = reinterpret_cast<float*>(sm + kSlX);
+    if (warp < 2 * kBwdEpiWarps && ((warp % kBwdEpiWarps) >> 2) == 0) {
+      const int idx = (warp / kBwdEpiWarps) * 128 + 32 * (warp & 3) + lane;
+      for (int c = 0; c < 3; ++c) red[c * 256 + idx] = db2[c];
+    }
     __syncthreads();
     if (tid < 3) {
       float acc = 0.f;
-      for (int i = 0; i < 128; ++i) acc += red[tid * 128 + i];
+      for (int i = 0; i < 256; ++i) acc += red[tid * 256 + i];
       pb2[tid] = acc;
     }
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  if (warp == 0) tc::tmem_dealloc(tmem, kTmemBwdCols);
+  if (warp == kBwdIssuer) tc::tmem_dealloc(tmem, kTmemBwdCols);
 }
 
 }  // namespace
 
-// Packs the FP32 weights into the BF16 tile blob (forward tiles, plus the
-// backward's transposed tiles when with_bwd).
+// Packs the FP32 weights into the BF16 tile blob (read by the forward and,
+// transposed, by the backward).
 int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* b1,
-                const float* w2, const float* b2, int c0, int dpe, int with_bwd, void** blob,
+                const float* w2, const float* b2, int c0, int dpe, void** blob,
                 size_t* blob_cap, cudaStream_t st) {
   if (c0 > 16 || c0 + dpe + 1 > kXK)
     return set_error(PVDB_ERR_ARG, "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
-  int rc = dev_reserve(blob, blob_cap, kPackAllBytes);
+  int rc = dev_reserve(blob, blob_cap, kPackFwdBytes);
   if (rc) return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
-  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob), with_bwd);
+  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob));
   PVDB_CHECK_LAUNCH("k_pack");
   return PVDB_OK;
 }
@@ -741,7 +795,7 @@ int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const
                         size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
                         cudaStream_t st, int packed, int x_ready) {
   int rc = PVDB_OK;
-  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 0, blob, blob_cap, st)))
+  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, blob, blob_cap, st)))
     return rc;
   if (!x_ready && (rc = mlp_tc_build_x(c0, dpe, k0rows, ray, pe, pe_stride, totals, max_rows, xt,
                                        xt_cap, st)))
@@ -765,16 +819,16 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
                          void** blob, size_t* blob_cap, void** xt, size_t* xt_cap, uint32_t* err,
                          cudaStream_t st, int packed, int x_ready) {
   int rc = PVDB_OK;
-  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, 1, blob, blob_cap, st)))
+  if (!packed && (rc = mlp_tc_pack(w0, b0, w1, b1, w2, b2, c0, dpe, blob, blob_cap, st)))
     return rc;
   if (!x_ready && (rc = mlp_tc_build_x(c0, dpe, k0rows, ray, pe, pe_stride, totals, max_rows, xt,
                                        xt_cap, st)))
     return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
-  k_mlp_bwd_tc<<<grid, kTcThreads, kSmBwdBytes, st>>>(a, static_cast<const uint8_t*>(*blob),
-                                                      static_cast<const uint8_t*>(*xt), totals, rgb,
-                                                      grad_rgb, grad_k0, wpart, err);
+  k_mlp_bwd_tc<<<grid, kBwdThreads, kSmBwdBytes, st>>>(
+      a, static_cast<const uint8_t*>(*blob), static_cast<const uint8_t*>(*xt), totals, rgb,
+      grad_rgb, grad_k0, wpart, err, debug_spin_limit(kWaitIters), debug_hold_first());
   PVDB_CHECK_LAUNCH("k_mlp_bwd_tc");
   return PVDB_OK;
 }

@@ -9,8 +9,11 @@
 // histograms, scan partials) in one fixed file-scope device array, so the call
 // itself allocates nothing. The caller still passes the points, the gradients
 // and the grid (device memory). The array holds kNoAllocMaxPoints points'
-// worth of scratch (about 5.3 MB) on every GPU that loads the library, until
-// the process exits.
+// worth of scratch (about 5.3 MB) on every GPU where the library's module is
+// loaded, until the process exits. With CUDA's lazy module loading (the
+// default) the module, and so the array, is loaded on a device by the first
+// call of this entry point there, which also looks up the array's address:
+// make that first call before reserving a memory pool or capturing a stream.
 #include <mutex>
 
 #include "reduce.cuh"
@@ -29,8 +32,10 @@ constexpr int64_t kNoAllocWords = 4 * kNoAllocMaxPairs + kNoAllocHistWords + kNo
 
 // Shared by every call on a device. Within one call every word is written
 // before it is read (keys and payloads for the call's pairs, histogram tiles,
-// partials, size words), so nothing needs clearing between calls; calls that
-// overlap on the GPU (e.g. issued on two streams) race on it.
+// partials, size words, the sort's status word, which the sort clears first),
+// so nothing needs clearing between calls; calls that overlap on the GPU
+// (e.g. issued on two streams) race on it, so serialise them on one stream
+// per device.
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
 namespace {
@@ -114,14 +119,18 @@ extern "C" int pvdb_grid_sample_backward_noalloc(pvdb_grid g, const float* xs, c
   k_noalloc_keys<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), xs, ys, zs, n, rs.keys[0]);
   PVDB_CHECK_LAUNCH("k_noalloc_keys");
   int buf = 0;
-  rc = radix_sort_pairs(rs, nc, slot_key_bits(g->nslots()), true, &buf, st);
+  uint32_t* status = nullptr;
+  rc = radix_sort_pairs(rs, nc, slot_key_bits(g->nslots()), true, &buf, st, &status);
   if (rc) return rc;
   NaPointSrc src{xs, ys, zs, grad_out, g->C};
   const int grid = int(std::min<int64_t>(ceil_div(nc, 256), int64_t(num_sms()) * 16));
   k_segment_reduce<NaPointSrc><<<grid, 256, 0, st>>>(
       rs.keys[buf], rs.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
-      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched);
+      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched, status);
   PVDB_CHECK_LAUNCH("k_segment_reduce(noalloc)");
   g->tlist_valid = false;  // new touched leaves
-  return PVDB_OK;
+  // the status word is read into host stack memory (no allocation); the call
+  // waits for its stream, as pvdb_grid_sample_backward does
+  return read_wait_status(status, st,
+                          "a radix-sort look-back wait of the no-alloc grid backward timed out");
 }

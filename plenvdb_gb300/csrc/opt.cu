@@ -4,6 +4,7 @@
 #include <cmath>
 
 #include "pvdb_internal.cuh"
+#include "tc.cuh"
 
 struct pvdb_opt_s {
   pvdb_grid_s* params = nullptr;  // borrowed (the caller keeps it alive, plenvdb.h:695)
@@ -75,11 +76,12 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
 // The same update for 12-channel grids (k0), one thread per voxel with the
 // channels in float4 loads; the four Vec3 groups keep their own skip rule.
 // Per-channel arithmetic is identical to k_vdb_adam.
+// half: the grid's BF16 shadow, written with every updated voxel (NULL: none).
 __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restrict__ v,
                                const float* __restrict__ perlr, float stepsz,
                                const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
                                int mode, int zero_after, const int32_t* __restrict__ list,
-                               const uint32_t* __restrict__ count) {
+                               const uint32_t* __restrict__ count, __nv_bfloat16* half) {
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
@@ -132,6 +134,13 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
       d4[b] = make_float4(dd[4 * b], dd[4 * b + 1], dd[4 * b + 2], dd[4 * b + 3]);
       if (zero_after) g4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    if (half) {  // 24 bytes per voxel: three 8-byte stores
+      uint2* h2 = reinterpret_cast<uint2*>(half + slot * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        h2[b] = make_uint2(tc::pack_bf16(dd[4 * b], dd[4 * b + 1]),
+                           tc::pack_bf16(dd[4 * b + 2], dd[4 * b + 3]));
+    }
   }
 }
 
@@ -153,14 +162,15 @@ __global__ void k_adam_dense(float* __restrict__ p, const float* __restrict__ g,
   const float gi = g[i];
   if (MODE == 1 && gi == 0.f) return;
   if (stepsz_dev) stepsz = *stepsz_dev;
-  const float mn = b1 * m[i] + (1 - b1) * gi;
-  const float vn = b2 * v[i] + (1 - b2) * gi * gi;
+  // the reference kernel's float arithmetic as nvcc contracts it
+  // (adam_upd_kernel.cu:19-21): the decayed moment fused onto the rounded
+  // gradient term, then a correctly rounded sqrt and divide
+  const float mn = __fmaf_rn(b1, m[i], __fmul_rn(1.f - b1, gi));
+  const float vn = __fmaf_rn(b2, v[i], __fmul_rn(__fmul_rn(1.f - b2, gi), gi));
   m[i] = mn;
   v[i] = vn;
-  if (MODE == 2)
-    p[i] -= stepsz * perlr[i] * mn / (sqrtf(vn) + eps);
-  else
-    p[i] -= stepsz * mn / (sqrtf(vn) + eps);
+  const float num = MODE == 2 ? __fmul_rn(__fmul_rn(stepsz, perlr[i]), mn) : __fmul_rn(stepsz, mn);
+  p[i] = __fsub_rn(p[i], __fdiv_rn(num, __fadd_rn(__fsqrt_rn(vn), eps)));
 }
 
 int adam_dense_launch(float* param, const float* grad, float* m, float* v, const float* perlr,
@@ -209,13 +219,14 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
       k_vdb_adam_c12<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half);
     else
       k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
           o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
     PVDB_CHECK_LAUNCH("k_vdb_adam");
+    if (g->C != 12) g->half_valid = false;  // only the 12-channel update writes the shadow
   }
   if (zero_after && g->nleaf) {
     k_clear_u8<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf);

@@ -131,6 +131,12 @@ struct pvdb_grid_s {
   uint32_t* d_bmax = nullptr;
   int bdim[3] = {0, 0, 0};
   bool bmax_valid = false;
+  // BF16 shadow of the values, [nleaf*512*C] (12-channel feature grids read
+  // by the BF16 train step): rebuilt from the FP32 master values when invalid,
+  // kept current by the voxel Adam (which writes both); any other write of
+  // the data invalidates it, as it does the brick bound.
+  __nv_bfloat16* d_half = nullptr;
+  bool half_valid = false;
   std::vector<int32_t> h_table;
   std::vector<int32_t> h_origin;
   std::vector<uint64_t> h_mask;
@@ -308,10 +314,21 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
 // Stable LSD radix sort of (key,val) pairs, low `key_bits` bits of the keys,
 // input in rs.keys[0] (and rs.vals[0] unless iota_vals, in which case the
 // payload is the input index). Result ends in rs.keys[*out_buf], rs.vals[*out_buf].
+// Both sorts clear a status word in rs.hist and point *status at it (when
+// given): nonzero after the sort means a bounded look-back wait gave up, the
+// order is wrong, and the kernels that take the status skip their work.
 int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,
-                     cudaStream_t st);
+                     cudaStream_t st, uint32_t** status = nullptr);
 int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
-                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t* err = nullptr);
+                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t** status = nullptr);
+// Test hooks of the bounded device waits (pvdb_debug_wait_limit): the spin
+// limit of the look-back waits (0 = the built-in limit) and whether the first
+// publisher of a look-back chain withholds its count.
+uint32_t debug_spin_limit(uint32_t builtin);
+int debug_hold_first();
+// Reads a device status word back (the stream is synchronised) and maps a
+// nonzero value to PVDB_ERR_TIMEOUT with the given message.
+int read_wait_status(const uint32_t* status, cudaStream_t st, const char* what);
 // Scratch words (rs.hist) the sort needs for n_max keys of key_bits bits.
 int radix_sort_words(int64_t n_max, int key_bits);
 
@@ -341,6 +358,14 @@ uint64_t launch_counter();
 
 // Allocates (once) and rebuilds the brick bound of a scalar grid if invalid.
 int bmax_ensure(pvdb_grid_s* g, cudaStream_t st);
+// Allocates (once) and rebuilds the BF16 shadow of a grid's values if invalid.
+int half_ensure(pvdb_grid_s* g, cudaStream_t st);
+// Marks the grid's derived data (brick bound, BF16 shadow) stale after a
+// write of its values that the library does not track.
+inline void data_written(pvdb_grid_s* g) {
+  g->bmax_valid = false;
+  g->half_valid = false;
+}
 
 // Compacts the touched flags of g into g->d_tlist / d_tcount unless the list
 // is still valid (device work on st, no host synchronisation).

@@ -15,9 +15,18 @@ struct RaySetup {
   int64_t n_steps;
 };
 
-// |d| as sqrt(fma(dz,dz,fma(dy,dy,dx*dx))) (infer_n_samples_cuda_kernel :47-50).
+// |d| as sqrt(fma(dz,dz,fma(dx,dx,dy*dy))) (infer_n_samples_cuda_kernel :47-50):
+// nvcc contracts `dx*dx + dy*dy + dz*dz` by fusing the left product of the
+// first sum and the right product of the second, which the golden vectors of
+// the reference's own kernel show bit for bit.
 __device__ __forceinline__ float ray_norm(float dx, float dy, float dz) {
-  return sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))));
+  return sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy))));
+}
+
+// torch's CPU vector norm of a float[3] (rays_d.norm(dim=-1) in the Python
+// steps around the path, dvgo.py:524, :236): sqrt(fma(z,z,fma(y,y,x*x))).
+__device__ __forceinline__ float torch_norm3(float x, float y, float z) {
+  return sqrtf(__fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x))));
 }
 
 // infer_t_minmax_cuda_kernel (:12-35): slab test, clamped to [near, far].

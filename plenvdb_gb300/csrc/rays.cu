@@ -54,7 +54,7 @@ __global__ void k_get_rays(GetRaysArgs a, float* rays_o, float* rays_d, float* v
     d[k] = __fadd_rn(__fadd_rn(__fmul_rn(dir[0], a.R[3 * k]), __fmul_rn(dir[1], a.R[3 * k + 1])),
                      __fmul_rn(dir[2], a.R[3 * k + 2]));
   // rays_d.norm(dim=-1): torch's CPU vector norm is sqrt(fma(z,z,fma(y,y,x*x)))
-  const float nrm = ray_norm(d[0], d[1], d[2]);
+  const float nrm = torch_norm3(d[0], d[1], d[2]);
 #pragma unroll
   for (int k = 0; k < 3; ++k) viewdirs[3 * p + k] = __fdiv_rn(d[k], nrm);
   float o[3] = {a.t[0], a.t[1], a.t[2]};

@@ -7,6 +7,8 @@
 // synchronises with the host.
 #include <algorithm>
 
+#include <atomic>
+
 #include "reduce.cuh"
 
 namespace pvdb {
@@ -255,7 +257,10 @@ __global__ void k_os_init(int64_t n_max, const uint32_t* n_dev, int npass, int64
   const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (t < int64_t(npass) * kRsBins) scratch[L.ghist + t] = 0u;
   if (t < npass) scratch[L.counters + t] = 0u;
-  if (t == 0) scratch[L.n] = uint32_t(n);
+  if (t == 0) {
+    scratch[L.n] = uint32_t(n);
+    scratch[L.err] = 0u;
+  }
 }
 
 __global__ void __launch_bounds__(kRsThreads)
@@ -278,7 +283,10 @@ __global__ void __launch_bounds__(kRsThreads)
 
 __global__ void __launch_bounds__(kRsThreads)
     k_os_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, int pass,
-                 uint32_t* scratch, OsLayout L, uint32_t* kout, uint32_t* vout, uint32_t* err) {
+                 uint32_t* scratch, OsLayout L, uint32_t* kout, uint32_t* vout, uint32_t* err,
+                 uint32_t spin_max, int hold_first) {
+  // an earlier pass gave up: its order is wrong, so this one does nothing
+  if (*(volatile uint32_t*)err) return;
   __shared__ uint32_t wh[kRsWarps][kRsBins];
   __shared__ uint32_t gbase[kRsBins];
   __shared__ uint32_t tile_s;
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(kRsThreads)
       for (int q = 0; q < kRsWarps; ++q) cnt += wh[q][d];
       volatile uint32_t* my = status + t * kRsBins + d;
       if (t == 0) {
-        *my = kOsPrefix | cnt;
+        if (!hold_first) *my = kOsPrefix | cnt;  // (the test hook withholds it)
       } else {
         *my = kOsAgg | cnt;
       }
@@ -331,7 +339,7 @@ __global__ void __launch_bounds__(kRsThreads)
       for (int64_t tt = t - 1; tt >= 0; --tt) {
         uint32_t v = status[tt * kRsBins + d];
         for (uint32_t it = 0; v == 0u; ++it) {
-          if (it >= kOsSpinMax) {
+          if (it >= spin_max) {
             atomicOr(err, 4u);
             v = kOsPrefix;  // give up: leave the positions wrong but finish
             break;
@@ -380,8 +388,9 @@ int slot_key_bits(int64_t nslots) {
 }
 
 int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
-                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t* err) {
+                         bool iota_vals, int* out_buf, cudaStream_t st, uint32_t** status) {
   *out_buf = 0;
+  if (status) *status = nullptr;
   if (n_max <= 0) return PVDB_OK;
   const int npass = (key_bits + 7) / 8;
   if (npass < 1 || npass > 4) return set_error(PVDB_ERR_ARG, "radix sort takes 1..32 key bits");
@@ -389,7 +398,10 @@ int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev
   int rc = dev_reserve((void**)&rs.hist, &rs.hist_cap, size_t(L.words) * 4);
   if (rc) return rc;
   uint32_t* sc = rs.hist;
-  uint32_t* errp = err ? err : sc + L.err;
+  uint32_t* errp = sc + L.err;
+  if (status) *status = errp;
+  const uint32_t spin = debug_spin_limit(kOsSpinMax);
+  const int hold = debug_hold_first();
   const int g_init = int(std::min<int64_t>(
       std::max<int64_t>(ceil_div(int64_t(npass) * L.ntiles_max * kRsBins, 256), 1),
       int64_t(num_sms()) * 8));
@@ -403,7 +415,8 @@ int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev
   for (int p = 0; p < npass; ++p) {
     k_os_scatter<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
                                               (p == 0 && iota_vals) ? nullptr : rs.vals[cur], p,
-                                              sc, L, rs.keys[cur ^ 1], rs.vals[cur ^ 1], errp);
+                                              sc, L, rs.keys[cur ^ 1], rs.vals[cur ^ 1], errp,
+                                              spin, hold);
     PVDB_CHECK_LAUNCH("k_os_scatter");
     cur ^= 1;
   }
@@ -416,8 +429,8 @@ int radix_sort_words(int64_t n_max, int key_bits) {
 }
 
 int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals, int* out_buf,
-                     cudaStream_t st) {
-  return radix_sort_pairs_dev(rs, n, nullptr, key_bits, iota_vals, out_buf, st);
+                     cudaStream_t st, uint32_t** status) {
+  return radix_sort_pairs_dev(rs, n, nullptr, key_bits, iota_vals, out_buf, st, status);
 }
 
 int scratch_reserve(ReduceScratch& rs, int64_t n) {
@@ -467,6 +480,26 @@ struct PointSrc {
   __device__ __forceinline__ float gc(int64_t s, int ch) const { return g[s * C + ch]; }
 };
 
+namespace {
+std::atomic<uint32_t> g_dbg_spin{0};
+std::atomic<int> g_dbg_hold{0};
+}  // namespace
+
+uint32_t debug_spin_limit(uint32_t builtin) {
+  const uint32_t v = g_dbg_spin.load();
+  return v ? v : builtin;
+}
+
+int debug_hold_first() { return g_dbg_hold.load(); }
+
+int read_wait_status(const uint32_t* status, cudaStream_t st, const char* what) {
+  uint32_t h = 0;
+  if (status) PVDB_CHECK_CUDA(cudaMemcpyAsync(&h, status, 4, cudaMemcpyDeviceToHost, st));
+  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (h) return set_error(PVDB_ERR_TIMEOUT, what);
+  return PVDB_OK;
+}
+
 __global__ void k_point_keys(GridView gv, const float* __restrict__ xs, const float* __restrict__ ys,
                              const float* __restrict__ zs, int64_t n, uint32_t* keys) {
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -477,6 +510,13 @@ __global__ void k_point_keys(GridView gv, const float* __restrict__ xs, const fl
 }  // namespace pvdb
 
 using namespace pvdb;
+
+extern "C" int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first) {
+  clear_error();
+  g_dbg_spin.store(spins);
+  g_dbg_hold.store(hold_first ? 1 : 0);
+  return PVDB_OK;
+}
 
 extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const float* ys,
                                          const float* zs, const float* grad_out, int64_t n,
@@ -505,15 +545,17 @@ extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const flo
   k_point_keys<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), dx, dy, dz, n, g->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_point_keys");
   int buf = 0;
-  rc = radix_sort_pairs(g->red, nc, slot_key_bits(g->nslots()), true, &buf, st);
+  uint32_t* status = nullptr;
+  rc = radix_sort_pairs(g->red, nc, slot_key_bits(g->nslots()), true, &buf, st, &status);
   if (rc) return rc;
   PointSrc src{dx, dy, dz, dg, g->C};
   const int grid = int(std::min<int64_t>(ceil_div(nc, 256), int64_t(num_sms()) * 16));
   k_segment_reduce<PointSrc><<<grid, 256, 0, st>>>(
       g->red.keys[buf], g->red.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
-      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched);
+      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched, status);
   PVDB_CHECK_LAUNCH("k_segment_reduce");
   g->tlist_valid = false;
-  if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
-  return PVDB_OK;
+  // the call waits for its stream (as the reference's backward does) so that a
+  // sort wait that gave up is reported, with the gradient left unchanged
+  return read_wait_status(status, st, "a radix-sort look-back wait of the grid backward timed out");
 }

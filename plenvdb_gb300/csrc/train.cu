@@ -30,7 +30,7 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
                        const float* rd, int R, const pvdb_march_params* prm, const uint8_t* mask,
                        const int32_t* mshape, cudaStream_t st, bool skip_k0);
 int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t* xt,
-               cudaStream_t st);
+               cudaStream_t st, const __nv_bfloat16* half);
 const float* mlp_pe_buffer(pvdb_march_s* m, int* stride);
 int mlp_reserve_x(pvdb_march_s* m);
 int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_last,
@@ -250,6 +250,10 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   // join: the tiles hold the PE too)
   const bool fused_x = cfg->precision == 1;
   if (fused_x && (rc = mlp_reserve_x(m))) return rc;
+  // BF16: 12-channel features are gathered from the grid's BF16 shadow (the
+  // voxel Adam keeps it current; a replayed graph requires it valid)
+  const bool use_half = fused_x && kg->C == 12;
+  if (use_half && (rc = half_ensure(kg, st))) return rc;
   rc = march_forward_impl(m, dg, kg, t.ro, t.rd, n_rays, &cfg->march, nullptr, nullptr, st,
                           fused_x);
   if (rc) return rc;
@@ -257,7 +261,8 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   if (fused_x) {
     int pe_stride = 0;
     const float* pe = mlp_pe_buffer(m, &pe_stride);
-    rc = march_k0_x(m, pe, pe_stride, a.dpe, static_cast<uint8_t*>(m->mlp_xt), st);
+    rc = march_k0_x(m, pe, pe_stride, a.dpe, static_cast<uint8_t*>(m->mlp_xt), st,
+                    use_half ? kg->d_half : nullptr);
     if (rc) return rc;
   }
   rc = mlp_forward_impl(m, a, m->w.r_k0, t.vd, m->t_rgb, cfg->precision, st, true, fused_x);
@@ -351,6 +356,8 @@ static void grid_key(std::vector<uint8_t>& k, const pvdb_grid_s* g) {
   key_put(k, g->nleaf);
   key_put(k, g->d_bmax);
   key_put(k, g->bmax_valid);
+  key_put(k, g->d_half);
+  key_put(k, g->half_valid);
 }
 
 // Everything a captured step has baked in: sizes, configuration, and the
@@ -457,8 +464,10 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   if (rc) return rc;
   // a graph replays the step whose gradients start at zero on tracked leaves;
   // right after the grids were written from outside, step eagerly once
-  // (and with the density grid's brick bound current: a replay does not rebuild it)
-  bool graph_ok = cfg->use_graph && !dg->all_touched && !kg->all_touched && dg->bmax_valid;
+  // (and with the density grid's brick bound and, in BF16, the k0 grid's BF16
+  // shadow current: a replay rebuilds neither)
+  bool graph_ok = cfg->use_graph && !dg->all_touched && !kg->all_touched && dg->bmax_valid &&
+                  (cfg->precision == 0 || kg->C != 12 || kg->half_valid);
   TrainArgs t{m, density_opt, k0_opt, net, rays_o, rays_d, viewdirs, target, n_rays, cfg,
               loss_out, {0.f, 0.f, 0.f}, nullptr, !graph_ok};
   if (graph_ok) {

@@ -15,30 +15,36 @@ from . import _lib as L
 from .plenvdb import ColorOpt, DensityOpt
 
 
+def _check_hparams(lr, betas, eps):
+    """The value checks both optimisers make on construction (masked_adam.py:20-27,
+    :103-110): non-negative lr and eps, betas in [0, 1). ValueError names the
+    offending value."""
+    bad = [(not 0.0 <= lr, f"Invalid learning rate: {lr}"),
+           (not 0.0 <= eps, f"Invalid epsilon value: {eps}")]
+    bad += [(not 0.0 <= b < 1.0, f"Invalid beta parameter at index {i}: {b}")
+            for i, b in enumerate(betas[:2])]
+    for failed, msg in bad:
+        if failed:
+            raise ValueError(msg)
+
+
 class VDBAdam:
+    """Per-voxel Adam over the two VDB grids (density and k0); `params` holds
+    one group per grid: {"params": VDBGrid-like (channels, grid), "lr": float,
+    "skip_zero_grad": bool}."""
+
     def __init__(self, params, lr=1e-3, betas=(0.9, 0.99), eps=1e-8):
-        if not 0.0 <= lr:
-            raise ValueError(f"Invalid learning rate: {lr}")
-        if not 0.0 <= eps:
-            raise ValueError(f"Invalid epsilon value: {eps}")
-        if not 0.0 <= betas[0] < 1.0:
-            raise ValueError(f"Invalid beta parameter at index 0: {betas[0]}")
-        if not 0.0 <= betas[1] < 1.0:
-            raise ValueError(f"Invalid beta parameter at index 1: {betas[1]}")
+        _check_hparams(lr, betas, eps)
         assert len(params) == 2
         self.has_per_lr = False
-        self.skip_density, self.skip_color = False, False
-        for group in params:
-            param = group["params"]
-            glr = group["lr"]
-            if param.channels == 1:
-                self.densityparam = param
-                self.densityOpt = DensityOpt(param.grid, glr, eps, betas[0], betas[1])
-                self.skip_density = group["skip_zero_grad"]
-            else:
-                self.colorparam = param
-                self.colorOpt = ColorOpt(param.grid, glr, eps, betas[0], betas[1])
-                self.skip_color = group["skip_zero_grad"]
+        b0, b1 = betas[0], betas[1]
+        by_kind = {("density" if g["params"].channels == 1 else "color"): g for g in params}
+        dgrp, cgrp = by_kind["density"], by_kind["color"]
+        self.densityparam, self.colorparam = dgrp["params"], cgrp["params"]
+        self.densityOpt = DensityOpt(self.densityparam.grid, dgrp["lr"], eps, b0, b1)
+        self.colorOpt = ColorOpt(self.colorparam.grid, cgrp["lr"], eps, b0, b1)
+        self.skip_density = dgrp["skip_zero_grad"]
+        self.skip_color = cgrp["skip_zero_grad"]
 
     def set_pervoxel_lr(self, count):
         self.has_per_lr = True
@@ -86,18 +92,13 @@ class VDBAdam:
 
 
 class MaskedAdam(torch.optim.Optimizer):
+    """Dense Adam over torch parameters (the rgbnet), with the reference's
+    skip-zero-gradient and per-voxel learning-rate modes."""
+
     def __init__(self, params, lr=1e-3, betas=(0.9, 0.99), eps=1e-8):
-        if not 0.0 <= lr:
-            raise ValueError(f"Invalid learning rate: {lr}")
-        if not 0.0 <= eps:
-            raise ValueError(f"Invalid epsilon value: {eps}")
-        if not 0.0 <= betas[0] < 1.0:
-            raise ValueError(f"Invalid beta parameter at index 0: {betas[0]}")
-        if not 0.0 <= betas[1] < 1.0:
-            raise ValueError(f"Invalid beta parameter at index 1: {betas[1]}")
-        defaults = dict(lr=lr, betas=betas, eps=eps)
+        _check_hparams(lr, betas, eps)
         self.per_lr = None
-        super().__init__(params, defaults)
+        super().__init__(params, {"lr": lr, "betas": betas, "eps": eps})
 
     def set_pervoxel_lr(self, count):
         assert self.param_groups[0]["params"][0].shape == count.shape

@@ -95,6 +95,8 @@ class FineStageTrainer:
         self.tc.rgbnet_beta1, self.tc.rgbnet_beta2 = cfg.betas
         self.tc.rgbnet_eps = cfg.eps
         self.tc.precision = cfg.precision
+        # bytes per k0 feature the BF16 step gathers (its 12-channel BF16 shadow)
+        self.k0_feature_bytes = 2 if (cfg.precision == 1 and self.c0 == 12) else 4
         self.tc.use_graph = int(cfg.use_graph)
         self.loss = torch.zeros(1, device="cuda")
         # gradients start clean

@@ -42,7 +42,8 @@ sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
 
-REF = "/root/reference/plenvdb"
+# the reference tree: $PVDB_REFERENCE_ROOT (default /root/reference)
+REF = os.path.join(os.environ.get("PVDB_REFERENCE_ROOT", "/root/reference"), "plenvdb")
 OUT = os.path.join(HERE, "lifecycle_golden.npz")
 
 

@@ -48,8 +48,38 @@ def test_noalloc_backward_matches_the_allocating_entry_point(channels):
         torch.cuda.synchronize()
         ga = a.get_dense_grid(which=L.WHICH_GRAD)
         gb = b.get_dense_grid(which=L.WHICH_GRAD)
-        np.testing.assert_allclose(gb, ga, rtol=1e-5, atol=1e-6)
+        # the same stable sort and per-slot sums in the same order: bit for bit
+        np.testing.assert_array_equal(gb, ga)
         assert np.abs(ga).sum() > 0
+
+
+def test_noalloc_backward_at_its_size_limit_with_four_sort_passes():
+    """n = 32768 points (the limit) on a dense 256^3 grid: 2^24 voxel slots
+    need 25-bit keys, so the sort runs all four digit passes and its histogram
+    words reach the fixed array's sizing."""
+    import torch
+
+    from plenvdb_gb300 import DensityVDB
+    from plenvdb_gb300 import _lib as L
+    rng = np.random.default_rng(4)
+    reso = [256, 256, 256]
+    a, b = DensityVDB(reso, 1), DensityVDB(reso, 1)
+    assert a.info()[2] == 32 ** 3
+    n = 32768
+    st = L.stream_of()
+    for call in range(2):
+        xyz = torch.from_numpy(rng.uniform(-0.5, 255.5, (n, 3)).astype(np.float32)).cuda()
+        xs, ys, zs = (xyz[:, q].contiguous() for q in range(3))
+        g = torch.from_numpy(rng.normal(0, 1, n).astype(np.float32)).cuda()
+        L.call("pvdb_grid_sample_backward", a.handle, L.ptr(xs), L.ptr(ys), L.ptr(zs), L.ptr(g),
+               n, L.MEM_DEVICE, st)
+        L.call("pvdb_grid_sample_backward_noalloc", b.handle, L.ptr(xs), L.ptr(ys), L.ptr(zs),
+               L.ptr(g), n, st)
+        torch.cuda.synchronize()
+        ga = a.get_dense_grid(which=L.WHICH_GRAD)
+        gb = b.get_dense_grid(which=L.WHICH_GRAD)
+        np.testing.assert_array_equal(gb, ga)
+        assert np.count_nonzero(ga) > 100000
 
 
 def test_noalloc_backward_rejects_sizes_beyond_its_scratch():

@@ -557,7 +557,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     uint8_t* h0 = sm + s * kSlot + kSlH0;
     uint8_t* h1 = sm + s * kSlot + kSlH1;
     uint8_t* dl = sm + s * kSlot + kSlDl;
-    const bool vec_k0 = (a.c0 & 3) == 0;
+    // 16-byte row stores only when every row starts on a 16-byte boundary
+    const bool vec_k0 = (a.c0 & 3) == 0 && (reinterpret_cast<uintptr_t>(grad_k0) & 15u) == 0;
     uint32_t mph = 0;
     bool ok = true;
     for (int j = s; ok && j < nj; j += 2) {
@@ -689,7 +690,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     const int n = 32 * q4 + lane;
     const uint32_t tl = tmem + (uint32_t(32 * q4) << 16);
     float v[16];
-    float4* w1row = reinterpret_cast<float4*>(pw1 + n * kW);  // 512 B per row, aligned
+    // (a CTA's partials start at blockIdx.x * P floats and P is odd: scalar stores)
+    float* w1row = pw1 + n * kW;
     if (half == 0) {
       tc::tmem_ld16(tl + kTW2, v);
 #pragma unroll
@@ -708,8 +710,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       for (int j = 0; j < 4; ++j) {  // dW1 columns 0..63
         tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-          w1row[4 * j + b] = make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
+        for (int i = 0; i < 16; ++i) w1row[16 * j + i] = v[i];
       }
       tc::tmem_ld16(tl + kTW1 + 128, v);  // db1
       pb1[n] = v[0];
@@ -725,8 +726,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       for (int j = 4; j < 8; ++j) {  // dW1 columns 64..127
         tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-          w1row[4 * j + b] = make_float4(v[4 * b], v[4 * b + 1], v[4 * b + 2], v[4 * b + 3]);
+        for (int i = 0; i < 16; ++i) w1row[16 * j + i] = v[i];
       }
     }
   }

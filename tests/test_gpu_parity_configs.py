@@ -128,6 +128,15 @@ def _check_fp64(s, o32):
     o = O.March(s["og"], s["ok"], s_sel["ro"], s_sel["rd"], s["op"], fp32=False)
     assert o.M == w.shape[0]
     np.testing.assert_array_equal(rid.cpu().numpy(), o.ray_id)
+    # the FP32 transmittance product (one rounding per kept sample, as the
+    # reference's float chain) against FP64, on the longest chains of the batch
+    T = last.detach().cpu().numpy().astype(np.float64)
+    rel_T = np.abs(T - o.T_last) / np.maximum(np.abs(o.T_last), 1e-30)
+    wv = w.detach().cpu().numpy().astype(np.float64)
+    rel_w = np.abs(wv - o.weight) / np.maximum(np.abs(o.weight), 1e-30)
+    print(f"FP32 vs FP64 over {o.R} rays, up to {int(o.n_kept.max())} kept samples per ray: "
+          f"max rel err alphainv_last {rel_T.max():.3e}, weights (weight > 1e-3) "
+          f"{rel_w[o.weight > 1e-3].max():.3e}")
     np.testing.assert_allclose(last.detach().cpu().numpy(), o.T_last, rtol=1e-5, atol=0)
     np.testing.assert_allclose(w.detach().cpu().numpy(), o.weight, rtol=1e-5, atol=1e-7)
     np.testing.assert_allclose(k0.detach().cpu().numpy(), o.k0, rtol=1e-5, atol=1e-7)

@@ -455,33 +455,31 @@ int bmax_ensure(pvdb_grid_s* g, cudaStream_t st) {
   return PVDB_OK;
 }
 
-// BF16 copy of every stored value (round to nearest even), 8 values a thread.
-__global__ void k_half_build(const float* __restrict__ src, __nv_bfloat16* dst, int64_t n) {
-  const int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) * 8;
-  if (i + 8 <= n) {
-    const float4 a = __ldg(reinterpret_cast<const float4*>(src + i));
-    const float4 b = __ldg(reinterpret_cast<const float4*>(src + i + 4));
-    uint4 o;
-    o.x = tc::pack_bf16(a.x, a.y);
-    o.y = tc::pack_bf16(a.z, a.w);
-    o.z = tc::pack_bf16(b.x, b.y);
-    o.w = tc::pack_bf16(b.z, b.w);
-    *reinterpret_cast<uint4*>(dst + i) = o;
-  } else {
-    for (int64_t q = i; q < n; ++q) dst[q] = __float2bfloat16_rn(src[q]);
-  }
+// BF16 copy of a 12-channel grid's values (round to nearest even), one voxel a
+// thread: 32 bytes per voxel, channels 0..11 then four zeros, so that a voxel
+// is one aligned 32-byte sector and two 16-byte loads.
+__global__ void k_half_build(const float* __restrict__ src, __nv_bfloat16* dst, int64_t nvox) {
+  const int64_t v = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (v >= nvox) return;
+  const float4* s4 = reinterpret_cast<const float4*>(src + v * 12);
+  const float4 a = __ldg(s4), b = __ldg(s4 + 1), c = __ldg(s4 + 2);
+  uint4* d4 = reinterpret_cast<uint4*>(dst + v * kHalfStride);
+  d4[0] = make_uint4(tc::pack_bf16(a.x, a.y), tc::pack_bf16(a.z, a.w), tc::pack_bf16(b.x, b.y),
+                     tc::pack_bf16(b.z, b.w));
+  d4[1] = make_uint4(tc::pack_bf16(c.x, c.y), tc::pack_bf16(c.z, c.w), 0u, 0u);
 }
 
 int half_ensure(pvdb_grid_s* g, cudaStream_t st) {
-  const int64_t n = g->nslots() * g->C;
+  if (g->C != 12) return set_error(PVDB_ERR_STATE, "the BF16 feature shadow is kept for 12 channels");
+  const int64_t nvox = g->nslots();
   if (!g->d_half) {
-    int rc = dev_alloc((void**)&g->d_half, size_t(std::max<int64_t>(n, 8)) * 2);
+    int rc = dev_alloc((void**)&g->d_half, size_t(std::max<int64_t>(nvox, 1)) * kHalfStride * 2);
     if (rc) return rc;
     g->half_valid = false;
   }
   if (g->half_valid) return PVDB_OK;
-  if (n) {
-    k_half_build<<<ceil_div((n + 7) / 8, 256), 256, 0, st>>>(g->d_data, g->d_half, n);
+  if (nvox) {
+    k_half_build<<<ceil_div(nvox, 256), 256, 0, st>>>(g->d_data, g->d_half, nvox);
     PVDB_CHECK_LAUNCH("k_half_build");
   }
   g->half_valid = true;

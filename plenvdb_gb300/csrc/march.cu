@@ -1,6 +1,6 @@
 // Fused training march over ragged per-ray sample counts.
 //
-// Forward (k_march_setup / k_march_alpha / k_march_chain) covers, per ray:
+// Forward (k_march_setup / k_march_chain) covers, per ray:
 // sample_pts_on_rays (render_utils_kernel.cu:196-242), the bbox filter and
 // MaskGrid lookup (dvgo.py:290-315), wld2idx (grid.py:77-78), DensityVDB
 // trilinear (densityvdb.cu:101-125), raw2alpha (render_utils_kernel.cu:430-443),
@@ -43,18 +43,16 @@ __device__ __forceinline__ void load_ray(const float* __restrict__ ro, const flo
   }
 }
 
-// Forward, in three passes:
+// Forward, in two passes:
 //  k_march_setup (thread per ray): slab test, sample count, start point and
 //    unit direction;
-//  k_march_alpha (thread per (ray, sample)): position, brick-bound skip,
-//    density trilinear and raw2alpha; writes alpha (0 for a sample that is not
-//    kept) into the ray's slots — independent work, so the gathers of all
-//    samples are in flight together;
-//  k_march_chain (warp per ray): the transmittance chain over the kept
-//    samples in order, the T < t_stop early stop, and the in-place compaction
-//    of the kept samples (a kept sample moves to a slot at or before its own,
-//    after the whole chunk has been read); then the ray's offsets among all
-//    kept samples and colour rows, and its colour rows' records.
+//  k_march_chain (warp per ray): 64 samples at a time, each lane computes the
+//    alphas of its samples (position, brick-bound skip, density trilinear,
+//    raw2alpha; two independent gathers in flight), then the warp walks the
+//    transmittance chain over the kept samples in order, stops at T < t_stop
+//    (no sample past the stop is evaluated) and writes the kept samples
+//    compacted into the ray's slots; then the ray's offsets among all kept
+//    samples and colour rows, and its colour rows' records.
 __global__ void __launch_bounds__(256)
     k_march_setup(const float* __restrict__ ro, const float* __restrict__ rd, int R, MarchP P,
                   MarchW W) {
@@ -75,50 +73,36 @@ __global__ void __launch_bounds__(256)
     W.ray_sd[r * 6 + 3 + a] = rs.dir[a];
   }
   W.ray_ns[r] = int32_t(ns);
-  atomicAdd(W.totals + 4, uint32_t(ns));
   W.chain_status[r] = 0ull;  // k_march_chain look-back status of this ray
 }
 
-// One block per ray, threads over the ray's samples.
-__global__ void __launch_bounds__(256)
-    k_march_alpha(GridView gd, MarchP P, MarchW W) {
-  const int r = blockIdx.x;
-  const int ns = W.ray_ns[r];
-  RaySetup rs;
+// Alpha of sample k of a ray (0 when the sample is not kept): position,
+// brick-bound skip, bbox / mask-cache filter, density trilinear, raw2alpha and
+// the fast_color_thres test.
+__device__ __forceinline__ float sample_alpha(const GridView& gd, const MarchP& P,
+                                              const RaySetup& rs, int k) {
+  float p[3];
+  ray_point(rs, P.stepdist, k, p);
+  if (gd.bmax) {
+    // brick of the (approximate) cell; its bound covers the cells next to it
+    int b[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    rs.start[a] = W.ray_sd[r * 6 + a];
-    rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+    for (int a = 0; a < 3; ++a)
+      b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
+    const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
+    if (fkey_inv(key) < P.sigma_skip) return 0.f;
   }
-  const int64_t sbase = int64_t(r) * P.cap;
-  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
-    float p[3];
-    ray_point(rs, P.stepdist, k, p);
-    float alpha = 0.f;
-    bool skip = false;
-    if (gd.bmax) {
-      // brick of the (approximate) cell; its bound covers the cells next to it
-      int b[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
-      const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
-      skip = fkey_inv(key) < P.sigma_skip;
-    }
-    if (!skip && !out_of_bbox(p, P.mn, P.mx) &&
-        (!P.mask || mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift))) {
-      float idx[3];
-      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-      const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
-      float e;
-      const float a = raw2alpha(sigma, P.shift, P.interval, e);
-      if (a > P.thr) alpha = a;
-    }
-    W.k_alpha[sbase + k] = alpha;
-  }
+  if (out_of_bbox(p, P.mn, P.mx)) return 0.f;
+  if (P.mask && !mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift)) return 0.f;
+  float idx[3];
+  world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+  const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
+  float e;
+  const float a = raw2alpha(sigma, P.shift, P.interval, e);
+  return a > P.thr ? a : 0.f;
 }
 
-constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
+constexpr int kChainBatch = 2;  // 32-sample chunks whose alphas are computed together
 
 // Ray offsets: warps take rays in order from a counter (totals[6]); a ray
 // publishes its (colour, kept) counts, then sums the earlier rays' published
@@ -132,7 +116,7 @@ constexpr uint64_t kChainValue = kChainAgg - 1;
 constexpr uint32_t kChainSpinMax = 1u << 24;
 
 __global__ void __launch_bounds__(kMarchThreads)
-    k_march_chain(int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
+    k_march_chain(GridView gd, int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
   const int lane = threadIdx.x & 31;
   uint32_t ticket = 0;
   if (lane == 0) ticket = atomicAdd(W.totals + 6, 1u);
@@ -143,17 +127,23 @@ __global__ void __launch_bounds__(kMarchThreads)
   int nk = 0, nc = 0;
   {
     const int ns = W.ray_ns[r];
+    RaySetup rs;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      rs.start[a] = W.ray_sd[r * 6 + a];
+      rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+    }
     float T = 1.f;
     bool stop = false;
+    int marched = ns;  // samples up to the ray's stop
     for (int b0 = 0; b0 < ns && !stop; b0 += 32 * kChainBatch) {
-      // the batch's alphas, loaded before any of them is used
+      // the batch's alphas: independent gathers, in flight together
       float al[kChainBatch];
 #pragma unroll
       for (int j = 0; j < kChainBatch; ++j) {
         const int k = b0 + 32 * j + lane;
-        al[j] = k < ns ? W.k_alpha[sbase + k] : 0.f;
+        al[j] = k < ns ? sample_alpha(gd, P, rs, k) : 0.f;
       }
-      __syncwarp();  // every lane has read its alphas before the compaction writes
 #pragma unroll
       for (int j = 0; j < kChainBatch; ++j) {
         if (stop) continue;
@@ -172,6 +162,7 @@ __global__ void __launch_bounds__(kMarchThreads)
           if (T < P.t_stop) {
             km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
             stop = true;
+            marched = b0 + 32 * j + l + 1;
             break;
           }
         }
@@ -193,6 +184,7 @@ __global__ void __launch_bounds__(kMarchThreads)
       W.T_last[r] = T;
       W.n_kept[r] = nk;
       W.n_color[r] = nc;
+      atomicAdd(W.totals + 4, uint32_t(marched));
     }
   }
   // publish, then look back 32 rays at a time
@@ -252,50 +244,60 @@ __device__ __forceinline__ void load_setup(const MarchW& W, int r, RaySetup& rs)
 }
 
 // Multi-channel trilinear of k0 at one point (colorvdb.cu:97-108 ordering).
-__device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[3], float* out) {
+// The 12-channel case: the channels in three 16-byte loads per corner.
+__device__ __forceinline__ void k0_trilinear12(const GridView& g, const float idx[3], float* out) {
   const int i = ifloor(idx[0]), j = ifloor(idx[1]), k = ifloor(idx[2]);
   float sc[8];
   corner_scales(idx[0] - float(i), idx[1] - float(j), idx[2] - float(k), sc);
   int slots[8];
   corner_slots(g, i, j, k, slots);
-  if (g.C == 12) {
-    float acc[12];
+  float acc[12];
 #pragma unroll
-    for (int q = 0; q < 12; ++q) acc[q] = 0.f;
+  for (int q = 0; q < 12; ++q) acc[q] = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    float v[12];
+    if (slots[c] >= 0) {
+      const float4* src = reinterpret_cast<const float4*>(g.data + int64_t(slots[c]) * 12);
+      const float4 a = __ldg(src), b = __ldg(src + 1), cc = __ldg(src + 2);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+      v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+      v[8] = cc.x; v[9] = cc.y; v[10] = cc.z; v[11] = cc.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 12; ++q) v[q] = g.background;
+    }
+#pragma unroll
+    for (int q = 0; q < 12; ++q) acc[q] = __fadd_rn(acc[q], __fmul_rn(v[q], sc[c]));
+  }
+#pragma unroll
+  for (int q = 0; q < 12; ++q) out[q] = acc[q];
+}
+
+__device__ __forceinline__ void k0_trilinear(const GridView& g, const float idx[3], float* out) {
+  if (g.C == 12) {
+    k0_trilinear12(g, idx, out);
+    return;
+  }
+  const int i = ifloor(idx[0]), j = ifloor(idx[1]), k = ifloor(idx[2]);
+  float sc[8];
+  corner_scales(idx[0] - float(i), idx[1] - float(j), idx[2] - float(k), sc);
+  int slots[8];
+  corner_slots(g, i, j, k, slots);
+  for (int ch = 0; ch < g.C; ++ch) {
+    float acc = 0.f;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      float v[12];
-      if (slots[c] >= 0) {
-        const float4* src = reinterpret_cast<const float4*>(g.data + int64_t(slots[c]) * 12);
-        const float4 a = __ldg(src), b = __ldg(src + 1), cc = __ldg(src + 2);
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-        v[8] = cc.x; v[9] = cc.y; v[10] = cc.z; v[11] = cc.w;
-      } else {
-#pragma unroll
-        for (int q = 0; q < 12; ++q) v[q] = g.background;
-      }
-#pragma unroll
-      for (int q = 0; q < 12; ++q) acc[q] = __fadd_rn(acc[q], __fmul_rn(v[q], sc[c]));
+      const float v = slots[c] < 0 ? g.background : __ldg(g.data + int64_t(slots[c]) * g.C + ch);
+      acc = __fadd_rn(acc, __fmul_rn(v, sc[c]));
     }
-#pragma unroll
-    for (int q = 0; q < 12; ++q) out[q] = acc[q];
-  } else {
-    for (int ch = 0; ch < g.C; ++ch) {
-      float acc = 0.f;
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const float v = slots[c] < 0 ? g.background : __ldg(g.data + int64_t(slots[c]) * g.C + ch);
-        acc = __fadd_rn(acc, __fmul_rn(v, sc[c]));
-      }
-      out[ch] = acc;
-    }
+    out[ch] = acc;
   }
 }
 
 // The 12-channel trilinear from the grid's BF16 shadow (the BF16 train step):
-// 24 bytes per corner in three 8-byte loads, FP32 interpolation in the order of
-// k0_trilinear.
+// one 32-byte record per corner in two 16-byte loads, FP32 interpolation in
+// the order of k0_trilinear.
 __device__ __forceinline__ void k0_trilinear_half(const GridView& g,
                                                   const __nv_bfloat16* __restrict__ half,
                                                   const float idx[3], float* out) {
@@ -304,13 +306,15 @@ __device__ __forceinline__ void k0_trilinear_half(const GridView& g,
   corner_scales(idx[0] - float(i), idx[1] - float(j), idx[2] - float(k), sc);
   int slots[8];
   corner_slots(g, i, j, k, slots);
-  uint2 raw[8][3];
+  uint4 lo[8];
+  uint2 hi[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     if (slots[c] >= 0) {
-      const uint2* src = reinterpret_cast<const uint2*>(half + int64_t(slots[c]) * 12);
-#pragma unroll
-      for (int b = 0; b < 3; ++b) raw[c][b] = __ldg(src + b);
+      const uint4* src = reinterpret_cast<const uint4*>(half + int64_t(slots[c]) * kHalfStride);
+      lo[c] = __ldg(src);
+      const uint4 h = __ldg(src + 1);
+      hi[c] = make_uint2(h.x, h.y);
     }
   }
   float acc[12];
@@ -320,12 +324,11 @@ __device__ __forceinline__ void k0_trilinear_half(const GridView& g,
   for (int c = 0; c < 8; ++c) {
     float v[12];
     if (slots[c] >= 0) {
+      const uint32_t w[6] = {lo[c].x, lo[c].y, lo[c].z, lo[c].w, hi[c].x, hi[c].y};
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        v[4 * b] = __uint_as_float(raw[c][b].x << 16);
-        v[4 * b + 1] = __uint_as_float(raw[c][b].x & 0xFFFF0000u);
-        v[4 * b + 2] = __uint_as_float(raw[c][b].y << 16);
-        v[4 * b + 3] = __uint_as_float(raw[c][b].y & 0xFFFF0000u);
+      for (int b = 0; b < 6; ++b) {
+        v[2 * b] = __uint_as_float(w[b] << 16);
+        v[2 * b + 1] = __uint_as_float(w[b] & 0xFFFF0000u);
       }
     } else {
 #pragma unroll
@@ -359,12 +362,15 @@ __global__ void __launch_bounds__(256)
 // goes straight into the row of its X tile ([k0 | PE | 1 | 0], BF16), so the
 // FP32 k0 rows are never written. pe: per-ray PE (pe_stride floats per ray).
 // The padding rows of the last tile are zero.
+template <int CT>
 __global__ void __launch_bounds__(256)
     k_march_k0_x(GridView gk, MarchP P, MarchW W, const float* __restrict__ pe, int pe_stride,
                  int dpe, uint8_t* xt, const __nv_bfloat16* __restrict__ half) {
+  // CT = 12: the channel count is a compile-time constant, so the row's
+  // features stay in registers; CT = 0: any count up to 16
   const int64_t M = W.totals[1];
   const int64_t Mpad = (M + 127) / 128 * 128;
-  const int C = gk.C, din = C + dpe;
+  const int C = CT ? CT : gk.C, din = C + dpe;
   for (int64_t m = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; m < Mpad;
        m += int64_t(gridDim.x) * blockDim.x) {
     float k0v[16];
@@ -376,10 +382,14 @@ __global__ void __launch_bounds__(256)
       float p[3], idx[3];
       ray_point(rs, P.stepdist, W.r_step[m], p);
       world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-      if (half)
-        k0_trilinear_half(gk, half, idx, k0v);
-      else
+      if (CT == 12) {
+        if (half)
+          k0_trilinear_half(gk, half, idx, k0v);
+        else
+          k0_trilinear12(gk, idx, k0v);
+      } else {
         k0_trilinear(gk, idx, k0v);
+      }
     }
     uint8_t* tile = xt + (m >> 7) * int64_t(kRgbXTile);
     const int row = int(m & 127);
@@ -952,9 +962,8 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     const int nb = ceil_div(R, kMarchWarps);
     k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_setup");
-    k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_alpha");
-    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w, debug_spin_limit(kChainSpinMax),
+    k_march_chain<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w,
+                                                debug_spin_limit(kChainSpinMax),
                                                 debug_hold_first());
     PVDB_CHECK_LAUNCH("k_march_chain");
     if (m->prof) prof_mark(st, 1);
@@ -986,7 +995,12 @@ int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t
   PVDB_REQUIRE(m->k0->C <= 16 && m->k0->C + dpe + 1 <= kRgbXK,
                "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   const int grid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16));
-  k_march_k0_x<<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt, half);
+  if (m->k0->C == 12)
+    k_march_k0_x<12><<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
+                                           half);
+  else
+    k_march_k0_x<0><<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
+                                          nullptr);
   PVDB_CHECK_LAUNCH("k_march_k0_x");
   if (m->prof) prof_mark(st, 2);
   return PVDB_OK;

@@ -134,12 +134,11 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
       d4[b] = make_float4(dd[4 * b], dd[4 * b + 1], dd[4 * b + 2], dd[4 * b + 3]);
       if (zero_after) g4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    if (half) {  // 24 bytes per voxel: three 8-byte stores
-      uint2* h2 = reinterpret_cast<uint2*>(half + slot * 12);
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
-        h2[b] = make_uint2(tc::pack_bf16(dd[4 * b], dd[4 * b + 1]),
-                           tc::pack_bf16(dd[4 * b + 2], dd[4 * b + 3]));
+    if (half) {  // the voxel's 32-byte shadow record: channels 0..11, then zeros
+      uint4* h4 = reinterpret_cast<uint4*>(half + slot * kHalfStride);
+      h4[0] = make_uint4(tc::pack_bf16(dd[0], dd[1]), tc::pack_bf16(dd[2], dd[3]),
+                         tc::pack_bf16(dd[4], dd[5]), tc::pack_bf16(dd[6], dd[7]));
+      h4[1] = make_uint4(tc::pack_bf16(dd[8], dd[9]), tc::pack_bf16(dd[10], dd[11]), 0u, 0u);
     }
   }
 }

@@ -24,6 +24,8 @@
 namespace pvdb {
 
 constexpr int kLeafVox = 512;
+// BF16 values per voxel in a 12-channel grid's shadow (32 bytes: one sector)
+constexpr int kHalfStride = 16;
 
 // ------------------------------------------------------------- errors (host)
 int set_error(int code, const std::string& msg);
@@ -131,10 +133,11 @@ struct pvdb_grid_s {
   uint32_t* d_bmax = nullptr;
   int bdim[3] = {0, 0, 0};
   bool bmax_valid = false;
-  // BF16 shadow of the values, [nleaf*512*C] (12-channel feature grids read
-  // by the BF16 train step): rebuilt from the FP32 master values when invalid,
-  // kept current by the voxel Adam (which writes both); any other write of
-  // the data invalidates it, as it does the brick bound.
+  // BF16 shadow of a 12-channel grid's values, [nleaf*512][kHalfStride]
+  // (channels 0..11, then zeros; read by the BF16 train step): rebuilt from
+  // the FP32 master values when invalid, kept current by the voxel Adam
+  // (which writes both); any other write of the data invalidates it, as it
+  // does the brick bound.
   __nv_bfloat16* d_half = nullptr;
   bool half_valid = false;
   std::vector<int32_t> h_table;

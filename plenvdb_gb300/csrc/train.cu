@@ -124,8 +124,20 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   if (!last_s) return;
   __threadfence();
+  // thread t sums partials t, t + 256, ... in that order; eight L2 loads are
+  // in flight at a time (the other blocks' partials bypass L1)
   float acc = 0.f;
-  for (int i = threadIdx.x; i < R; i += blockDim.x) acc += ((volatile float*)loss_part)[i];
+  for (int i0 = threadIdx.x; i0 < R; i0 += 8 * blockDim.x) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = i0 + u * int(blockDim.x);
+      v[u] = i < R ? __ldcg(loss_part + i) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (i0 + u * int(blockDim.x) < R) acc += v[u];
+  }
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {

@@ -368,8 +368,9 @@ int pvdb_march_views(pvdb_march m, pvdb_march_views_t* v);
 /* Host copy of the totals (synchronises the stream). */
 int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pvdb_stream s);
 /* Counts of the last forward (synchronises s): kept samples, colour rows, and
- * samples evaluated (in the bbox, up to each ray's early stop). No reference
- * counterpart: the reference materialises these as tensor sizes. */
+ * samples marched (every ray's N_steps samples, as sample_pts_on_rays makes
+ * them, up to samples_cap). No reference counterpart: the reference
+ * materialises these as tensor sizes. */
 int pvdb_march_stats(pvdb_march m, int64_t* kept, int64_t* rows, int64_t* evaluated,
                      pvdb_stream s);
 

@@ -1,6 +1,6 @@
 // Fused training march over ragged per-ray sample counts.
 //
-// Forward (k_march_setup / k_march_chain) covers, per ray:
+// Forward (k_march_setup / k_march_alpha / k_march_chain) covers, per ray:
 // sample_pts_on_rays (render_utils_kernel.cu:196-242), the bbox filter and
 // MaskGrid lookup (dvgo.py:290-315), wld2idx (grid.py:77-78), DensityVDB
 // trilinear (densityvdb.cu:101-125), raw2alpha (render_utils_kernel.cu:430-443),
@@ -43,16 +43,18 @@ __device__ __forceinline__ void load_ray(const float* __restrict__ ro, const flo
   }
 }
 
-// Forward, in two passes:
+// Forward, in three passes:
 //  k_march_setup (thread per ray): slab test, sample count, start point and
 //    unit direction;
-//  k_march_chain (warp per ray): 64 samples at a time, each lane computes the
-//    alphas of its samples (position, brick-bound skip, density trilinear,
-//    raw2alpha; two independent gathers in flight), then the warp walks the
-//    transmittance chain over the kept samples in order, stops at T < t_stop
-//    (no sample past the stop is evaluated) and writes the kept samples
-//    compacted into the ray's slots; then the ray's offsets among all kept
-//    samples and colour rows, and its colour rows' records.
+//  k_march_alpha (thread per (ray, sample)): position, brick-bound skip,
+//    density trilinear and raw2alpha; writes alpha (0 for a sample that is not
+//    kept) into the ray's slots — independent work, so the gathers of all
+//    samples are in flight together;
+//  k_march_chain (warp per ray): the transmittance chain over the kept
+//    samples in order, the T < t_stop early stop, and the in-place compaction
+//    of the kept samples (a kept sample moves to a slot at or before its own,
+//    after the whole chunk has been read); then the ray's offsets among all
+//    kept samples and colour rows, and its colour rows' records.
 __global__ void __launch_bounds__(256)
     k_march_setup(const float* __restrict__ ro, const float* __restrict__ rd, int R, MarchP P,
                   MarchW W) {
@@ -73,36 +75,50 @@ __global__ void __launch_bounds__(256)
     W.ray_sd[r * 6 + 3 + a] = rs.dir[a];
   }
   W.ray_ns[r] = int32_t(ns);
+  atomicAdd(W.totals + 4, uint32_t(ns));
   W.chain_status[r] = 0ull;  // k_march_chain look-back status of this ray
 }
 
-// Alpha of sample k of a ray (0 when the sample is not kept): position,
-// brick-bound skip, bbox / mask-cache filter, density trilinear, raw2alpha and
-// the fast_color_thres test.
-__device__ __forceinline__ float sample_alpha(const GridView& gd, const MarchP& P,
-                                              const RaySetup& rs, int k) {
-  float p[3];
-  ray_point(rs, P.stepdist, k, p);
-  if (gd.bmax) {
-    // brick of the (approximate) cell; its bound covers the cells next to it
-    int b[3];
+// One block per ray, threads over the ray's samples.
+__global__ void __launch_bounds__(256)
+    k_march_alpha(GridView gd, MarchP P, MarchW W) {
+  const int r = blockIdx.x;
+  const int ns = W.ray_ns[r];
+  RaySetup rs;
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-      b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
-    const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
-    if (fkey_inv(key) < P.sigma_skip) return 0.f;
+  for (int a = 0; a < 3; ++a) {
+    rs.start[a] = W.ray_sd[r * 6 + a];
+    rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
   }
-  if (out_of_bbox(p, P.mn, P.mx)) return 0.f;
-  if (P.mask && !mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift)) return 0.f;
-  float idx[3];
-  world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-  const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
-  float e;
-  const float a = raw2alpha(sigma, P.shift, P.interval, e);
-  return a > P.thr ? a : 0.f;
+  const int64_t sbase = int64_t(r) * P.cap;
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+    float p[3];
+    ray_point(rs, P.stepdist, k, p);
+    float alpha = 0.f;
+    bool skip = false;
+    if (gd.bmax) {
+      // brick of the (approximate) cell; its bound covers the cells next to it
+      int b[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
+      const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
+      skip = fkey_inv(key) < P.sigma_skip;
+    }
+    if (!skip && !out_of_bbox(p, P.mn, P.mx) &&
+        (!P.mask || mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift))) {
+      float idx[3];
+      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+      const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
+      float e;
+      const float a = raw2alpha(sigma, P.shift, P.interval, e);
+      if (a > P.thr) alpha = a;
+    }
+    W.k_alpha[sbase + k] = alpha;
+  }
 }
 
-constexpr int kChainBatch = 2;  // 32-sample chunks whose alphas are computed together
+constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
 
 // Ray offsets: warps take rays in order from a counter (totals[6]); a ray
 // publishes its (colour, kept) counts, then sums the earlier rays' published
@@ -116,7 +132,7 @@ constexpr uint64_t kChainValue = kChainAgg - 1;
 constexpr uint32_t kChainSpinMax = 1u << 24;
 
 __global__ void __launch_bounds__(kMarchThreads)
-    k_march_chain(GridView gd, int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
+    k_march_chain(int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
   const int lane = threadIdx.x & 31;
   uint32_t ticket = 0;
   if (lane == 0) ticket = atomicAdd(W.totals + 6, 1u);
@@ -127,23 +143,17 @@ __global__ void __launch_bounds__(kMarchThreads)
   int nk = 0, nc = 0;
   {
     const int ns = W.ray_ns[r];
-    RaySetup rs;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      rs.start[a] = W.ray_sd[r * 6 + a];
-      rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
-    }
     float T = 1.f;
     bool stop = false;
-    int marched = ns;  // samples up to the ray's stop
     for (int b0 = 0; b0 < ns && !stop; b0 += 32 * kChainBatch) {
-      // the batch's alphas: independent gathers, in flight together
+      // the batch's alphas, loaded before any of them is used
       float al[kChainBatch];
 #pragma unroll
       for (int j = 0; j < kChainBatch; ++j) {
         const int k = b0 + 32 * j + lane;
-        al[j] = k < ns ? sample_alpha(gd, P, rs, k) : 0.f;
+        al[j] = k < ns ? W.k_alpha[sbase + k] : 0.f;
       }
+      __syncwarp();  // every lane has read its alphas before the compaction writes
 #pragma unroll
       for (int j = 0; j < kChainBatch; ++j) {
         if (stop) continue;
@@ -162,7 +172,6 @@ __global__ void __launch_bounds__(kMarchThreads)
           if (T < P.t_stop) {
             km &= (l == 31) ? 0xffffffffu : ((2u << l) - 1u);
             stop = true;
-            marched = b0 + 32 * j + l + 1;
             break;
           }
         }
@@ -184,7 +193,6 @@ __global__ void __launch_bounds__(kMarchThreads)
       W.T_last[r] = T;
       W.n_kept[r] = nk;
       W.n_color[r] = nc;
-      atomicAdd(W.totals + 4, uint32_t(marched));
     }
   }
   // publish, then look back 32 rays at a time
@@ -962,8 +970,9 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     const int nb = ceil_div(R, kMarchWarps);
     k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_setup");
-    k_march_chain<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w,
-                                                debug_spin_limit(kChainSpinMax),
+    k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
+    PVDB_CHECK_LAUNCH("k_march_alpha");
+    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w, debug_spin_limit(kChainSpinMax),
                                                 debug_hold_first());
     PVDB_CHECK_LAUNCH("k_march_chain");
     if (m->prof) prof_mark(st, 1);

@@ -52,7 +52,7 @@ struct MarchW {
   int32_t* b_row;
   // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
   // (1 samples_cap exceeded, 2 tensor-core wait, 4 ray-offset look-back
-  // wait), [4] samples marched (up to each ray's stop), [5] samples grouped by cell (backward),
+  // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
   // [6] k_march_chain ray counter, [7] train-step loss block counter
   uint32_t* totals;
 };

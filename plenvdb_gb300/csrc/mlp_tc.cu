@@ -297,49 +297,56 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 //   gk0  = dZ0 . W0k
 //   dW2 += H1^T . dl      dW1|db1 += dZ1^T . [H0|1]   dW0|db0 += dZ0^T . X
 // One persistent CTA per SM keeps two tiles in flight, in two slots with their
-// own shared-memory tiles and TMEM columns: while the four epilogue warps of
+// own shared-memory tiles and TMEM columns: while the eight epilogue warps of
 // one slot drain TMEM and write the next operand, the tensor cores run the
-// other slot's MMAs. One elected thread of a ninth warp issues every MMA, in a
-// fixed order (stage k of slot 0, then stage k of slot 1, tile pair after tile
-// pair), so the weight-gradient accumulators, resident in TMEM across all the
-// CTA's tiles, sum in an order fixed by the data: bitwise reproducible.
+// other slot's MMAs. One elected thread of a seventeenth warp issues every
+// MMA, in a fixed order (stage k of slot 0, then stage k of slot 1, tile pair
+// after tile pair), so the weight-gradient accumulators, resident in TMEM
+// across all the CTA's tiles, sum in an order fixed by the data: bitwise
+// reproducible.
 //   stage  MMAs (issuer)                                   epilogue (the slot's warps)
 //   S0     Z0 = X.W0f^T                -> A                E0  H0 = relu(Z0)
 //   S1     Z1 = H0.W1^T                -> A                E1  H1 = relu(Z1 + b1), dl
-//   S2     dZ1' = dl.W2 -> A;  dW2 += H1^T.dl              E2  dZ1 = dZ1'*[H1 > 0], over H1
+//   S2     dW2 += H1^T.dl                                  E2  dZ1 = (dl.W2)*[H1 > 0], over H1
 //   S3     dH0 = dZ1.W1 -> A;  dW1|db1 += dZ1^T.[H0|1]     E3  dZ0 = dH0*[H0 > 0], over dZ1
 //   S4     gk0 = dZ0.W0k -> G; dW0|db0 += dZ0^T.X          E4  gk0 -> global
-// A ones column in H0 and in X turns the bias sums into one more MMA column.
-// The backward's operands W2, W1 and W0k are the forward's K-major weight tiles
-// read through MN-major descriptors (no transposed copies). An epilogue
-// signals the issuer through its slot's mbarrier (128 arrivals) after a
-// proxy fence (its shared-memory writes feed the next MMAs) and a tcgen05
-// fence (its TMEM reads precede the next MMA into those columns); E4 instead
-// starts the bulk copy of the slot's next X tile, whose arrival releases S0.
-// At the end the CTA writes its partial weight gradients in the flat parameter
-// layout; the partials are summed over CTAs in a fixed order.
+// dl has three nonzero columns, so E2 forms dl.W2 on the CUDA cores (three
+// FMAs per element, from the BF16-rounded operands the MMA would read). A ones
+// column in H0 and in X turns the bias sums into one more MMA column. W1 and
+// W0k are the forward's K-major weight tiles read through MN-major
+// descriptors (no transposed copies). An epilogue signals the issuer through
+// its slot's mbarrier (256 arrivals) after a proxy fence (its shared-memory
+// writes feed the next MMAs) and a tcgen05 fence (its TMEM reads precede the
+// next MMA into those columns). The X tiles rotate through three buffers
+// (tile j in buffer j % 3): E4 of tile j, after S4 has read the buffer for the
+// last time, starts the bulk copy of tile j + 3's X, so a copy has two tiles'
+// time to land before S0 needs it. At the end the CTA writes its partial
+// weight gradients in the flat parameter layout; the partials are summed over
+// CTAs in a fixed order.
 constexpr int kBwdEpiWarps = 8;             // per slot: 4 lane quarters x 2 column halves
 constexpr int kBwdThreads = (2 * kBwdEpiWarps + 1) * 32;  // + the issuer warp: 544
 constexpr int kBwdIssuer = 2 * kBwdEpiWarps;  // warp index of the issuer
+constexpr int kBwdXBufs = 3;                // X tiles in flight: tile j uses buffer j % 3
 constexpr uint32_t kSlH0 = 0;               // H0 [128 r][144 k], col 128 = 1
 constexpr uint32_t kSlH1 = kSlH0 + 128 * 144 * 2;  // H1, then dZ1, then dZ0 [128 r][128 n]
-constexpr uint32_t kSlX = kSlH1 + 128 * 128 * 2;   // X [128 r][48 q]: k0 | PE | 1 | 0
-constexpr uint32_t kSlDl = kSlX + kXTile;          // dl [128 r][16 c]
-constexpr uint32_t kSlot = kSlDl + 128 * 16 * 2;   // 86016 B per slot
-constexpr uint32_t kBW0f = 2 * kSlot;              // W0f [128 n][48 q]
+constexpr uint32_t kSlDl = kSlH1 + 128 * 128 * 2;  // dl [128 r][16 c]
+constexpr uint32_t kSlot = kSlDl + 128 * 16 * 2;   // 73728 B per slot
+constexpr uint32_t kBX = 2 * kSlot;                // X x 3 [128 r][48 q]: k0 | PE | 1 | 0
+constexpr uint32_t kBW0f = kBX + kBwdXBufs * kXTile;  // W0f [128 n][48 q]
 constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;   // W1  [128 n][128 k]
-constexpr uint32_t kBW2 = kBW1 + 128 * 128 * 2;    // W2p [16 c][128 k]
-constexpr uint32_t kBB1 = kBW2 + 16 * 128 * 2;     // b1 f32[128]
-constexpr uint32_t kBBar = kBB1 + 128 * 4;         // mma[2], epi[2], x[2], drain, weights
-constexpr uint32_t kBTmem = kBBar + 64;
+constexpr uint32_t kBW2f = kBW1 + 128 * 128 * 2;   // W2 as f32 [3 c][128 n] (BF16 values)
+constexpr uint32_t kBB1 = kBW2f + 3 * 128 * 4;     // b1 f32[128]
+constexpr uint32_t kBBar = kBB1 + 128 * 4;         // mma[2], epi[2], x[3], drain, weights
+constexpr uint32_t kBTmem = kBBar + 80;
 constexpr uint32_t kBFlag = kBTmem + 4;
-constexpr uint32_t kBXIssued = kBFlag + 4;         // X copies started, per slot
-constexpr uint32_t kSmBwdBytes = kBXIssued + 8;
+constexpr uint32_t kBXIssued = kBFlag + 4;         // X copies started, per buffer
+constexpr uint32_t kSmBwdBytes = kBXIssued + 12;
+constexpr uint32_t kBwdWBytes = kOffW2;            // W0f and W1 of the blob (45056 B)
 static_assert(kSlot % 1024 == 0, "slot tiles keep their alignment");
-static_assert(kBW2 + 16 * 128 * 2 - kBW0f == kPackFwdBytes, "weight region = the forward blob");
+static_assert(kBW1 - kBW0f == kOffW1 - kOffW0 && kBwdWBytes % 16 == 0, "W0f, W1 as in the blob");
 static_assert(kSmBwdBytes <= 232448, "backward CTA exceeds 227 KB of shared memory");
 // TMEM columns: per slot A (128) and G (16); the resident weight-gradient sums
-constexpr uint32_t kTA0 = 0;     // slot s: kTA0 + 128*s  (Z0, Z1, dZ1', dH0)
+constexpr uint32_t kTA0 = 0;     // slot s: kTA0 + 128*s  (Z0, Z1, dH0)
 constexpr uint32_t kTG0 = 256;   // slot s: kTG0 + 16*s   (grad k0)
 constexpr uint32_t kTW2 = 288;   // dW2 [128 n x 16 c]
 constexpr uint32_t kTW0 = 304;   // dW0|db0 [128 n x 48 q]
@@ -411,14 +418,17 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
   const int nj = int((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kBBar);  // [2] MMA stage done
   uint64_t* ebar = mbar + 2;                                  // [2] epilogue done
-  uint64_t* xbar = mbar + 4;                                  // [2] X tile landed
-  uint64_t* dbar = mbar + 6;                                  // drain
-  uint64_t* wbar = mbar + 7;                                  // weight tiles landed
+  uint64_t* xbar = mbar + 4;                                  // [3] X buffer landed
+  uint64_t* dbar = mbar + 7;                                  // drain
+  uint64_t* wbar = mbar + 8;                                  // weight tiles landed
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kBTmem);
   uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kBFlag);
   uint32_t* xissued = reinterpret_cast<uint32_t*>(sm + kBXIssued);
   float* b1s = reinterpret_cast<float*>(sm + kBB1);
+  float* w2f = reinterpret_cast<float*>(sm + kBW2f);
   if (tid < 128) b1s[tid] = a.b1[tid];
+  // W2 at the BF16 precision of the forward's operand, for dZ1 = dl . W2
+  if (tid < 3 * 128) w2f[tid] = __bfloat162float(__float2bfloat16_rn(a.w2[tid]));
   if (tid < 256) {
     // H0 columns 128..143 of both slots: [1, 0 x 15] for every row
     const int s = tid >> 7, r = tid & 127;
@@ -433,16 +443,16 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     tc::mbar_init(mbar + 1, 1);
     tc::mbar_init(ebar, 32 * kBwdEpiWarps);
     tc::mbar_init(ebar + 1, 32 * kBwdEpiWarps);
-    tc::mbar_init(xbar, 1);
-    tc::mbar_init(xbar + 1, 1);
+    for (int b = 0; b < kBwdXBufs; ++b) tc::mbar_init(xbar + b, 1);
     tc::mbar_init(dbar, 1);
     tc::mbar_init(wbar, 1);
-    // the weight tiles (the forward's blob) in one bulk copy
-    tc::mbar_expect_tx(wbar, kPackFwdBytes);
-    tc::bulk_g2s(sm + kBW0f, blob, kPackFwdBytes, wbar);
-    for (int s = 0; s < 2; ++s) {
-      xissued[s] = s < nj ? 1u : 0u;
-      if (s < nj) x_fetch(sm + s * kSlot + kSlX, xt, blockIdx.x + int64_t(s) * gridDim.x, xbar + s);
+    // W0f and W1 of the forward's blob in one bulk copy
+    tc::mbar_expect_tx(wbar, kBwdWBytes);
+    tc::bulk_g2s(sm + kBW0f, blob, kBwdWBytes, wbar);
+    // the X tiles of the first three tiles
+    for (int b = 0; b < kBwdXBufs; ++b) {
+      xissued[b] = b < nj ? 1u : 0u;
+      if (b < nj) x_fetch(sm + kBX + b * kXTile, xt, blockIdx.x + int64_t(b) * gridDim.x, xbar + b);
     }
   }
   if (warp == kBwdIssuer) {
@@ -455,7 +465,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
   const uint32_t tmem = *tmem_slot;
   const uint32_t sb = tc::smem_addr(sm);
   float db2[3] = {0.f, 0.f, 0.f};
-  uint32_t xwaits[2] = {0u, 0u};  // X arrivals the issuer consumed, per slot
+  uint32_t xwaits[kBwdXBufs] = {0u, 0u, 0u};  // X arrivals the issuer consumed, per buffer
   bool wdone = false;             // the issuer saw the weight copy land
 
   if (warp == kBwdIssuer) {
@@ -467,19 +477,18 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       const uint32_t id_w2 = tc::idesc_bf16(128, 16, true, true);    // H1^T . dl
       const uint32_t id_w1 = tc::idesc_bf16(128, 144, true, true);   // dZ1^T . [H0|1]
       const uint32_t id_w0 = tc::idesc_bf16(128, 48, true, true);    // dZ0^T . X
-      uint32_t eph[2] = {0u, 0u}, xph[2] = {0u, 0u};
+      uint32_t eph[2] = {0u, 0u};
       bool w2_on = false, w1_on = false, w0_on = false;
       bool ok = wdone = bwait(wbar, 0, flag, err, spin_max);
       for (int pair = 0; ok && 2 * pair < nj; ++pair) {
         for (int k = 0; ok && k < 5; ++k) {
           for (int s = 0; ok && s < 2; ++s) {
-            if (2 * pair + s >= nj) continue;
+            const int j = 2 * pair + s;
+            if (j >= nj) continue;
+            const int xb = j % kBwdXBufs;
             if (k == 0) {
-              ok = bwait(xbar + s, xph[s], flag, err, spin_max);
-              if (ok) {
-                xph[s] ^= 1u;
-                xwaits[s]++;
-              }
+              ok = bwait(xbar + xb, xwaits[xb] & 1u, flag, err, spin_max);
+              if (ok) xwaits[xb]++;
             } else {
               ok = bwait(ebar + s, eph[s], flag, err, spin_max);
               eph[s] ^= 1u;
@@ -490,9 +499,10 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
             // the loops stay rolled so the single issuing thread keeps few
             // registers live
             const uint32_t sl = sb + uint32_t(s) * kSlot;
+            const uint32_t sx = sb + kBX + uint32_t(xb) * kXTile;
             const uint32_t tA = tmem + kTA0 + 128u * uint32_t(s);
             if (k == 0) {  // Z0 = X . W0f^T
-              uint64_t da = tc::make_desc(sl + kSlX, 128, 768);
+              uint64_t da = tc::make_desc(sx, 128, 768);
               uint64_t db = tc::make_desc(sb + kBW0f, 128, 768);
 #pragma unroll 1
               for (int q = 0; q < 3; ++q, da += 256 >> 4, db += 256 >> 4)
@@ -503,9 +513,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
 #pragma unroll 1
               for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 256 >> 4)
                 tc::mma_bf16(tA, da, db, id_kk, q > 0);
-            } else if (k == 2) {  // dZ1' = dl . W2;  dW2 += H1^T . dl
-              tc::mma_bf16(tA, tc::make_desc(sl + kSlDl, 128, 256),
-                           tc::make_desc(sb + kBW2, 2048, 128), id_kn, 0);
+            } else if (k == 2) {  // dW2 += H1^T . dl
               uint64_t da = tc::make_desc(sl + kSlH1, 2048, 128);
               uint64_t db = tc::make_desc(sl + kSlDl, 256, 128);
 #pragma unroll 1
@@ -532,7 +540,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
               for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 1536 >> 4)
                 tc::mma_bf16(tG, da, db, id_g, q > 0);
               da = tc::make_desc(sl + kSlH1, 2048, 128);
-              db = tc::make_desc(sl + kSlX, 768, 128);
+              db = tc::make_desc(sx, 768, 128);
 #pragma unroll 1
               for (int q = 0; q < 8; ++q, da += 4096 >> 4, db += 1536 >> 4)
                 tc::mma_bf16(tmem + kTW0, da, db, id_w0, (w0_on || q > 0) ? 1u : 0u);
@@ -563,9 +571,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     bool ok = true;
     for (int j = s; ok && j < nj; j += 2) {
       const int64_t mrow = (int64_t(blockIdx.x) + int64_t(j) * gridDim.x) * 128 + row;
-      // sigmoid inputs of this row, read before the first wait (column half 0)
+      // sigmoid inputs of this row, read before the first wait
       float yv[3] = {0.f, 0.f, 0.f}, gv[3] = {0.f, 0.f, 0.f};
-      if (half == 0 && mrow < M) {
+      if (mrow < M) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           yv[c] = __ldg(rgb + mrow * 3 + c);
@@ -593,30 +601,41 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         tc::tmem_ld32(tA + uint32_t(cb), v);
         store_relu32(h1, row, c0 + cb, 128, v, b1s);
       }
-      if (half == 0) {
+      // dl at the BF16 precision of the dW2 operand; E2 reuses the same values
+      float dlb[3];
+      {
         float d[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           d[c] = gv[c] * (1.f - yv[c]) * yv[c];
-          db2[c] += d[c];
+          dlb[c] = __bfloat162float(__float2bfloat16_rn(d[c]));
         }
-        *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 0, 16)) =
-            make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
-        *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+        if (half == 0) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) db2[c] += d[c];
+          *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 0, 16)) =
+              make_uint4(tc::pack_bf16(d[0], d[1]), tc::pack_bf16(d[2], 0.f), 0u, 0u);
+          *reinterpret_cast<uint4*>(dl + tc::kmaj(row, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+        }
       }
       epi_done(ebar + s);
-      // ---- E2: dZ1 = (dl . W2) * [H1 > 0], in place over H1
+      // ---- E2: dZ1 = (dl . W2) * [H1 > 0] on the CUDA cores (dl has three
+      // nonzero columns), in place over H1 once the dW2 MMA has read it
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
 #pragma unroll
       for (int cb = 0; cb < 64; cb += 32) {
-        float v[32];
-        tc::tmem_ld32(tA + uint32_t(cb), v);
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          uint4* p = reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128));
-          *p = mask_pack(v + 8 * c, *p);
+          const int n0 = c0 + cb + 8 * c;
+          float v[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e)
+            v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
+                             __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
+          uint4* p = reinterpret_cast<uint4*>(h1 + tc::kmaj(row, n0, 128));
+          *p = mask_pack(v, *p);
         }
       }
       epi_done(ebar + s);
@@ -637,13 +656,16 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         }
       }
       epi_done(ebar + s);
-      // ---- E4: grad k0; the slot's X buffer is free again (S4 is done)
+      // ---- E4: grad k0; the tile's X buffer is free again (S4 is done): it
+      // takes the X tile of tile j + 3
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
-      if (w8 == 0 && lane == 0 && j + 2 < nj) {
-        xissued[s] += 1u;
-        x_fetch(sm + s * kSlot + kSlX, xt, blockIdx.x + int64_t(j + 2) * gridDim.x, xbar + s);
+      if (w8 == 0 && lane == 0 && j + kBwdXBufs < nj) {
+        const int xb = j % kBwdXBufs;
+        xissued[xb] += 1u;
+        x_fetch(sm + kBX + xb * kXTile, xt, blockIdx.x + int64_t(j + kBwdXBufs) * gridDim.x,
+                xbar + xb);
       }
       if (half == 0) {
         float v[16];
@@ -677,8 +699,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       tc::mbar_wait(dbar, 0, spin_max);
     }
     if (!wdone) tc::mbar_wait(wbar, 0, spin_max);
-    for (int s = 0; s < 2; ++s)  // at most one copy per slot is outstanding
-      if (xissued[s] > xwaits[s]) tc::mbar_wait(xbar + s, xwaits[s] & 1u, spin_max);
+    for (int b = 0; b < kBwdXBufs; ++b)  // at most one copy per buffer is outstanding
+      if (xissued[b] > xwaits[b]) tc::mbar_wait(xbar + b, xwaits[b] & 1u, spin_max);
   }
   __syncthreads();
   if (failed) {
@@ -731,9 +753,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     }
   }
   if (!failed) {
-    // db2: fixed-order sum of the per-row partials of both slots (slot 0's X
+    // db2: fixed-order sum of the per-row partials of both slots (the first X
     // buffer as scratch: no copy or MMA touches it any more)
-    float* red = reinterpret_cast<float*>(sm + kSlX);
+    float* red = reinterpret_cast<float*>(sm + kBX);
     if (warp < 2 * kBwdEpiWarps && ((warp % kBwdEpiWarps) >> 2) == 0) {
       const int idx = (warp / kBwdEpiWarps) * 128 + 32 * (warp & 3) + lane;
       for (int c = 0; c < 3; ++c) red[c * 256 + idx] = db2[c];

@@ -634,19 +634,58 @@ __device__ void sort_segment(uint32_t* a, uint32_t len) {
   }
 }
 
-// Thread per placed index; cell heads sort their segment and flag the leaves
-// of the cell's corners as touched in the density grid and (touched_c !=
-// NULL) the k0 grid (k0_same: the k0 grid has the density topology, so the
-// density grid's corner slots serve both).
+// Ascending sort of up to 8 indices in registers (odd-even transposition
+// network; entries past len are padded with the largest value and stay last).
+__device__ __forceinline__ void sort8(uint32_t v[8]) {
+#pragma unroll
+  for (int round = 0; round < 8; ++round) {
+#pragma unroll
+    for (int i = round & 1; i + 1 < 8; i += 2) {
+      const uint32_t a = v[i], b = v[i + 1];
+      v[i] = min(a, b);
+      v[i + 1] = max(a, b);
+    }
+  }
+}
+
+// Thread per placed index; cell heads sort their segment (by sample index),
+// lay the segment's gradient records out in that order (rec_s, row_s: the
+// per-voxel sums then read each cell's records contiguously, without the
+// sample-index indirection), and flag the leaves of the cell's corners as
+// touched in the density grid and (touched_c != NULL) the k0 grid (k0_same:
+// the k0 grid has the density topology, so the density grid's corner slots
+// serve both).
 __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
                              const uint32_t* __restrict__ cnt, uint32_t* svals, GridView gd,
-                             GridView gc, uint8_t* touched_d, uint8_t* touched_c, int k0_same) {
+                             GridView gc, uint8_t* touched_d, uint8_t* touched_c, int k0_same,
+                             const float4* __restrict__ rec, const int32_t* __restrict__ brow,
+                             float4* rec_s, int32_t* row_s) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x) {
     const uint32_t key = skeys[i];
     if (i > 0 && skeys[i - 1] == key) continue;
-    sort_segment(svals + i, cnt[key]);
+    const uint32_t len = cnt[key];
+    if (len <= 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (uint32_t t = 0; t < 8; ++t) v[t] = t < len ? svals[i + t] : 0xFFFFFFFFu;
+      sort8(v);
+#pragma unroll
+      for (uint32_t t = 0; t < 8; ++t)
+        if (t < len) {
+          svals[i + t] = v[t];
+          rec_s[i + t] = rec[v[t]];
+          row_s[i + t] = brow[v[t]];
+        }
+    } else {
+      sort_segment(svals + i, len);
+      for (uint32_t t = 0; t < len; ++t) {
+        const uint32_t sv = svals[i + t];
+        rec_s[i + t] = rec[sv];
+        row_s[i + t] = brow[sv];
+      }
+    }
     const int off = int(key & 511u);
     const int al = __ldg(gd.table + (key >> 9));  // the cell's own leaf, if allocated
     const bool interior = al >= 0 && (off >> 6) != 7 && ((off >> 3) & 7) != 7 && (off & 7) != 7;
@@ -749,9 +788,9 @@ template <int NQ>
 __global__ void __launch_bounds__(256)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                    const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
-                   const uint32_t* __restrict__ svals, const float4* __restrict__ rec,
-                   const int32_t* __restrict__ brow, const float* __restrict__ gk0, int gk0_vec,
-                   float* grad_d, float* grad_c, int C) {
+                   const float4* __restrict__ rec_s, const int32_t* __restrict__ row_s,
+                   const float* __restrict__ gk0, int gk0_vec, float* grad_d, float* grad_c,
+                   int C) {
   constexpr int NB = NQ > 0 ? NQ : 1;
   const int64_t nv = int64_t(*count) * kLeafVox;
   const bool want_d = grad_d != nullptr, want_c = NQ && grad_c;
@@ -791,9 +830,8 @@ __global__ void __launch_bounds__(256)
       for (int b = 0; b < NB; ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
       const uint32_t h = __ldg(off + key[c]);
       for (uint32_t j = h; j < h + len[c]; ++j) {
-        const uint32_t s0 = svals[j];
-        const float4 p0 = rec[s0];
-        const int32_t r0 = want_c ? brow[s0] : -1;
+        const float4 p0 = rec_s[j];
+        const int32_t r0 = want_c ? row_s[j] : -1;
         float4 q0[NB];
         gather_row<NQ>(gk0, r0, C, gk0_vec, q0);
         gather_add<NQ>(p0, q0, r0 >= 0, want_d, c, pd, pk);
@@ -833,16 +871,18 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const bool same = NQ && k0->h_table == density->h_table;
   const int C = NQ ? k0->C : 0;
   const int vec = NQ && C % 4 == 0 && (reinterpret_cast<uintptr_t>(grad_k0) & 15u) == 0;
-  const uint32_t* svals = m->red.vals[0];
+  // the kept samples' records in grouped order (k_cell_heads)
+  const float4* rec_s = m->b_rec_s;
+  const int32_t* row_s = reinterpret_cast<const int32_t*>(m->red.vals[1]);
   k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_cnt,
-                                           m->cell_off, svals, m->w.b_rec, m->w.b_row, grad_k0,
-                                           vec, density->d_grad, same ? k0->d_grad : nullptr, C);
+                                           m->cell_off, rec_s, row_s, grad_k0, vec,
+                                           density->d_grad, same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
     k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
-                                             m->cell_off, svals, m->w.b_rec, m->w.b_row, grad_k0,
-                                             vec, nullptr, k0->d_grad, C);
+                                             m->cell_off, rec_s, row_s, grad_k0, vec, nullptr,
+                                             k0->d_grad, C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -1042,7 +1082,8 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
     m->cell_cap = size_t(ncells);
   }
   if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * 16)) ||
-      (rc = dev_reserve((void**)&m->w.b_row, &m->b_row_cap, size_t(nmax) * 4)))
+      (rc = dev_reserve((void**)&m->w.b_row, &m->b_row_cap, size_t(nmax) * 4)) ||
+      (rc = dev_reserve((void**)&m->b_rec_s, &m->b_rec_s_cap, size_t(nmax) * 16)))
     return rc;
   const int nb = ceil_div(R, kMarchWarps);
   // the kept samples' keys, with their per-cell ranks and the per-cell and
@@ -1067,9 +1108,13 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   PVDB_CHECK_LAUNCH("k_cell_place");
   const GridView gv = density->view();
   const GridView kv = k0 ? k0->view() : gv;
+  // (the ranks are dead after the placement: their buffer takes the
+  // grouped-order colour rows)
   k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals, gv, kv,
                                               density->d_touched, k0 ? k0->d_touched : nullptr,
-                                              k0 && k0->h_table == density->h_table ? 1 : 0);
+                                              k0 && k0->h_table == density->h_table ? 1 : 0,
+                                              m->w.b_rec, m->w.b_row, m->b_rec_s,
+                                              reinterpret_cast<int32_t*>(rank));
   PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;
   if (k0) k0->tlist_valid = false;
@@ -1206,7 +1251,7 @@ int pvdb_march_destroy(pvdb_march m) {
   MarchW& w = m->w;
   void* ptrs[] = {w.ray_sd, w.ray_ns, w.chain_status, w.T_last, w.n_kept, w.n_color, w.kept_off, w.color_off, w.k_alpha, w.k_w,
                   w.k_step, w.k_row, w.r_k0, w.r_w, w.r_alpha, w.r_ray, w.r_step, w.b_rec, w.b_row,
-                  w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed, m->mlp_xt,
+                  m->b_rec_s, w.totals, m->scan_partial, m->hpe, m->wpart, m->mlp_packed, m->mlp_xt,
                   m->t_rgb, m->t_grad_rgb, m->t_grad_w, m->t_grad_k0, m->t_grad_last,
                   m->t_loss_part, m->t_rgb_marched};
   for (void* p : ptrs) dev_free(p);

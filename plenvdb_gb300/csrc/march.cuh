@@ -74,6 +74,8 @@ struct pvdb_march_s {
   uint32_t* leaf_off = nullptr;
   size_t cell_cap = 0;  // cells
   size_t b_rec_cap = 0;         // bytes of w.b_rec
+  float4* b_rec_s = nullptr;    // w.b_rec in grouped (cell, sample) order
+  size_t b_rec_s_cap = 0;
   size_t b_row_cap = 0;         // bytes of w.b_row
   bool bwd_keys_ready = false;  // march_backward_keys ran since the last reduce
   bool bwd_with_k0 = false;

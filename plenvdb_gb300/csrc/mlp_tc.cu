@@ -133,22 +133,31 @@ __device__ __forceinline__ void x_fetch(uint8_t* sm_x, const uint8_t* xt, int64_
   tc::bulk_g2s(sm_x, xt + t * kXTile, kXTile, xbar);
 }
 
+// BF16 pair (lo, hi) of FP32 values, rounded to nearest even and clamped below
+// at zero: relu and rounding in one instruction (the values of relu before
+// rounding, up to the sign of a zero).
+__device__ __forceinline__ uint32_t pack_relu_bf16(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// relu(v + bias) of 8 consecutive columns as 8 BF16.
+__device__ __forceinline__ uint4 relu_pack8(const float* v, const float* bias, int col) {
+  float h[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) h[e] = bias ? v[e] + bias[col + e] : v[e];
+  return make_uint4(pack_relu_bf16(h[0], h[1]), pack_relu_bf16(h[2], h[3]),
+                    pack_relu_bf16(h[4], h[5]), pack_relu_bf16(h[6], h[7]));
+}
+
 // 32 FP32 values (+ bias, relu) -> 4 x 8 BF16 into a K-major tile (ktot columns).
 __device__ __forceinline__ void store_relu32(uint8_t* tile, int row, int col0, int ktot,
                                              const float* v, const float* bias) {
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const int o = 8 * c;
-    float h[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) h[e] = fmaxf(v[o + e] + (bias ? bias[col0 + o + e] : 0.f), 0.f);
-    uint4 pk;
-    pk.x = tc::pack_bf16(h[0], h[1]);
-    pk.y = tc::pack_bf16(h[2], h[3]);
-    pk.z = tc::pack_bf16(h[4], h[5]);
-    pk.w = tc::pack_bf16(h[6], h[7]);
-    *reinterpret_cast<uint4*>(tile + tc::kmaj(row, col0 + o, ktot)) = pk;
-  }
+  for (int c = 0; c < 4; ++c)
+    *reinterpret_cast<uint4*>(tile + tc::kmaj(row, col0 + 8 * c, ktot)) =
+        relu_pack8(v + 8 * c, bias, col0 + 8 * c);
 }
 
 __global__ void __launch_bounds__(kTcThreads, 2)
@@ -307,11 +316,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 //   stage  MMAs (issuer)                                   epilogue (the slot's warps)
 //   S0     Z0 = X.W0f^T                -> A                E0  H0 = relu(Z0)
 //   S1     Z1 = H0.W1^T                -> A                E1  H1 = relu(Z1 + b1), dl
-//   S2     dW2 += H1^T.dl                                  E2  dZ1 = (dl.W2)*[H1 > 0], over H1
+//   S2     dW2 += H1^T.dl                                  E2  dZ1 over H1
 //   S3     dH0 = dZ1.W1 -> A;  dW1|db1 += dZ1^T.[H0|1]     E3  dZ0 = dH0*[H0 > 0], over dZ1
 //   S4     gk0 = dZ0.W0k -> G; dW0|db0 += dZ0^T.X          E4  gk0 -> global
-// dl has three nonzero columns, so E2 forms dl.W2 on the CUDA cores (three
-// FMAs per element, from the BF16-rounded operands the MMA would read). A ones
+// dl has three nonzero columns, so dZ1 = (dl.W2)*[H1 > 0] is formed on the
+// CUDA cores (three FMAs per element, from the BF16-rounded operands the MMA
+// would read), in registers after E1 has released H1 and dl to S2: the
+// arithmetic overlaps the dW2 MMA, and E2 only stores dZ1 once S2 is done. A ones
 // column in H0 and in X turns the bias sums into one more MMA column. W1 and
 // W0k are the forward's K-major weight tiles read through MN-major
 // descriptors (no transposed copies). An epilogue signals the issuer through
@@ -327,6 +338,9 @@ constexpr int kBwdEpiWarps = 8;             // per slot: 4 lane quarters x 2 col
 constexpr int kBwdThreads = (2 * kBwdEpiWarps + 1) * 32;  // + the issuer warp: 544
 constexpr int kBwdIssuer = 2 * kBwdEpiWarps;  // warp index of the issuer
 constexpr int kBwdXBufs = 3;                // X tiles in flight: tile j uses buffer j % 3
+// dZ1 column groups (8 columns each) formed while the dW2 MMA runs; the other
+// two after it (holding all eight across the wait spills registers)
+constexpr int kDz1Early = 6;
 constexpr uint32_t kSlH0 = 0;               // H0 [128 r][144 k], col 128 = 1
 constexpr uint32_t kSlH1 = kSlH0 + 128 * 144 * 2;  // H1, then dZ1, then dZ0 [128 r][128 n]
 constexpr uint32_t kSlDl = kSlH1 + 128 * 128 * 2;  // dl [128 r][16 c]
@@ -354,23 +368,24 @@ constexpr uint32_t kTW1 = 352;   // dW1|db1 [128 n x 144 k]
 constexpr uint32_t kTmemBwdCols = 512;
 static_assert(kTW1 + 144 <= kTmemBwdCols, "TMEM columns");
 
-__device__ __forceinline__ bool bf16_pos(uint32_t bits16) { return (bits16 & 0x7FFFu) != 0u; }
+// 0xFFFF in each 16-bit half of a BF16 pair whose magnitude is nonzero: bit 15
+// (bit 31) of (w & 0x7FFF7FFF) + 0x7FFF7FFF is set exactly when the low (high)
+// half is nonzero, and a byte permute replicates those sign bits over their
+// halves.
+__device__ __forceinline__ uint32_t nonzero_mask_bf16x2(uint32_t w) {
+  const uint32_t t = (w & 0x7FFF7FFFu) + 0x7FFF7FFFu;
+  uint32_t m;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(m) : "r"(t), "r"(0u), "r"(0xBB99u));
+  return m;
+}
 
-// relu mask of 8 BF16 activations (a uint4) applied to 8 FP32 values.
+// relu mask of 8 BF16 activations (a uint4: a relu output is positive exactly
+// when its magnitude is nonzero) applied to 8 FP32 values, as 8 BF16.
 __device__ __forceinline__ uint4 mask_pack(const float* v, uint4 h) {
-  const uint32_t w[4] = {h.x, h.y, h.z, h.w};
-  float o[8];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    o[2 * i] = bf16_pos(w[i] & 0xFFFFu) ? v[2 * i] : 0.f;
-    o[2 * i + 1] = bf16_pos(w[i] >> 16) ? v[2 * i + 1] : 0.f;
-  }
-  uint4 pk;
-  pk.x = tc::pack_bf16(o[0], o[1]);
-  pk.y = tc::pack_bf16(o[2], o[3]);
-  pk.z = tc::pack_bf16(o[4], o[5]);
-  pk.w = tc::pack_bf16(o[6], o[7]);
-  return pk;
+  return make_uint4(tc::pack_bf16(v[0], v[1]) & nonzero_mask_bf16x2(h.x),
+                    tc::pack_bf16(v[2], v[3]) & nonzero_mask_bf16x2(h.y),
+                    tc::pack_bf16(v[4], v[5]) & nonzero_mask_bf16x2(h.z),
+                    tc::pack_bf16(v[6], v[7]) & nonzero_mask_bf16x2(h.w));
 }
 
 // Bounded wait that also gives up as soon as another role has (flag set).
@@ -595,11 +610,16 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
+      uint4 hp[8];  // this thread's 64 H1 values, then its dZ1 values, as BF16
 #pragma unroll
       for (int cb = 0; cb < 64; cb += 32) {
         float v[32];
         tc::tmem_ld32(tA + uint32_t(cb), v);
-        store_relu32(h1, row, c0 + cb, 128, v, b1s);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          hp[cb / 8 + c] = relu_pack8(v + 8 * c, b1s, c0 + cb + 8 * c);
+          *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128)) = hp[cb / 8 + c];
+        }
       }
       // dl at the BF16 precision of the dW2 operand; E2 reuses the same values
       float dlb[3];
@@ -619,25 +639,35 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         }
       }
       epi_done(ebar + s);
-      // ---- E2: dZ1 = (dl . W2) * [H1 > 0] on the CUDA cores (dl has three
-      // nonzero columns), in place over H1 once the dW2 MMA has read it
+      // dZ1 = (dl . W2) * [H1 > 0] on the CUDA cores (dl has three nonzero
+      // columns), in registers while the dW2 MMA reads H1
+#pragma unroll
+      for (int g = 0; g < kDz1Early; ++g) {
+        const int n0 = c0 + 8 * g;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
+                           __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
+        hp[g] = mask_pack(v, hp[g]);
+      }
+      // ---- E2: dZ1 over H1 once the dW2 MMA has read it
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
 #pragma unroll
-      for (int cb = 0; cb < 64; cb += 32) {
+      for (int g = kDz1Early; g < 8; ++g) {
+        const int n0 = c0 + 8 * g;
+        float v[8];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int n0 = c0 + cb + 8 * c;
-          float v[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e)
-            v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
-                             __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
-          uint4* p = reinterpret_cast<uint4*>(h1 + tc::kmaj(row, n0, 128));
-          *p = mask_pack(v, *p);
-        }
+        for (int e = 0; e < 8; ++e)
+          v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
+                           __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
+        hp[g] = mask_pack(v, hp[g]);
       }
+#pragma unroll
+      for (int g = 0; g < 8; ++g)
+        *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + 8 * g, 128)) = hp[g];
       epi_done(ebar + s);
       // ---- E3: dZ0 = dH0 * [H0 > 0], over dZ1
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;

@@ -307,6 +307,7 @@ def run_ours(args):
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
     value, ms_per_step = replica_throughput(step_ms, args.steps, ws_)
     stage_ms = stage_profile(tr, dev, nb, flush, args)
+    staging = leaf_staging_compare(tr, dev, nb, flush, args, stage_ms)
     # ---------------- the FP32 plain method on the same workload, same timing
     plain = None
     if args.precision == "bf16" and not args.no_fp32_plain:
@@ -379,6 +380,7 @@ def run_ours(args):
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(scfg, cfg, cam, ro, rd, vd, tgt, tr, args)
         out["stage_ms"] = stage_ms
+        out["leaf_staging"] = staging
         if plain:
             out["fp32_plain"] = plain
         out["density_only"] = dens_only
@@ -420,6 +422,20 @@ def stage_profile(tr, dev, nb, flush, args, n=None):
                    5: "rgbnet_bwd", 6: "march_bwd", 7: "cell_grouping", 8: "voxel_gather",
                    9: "tv", 10: "voxel_adam", 11: "rgbnet_adam"}
     return {stage_names[i]: marks[i] / max(1, ncalls.value) for i in stage_names}
+
+
+def leaf_staging_compare(tr, dev, nb, flush, args, stage_ms, n=None):
+    """The march forward stage with the density leaves staged in shared memory
+    by bulk copies (pvdb_march_set_leaf_staging) against the default pass,
+    from the same eager stage profile; staging is switched off again."""
+    tr.ws.set_leaf_staging(True)
+    try:
+        sm = stage_profile(tr, dev, nb, flush, args, n=n)
+    finally:
+        tr.ws.set_leaf_staging(False)
+    return {"march_fwd_ms_default": stage_ms["march_fwd"], "march_fwd_ms_staged": sm["march_fwd"],
+            "note": "density leaves of each ray's evaluated samples copied into shared memory "
+                    "with cp.async.bulk (24 slots of 2 KB per ray block); off by default"}
 
 
 def run_e2e(tr, ro, rd, vd, tgt, args, flush):
@@ -783,6 +799,7 @@ def run_large(args, steps=10, warmup=3):
             roof = roofline(sm, tr, scfg, R=R)
             res[tag]["stage_ms"] = sm
             res[tag]["stages"] = roof["stages"]
+            res[tag]["leaf_staging"] = leaf_staging_compare(tr, batches, nb, None, None, sm, n=5)
         del tr, dg, kg
     res["speedup_bf16"] = res["bf16"]["it_s"] / res["fp32"]["it_s"]
     res["timing"] = (f"CUDA events over {steps} steps after {warmup} warm-up steps; inputs "

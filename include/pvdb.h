@@ -58,12 +58,16 @@ int pvdb_last_error(char* buf, size_t len);
  * with PVDB_ERR_NOMEM (host-side injection; no device call is made for them). */
 int pvdb_debug_fail_next_allocs(int count);
 /* Test hook of the bounded device-side waits (no counterpart in the
- * reference): spins > 0 replaces the built-in spin limit of the look-back
- * waits (radix sort, march ray offsets; 0 restores it); hold_first != 0 makes
- * the first publisher of each look-back chain withhold its count, so that the
- * waits behind it run out and the call reports PVDB_ERR_TIMEOUT. Applies to
- * launches made after the call (a captured train-step graph keeps the values
- * it was captured with). */
+ * reference): spins > 0 replaces the built-in spin limit of the device waits
+ * (radix sort and march look-backs, tensor-core MMA waits, leaf-staging copy
+ * waits; 0 restores it); hold_first == 1 makes the first publisher of each
+ * look-back chain (and the rgbnet backward's MMA issuer) withhold its work, so
+ * that the waits behind it run out and the call reports PVDB_ERR_TIMEOUT;
+ * hold_first == 2 makes the first block of the staged density pass
+ * (pvdb_march_set_leaf_staging) issue no leaf copies, so its copy wait runs
+ * out (it then reads global memory: the results are unchanged, the workspace
+ * reports PVDB_ERR_TIMEOUT). Applies to launches made after the call (a
+ * captured train-step graph keeps the values it was captured with). */
 int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first);
 
 /* Stage profiler. Between begin and end, pvdb_train_step and
@@ -335,6 +339,14 @@ typedef struct pvdb_march_params {
 /* Workspace for up to max_rays rays of at most samples_cap samples each. */
 int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out);
 int pvdb_march_destroy(pvdb_march m);
+
+/* Leaf staging of the forward's density pass (a GB300 option, off by default;
+ * no counterpart in the reference): each ray's block copies the density leaves
+ * its evaluated samples interpolate from into shared memory with 1-D bulk
+ * copies (up to 24 leaves of 2 KB; the rest are read from global memory) and
+ * interpolates there. Results are bitwise those of the default pass. Applies
+ * to forwards (and train-step captures) made after the call. */
+int pvdb_march_set_leaf_staging(pvdb_march m, int32_t on);
 
 /* Upper bound on the per-ray sample count for a bbox and step distance. */
 int32_t pvdb_march_samples_cap(const float xyz_min[3], const float xyz_max[3], float stepdist);

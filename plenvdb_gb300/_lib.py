@@ -134,6 +134,7 @@ _SIGS = {
     "pvdb_maskcache_lookup": (C.c_int, [vp, P_i32, vp, i64, P_f32, P_f32, vp, vp]),
     "pvdb_march_create": (C.c_int, [i32, i32, C.POINTER(vp)]),
     "pvdb_march_destroy": (C.c_int, [vp]),
+    "pvdb_march_set_leaf_staging": (C.c_int, [vp, i32]),
     "pvdb_march_samples_cap": (i32, [P_f32, P_f32, f32]),
     "pvdb_march_forward": (C.c_int, [vp, vp, vp, vp, vp, i32, C.POINTER(MarchParams), vp, P_i32,
                                      vp]),

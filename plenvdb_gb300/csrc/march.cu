@@ -79,43 +79,190 @@ __global__ void __launch_bounds__(256)
   W.chain_status[r] = 0ull;  // k_march_chain look-back status of this ray
 }
 
+// Sample k of a ray: its index-space position when the sample is evaluated
+// (its brick bound does not rule it out, it lies in the bbox and, with a mask,
+// in the mask); false otherwise (alpha 0).
+__device__ __forceinline__ bool alpha_eval_index(const GridView& gd, const MarchP& P,
+                                                 const RaySetup& rs, int k, float idx[3]) {
+  float p[3];
+  ray_point(rs, P.stepdist, k, p);
+  if (gd.bmax) {
+    // brick of the (approximate) cell; its bound covers the cells next to it
+    int b[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
+    const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
+    if (fkey_inv(key) < P.sigma_skip) return false;
+  }
+  if (out_of_bbox(p, P.mn, P.mx) ||
+      (P.mask && !mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift)))
+    return false;
+  world_to_index(p, P.mn, P.ext, P.wsm1, idx);
+  return true;
+}
+
+__device__ __forceinline__ float alpha_of(const MarchP& P, float sigma) {
+  float e;
+  const float a = raw2alpha(sigma, P.shift, P.interval, e);
+  return a > P.thr ? a : 0.f;
+}
+
+__device__ __forceinline__ void load_ray_setup(const MarchW& W, int r, RaySetup& rs) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rs.start[a] = W.ray_sd[r * 6 + a];
+    rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+  }
+}
+
 // One block per ray, threads over the ray's samples.
 __global__ void __launch_bounds__(256)
     k_march_alpha(GridView gd, MarchP P, MarchW W) {
   const int r = blockIdx.x;
   const int ns = W.ray_ns[r];
   RaySetup rs;
+  load_ray_setup(W, r, rs);
+  const int64_t sbase = int64_t(r) * P.cap;
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+    float idx[3];
+    float alpha = 0.f;
+    if (alpha_eval_index(gd, P, rs, k, idx)) alpha = alpha_of(P, trilinear1(gd, idx[0], idx[1], idx[2]));
+    W.k_alpha[sbase + k] = alpha;
+  }
+}
+
+// The same pass with the density leaves staged in shared memory
+// (pvdb_march_set_leaf_staging). A block first walks its ray's samples and
+// collects, in an open-addressing table, the leaves of every corner of every
+// evaluated sample; up to kStageSlots of them are copied into shared memory
+// with one 1-D bulk copy each (cp.async.bulk, 2 KB, completion counted on one
+// mbarrier); then it walks the samples again and interpolates, reading staged
+// leaves from shared memory and the others (beyond the slots, or all of them
+// after a copy wait that gave up: error bit 8) from global memory. The values
+// and the arithmetic are those of k_march_alpha.
+constexpr int kStageSlots = 24;                 // 48 KB of density leaves per block
+constexpr int kStageHash = 128;                 // table entries (a power of two)
+constexpr uint32_t kStageSpinMax = 1u << 22;
+constexpr size_t kStageSmem = size_t(kStageSlots) * kLeafVox * 4;
+
+__device__ __forceinline__ uint32_t stage_hash(int leaf) {
+  return (uint32_t(leaf) * 2654435761u) >> 25;  // 7 bits: kStageHash entries
+}
+
+// Staging slot of a leaf, -1 when it is not staged.
+__device__ __forceinline__ int stage_find(const int32_t* hkey, const int16_t* hslot, int leaf) {
+  uint32_t h = stage_hash(leaf);
+  for (int t = 0; t < kStageHash; ++t, h = (h + 1) & (kStageHash - 1)) {
+    const int key = hkey[h];
+    if (key == leaf) return hslot[h];
+    if (key < 0) return -1;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void stage_insert(int32_t* hkey, int16_t* hslot, uint32_t* nslot,
+                                             int leaf) {
+  uint32_t h = stage_hash(leaf);
+  for (int t = 0; t < kStageHash; ++t, h = (h + 1) & (kStageHash - 1)) {
+    const int old = atomicCAS(hkey + h, -1, leaf);
+    if (old == -1) {
+      const uint32_t slot = atomicAdd(nslot, 1u);
+      hslot[h] = int16_t(slot < uint32_t(kStageSlots) ? int(slot) : -1);
+      return;
+    }
+    if (old == leaf) return;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_march_alpha_staged(GridView gd, MarchP P, MarchW W, uint32_t spin_max, int hold) {
+  extern __shared__ __align__(128) float st_vox[];  // [kStageSlots][512]
+  __shared__ int32_t hkey[kStageHash];
+  __shared__ int16_t hslot[kStageHash];
+  __shared__ uint32_t nslot;
+  __shared__ __align__(8) uint64_t bar;
+  const int r = blockIdx.x;
+  const int ns = W.ray_ns[r];
+  RaySetup rs;
+  load_ray_setup(W, r, rs);
+  for (int h = threadIdx.x; h < kStageHash; h += blockDim.x) hkey[h] = -1;
+  if (threadIdx.x == 0) {
+    nslot = 0;
+    tc::mbar_init(&bar, 1);
+  }
+  __syncthreads();
+  // the leaves of the evaluated samples' corners
+  for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+    float idx[3];
+    if (!alpha_eval_index(gd, P, rs, k, idx)) continue;
+    const int i = ifloor(idx[0]), j = ifloor(idx[1]), kk = ifloor(idx[2]);
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    rs.start[a] = W.ray_sd[r * 6 + a];
-    rs.dir[a] = W.ray_sd[r * 6 + 3 + a];
+    for (int c = 0; c < 8; ++c) {
+      int di, dj, dk;
+      corner_delta(c, di, dj, dk);
+      // a corner in another leaf than corner 0 only where the cell crosses a leaf face
+      if (c > 0 && !(((i & 7) == 7 && di) || ((j & 7) == 7 && dj) || ((kk & 7) == 7 && dk)))
+        continue;
+      const int l = leaf_of(gd, i + di, j + dj, kk + dk);
+      if (l >= 0) stage_insert(hkey, hslot, &nslot, l);
+    }
+  }
+  __syncthreads();
+  const uint32_t nstaged = min(nslot, uint32_t(kStageSlots));
+  bool staged = nstaged > 0;
+  if (staged) {
+    __shared__ int held;
+    if (threadIdx.x == 0) {
+      tc::mbar_expect_tx(&bar, nstaged * uint32_t(kLeafVox * 4));
+      // test hook: the first block with leaves to stage issues no copies
+      held = hold && atomicCAS(W.totals + 2, 0u, 1u) == 0u;
+    }
+    __syncthreads();  // the transaction count is set before any copy lands
+    if (threadIdx.x < 32 && !held) {
+      for (int h = threadIdx.x; h < kStageHash; h += 32) {
+        const int l = hkey[h], sl = hslot[h];
+        if (l >= 0 && sl >= 0)
+          tc::bulk_g2s(st_vox + sl * kLeafVox, gd.data + int64_t(l) * kLeafVox,
+                       uint32_t(kLeafVox * 4), &bar);
+      }
+    }
+    if (!tc::mbar_wait(&bar, 0, spin_max)) {
+      atomicOr(W.totals + 3, 8u);
+      staged = false;
+    }
   }
   const int64_t sbase = int64_t(r) * P.cap;
   for (int k = threadIdx.x; k < ns; k += blockDim.x) {
-    float p[3];
-    ray_point(rs, P.stepdist, k, p);
+    float idx[3];
     float alpha = 0.f;
-    bool skip = false;
-    if (gd.bmax) {
-      // brick of the (approximate) cell; its bound covers the cells next to it
-      int b[3];
+    if (alpha_eval_index(gd, P, rs, k, idx)) {
+      const int i = ifloor(idx[0]), j = ifloor(idx[1]), kk = ifloor(idx[2]);
+      const float u = idx[0] - float(i), v = idx[1] - float(j), w = idx[2] - float(kk);
+      const bool inner = (i & 7) != 7 && (j & 7) != 7 && (kk & 7) != 7;
+      const int l0 = leaf_of(gd, i, j, kk);
+      const int s0 = staged && l0 >= 0 ? stage_find(hkey, hslot, l0) : -1;
+      float val[8];
 #pragma unroll
-      for (int a = 0; a < 3; ++a)
-        b[a] = min(max(int(floorf((p[a] - P.mn[a]) * P.binv[a])), 0), gd.bdim[a] - 1);
-      const uint32_t key = __ldg(gd.bmax + (b[0] * gd.bdim[1] + b[1]) * gd.bdim[2] + b[2]);
-      skip = fkey_inv(key) < P.sigma_skip;
-    }
-    if (!skip && !out_of_bbox(p, P.mn, P.mx) &&
-        (!P.mask || mask_lookup(P.mask, P.mshape, p, P.mscale, P.mshift))) {
-      float idx[3];
-      world_to_index(p, P.mn, P.ext, P.wsm1, idx);
-      const float sigma = trilinear1(gd, idx[0], idx[1], idx[2]);
-      float e;
-      const float a = raw2alpha(sigma, P.shift, P.interval, e);
-      if (a > P.thr) alpha = a;
+      for (int c = 0; c < 8; ++c) {
+        int di, dj, dk;
+        corner_delta(c, di, dj, dk);
+        const int off = vox_offset(i + di, j + dj, kk + dk);
+        int l = l0, sl = s0;
+        if (!inner && c > 0) {
+          l = leaf_of(gd, i + di, j + dj, kk + dk);
+          sl = staged && l >= 0 ? stage_find(hkey, hslot, l) : -1;
+        }
+        val[c] = l < 0 ? gd.background
+                 : sl >= 0 ? st_vox[sl * kLeafVox + off]
+                           : __ldg(gd.data + (int64_t(l) << 9) + off);
+      }
+      alpha = alpha_of(P, trilinear1_values(val, u, v, w));
     }
     W.k_alpha[sbase + k] = alpha;
   }
+  if (nstaged > 0 && !staged && threadIdx.x == 0)
+    tc::mbar_wait(&bar, 0, spin_max);  // copies still in flight land before the block exits
 }
 
 constexpr int kChainBatch = 8;  // 32-sample chunks whose alphas are loaded together
@@ -1010,8 +1157,16 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
     const int nb = ceil_div(R, kMarchWarps);
     k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_setup");
-    k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
-    PVDB_CHECK_LAUNCH("k_march_alpha");
+    if (m->leaf_staging) {
+      PVDB_SMEM_ATTR(k_march_alpha_staged, int(kStageSmem));
+      k_march_alpha_staged<<<R, 256, kStageSmem, st>>>(density->view(), m->p, m->w,
+                                                       debug_spin_limit(kStageSpinMax),
+                                                       debug_hold_staging());
+      PVDB_CHECK_LAUNCH("k_march_alpha_staged");
+    } else {
+      k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
+      PVDB_CHECK_LAUNCH("k_march_alpha");
+    }
     k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w, debug_spin_limit(kChainSpinMax),
                                                 debug_hold_first());
     PVDB_CHECK_LAUNCH("k_march_chain");
@@ -1246,6 +1401,13 @@ int pvdb_march_create(int32_t max_rays, int32_t samples_cap, pvdb_march* out) {
   return PVDB_OK;
 }
 
+int pvdb_march_set_leaf_staging(pvdb_march m, int32_t on) {
+  clear_error();
+  if (!m) return set_error(PVDB_ERR_ARG, "pvdb_march_set_leaf_staging: null workspace");
+  m->leaf_staging = on ? 1 : 0;
+  return PVDB_OK;
+}
+
 int pvdb_march_destroy(pvdb_march m) {
   if (!m) return PVDB_OK;
   MarchW& w = m->w;
@@ -1313,6 +1475,9 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
   if (t[3] & 1u) return set_error(PVDB_ERR_STATE, "a ray had more samples than samples_cap");
   if (t[3] & 2u) return set_error(PVDB_ERR_TIMEOUT, "a tensor-core MMA wait timed out");
   if (t[3] & 4u) return set_error(PVDB_ERR_TIMEOUT, "a ray-offset look-back wait of the march timed out");
+  if (t[3] & 8u)
+    return set_error(PVDB_ERR_TIMEOUT, "a leaf-staging copy wait of the march timed out "
+                                       "(those samples read global memory)");
   return PVDB_OK;
 }
 

@@ -50,8 +50,9 @@ struct MarchW {
   // rgbnet backward's output
   float4* b_rec;
   int32_t* b_row;
-  // [0] total kept, [1] total colour rows, [2] 8*total kept, [3] error flags
-  // (1 samples_cap exceeded, 2 tensor-core wait, 4 ray-offset look-back
+  // [0] total kept, [1] total colour rows, [2] block claimed by the
+  // leaf-staging test hook, [3] error flags (1 samples_cap exceeded,
+  // 2 tensor-core wait, 4 ray-offset look-back wait, 8 leaf-staging copy
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
   // [6] k_march_chain ray counter, [7] train-step loss block counter
   uint32_t* totals;
@@ -86,6 +87,7 @@ struct pvdb_march_s {
   int n_rays = 0;
   bool has_fwd = false;
   bool prof = false;  // record stage-profiler marks (set by the train step)
+  int leaf_staging = 0;  // density leaves staged in shared memory (pvdb_march_set_leaf_staging)
   pvdb_grid_s* density = nullptr;
   pvdb_grid_s* k0 = nullptr;
   // rgbnet scratch (mlp.cu)

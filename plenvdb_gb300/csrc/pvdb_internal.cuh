@@ -230,16 +230,10 @@ __device__ __forceinline__ void corner_slots(const GridView& g, int i, int j, in
 }
 
 // Density trilinear with the reference's association: for each corner in order,
-// res += ((v*(1-u))*(1-v))*(1-w) (densityvdb.cu:115-123).
-__device__ __forceinline__ float trilinear1(const GridView& g, float x, float y, float z) {
-  const int i = ifloor(x), j = ifloor(y), k = ifloor(z);
-  const float u = x - float(i), v = y - float(j), w = z - float(k);
+// res += ((v*(1-u))*(1-v))*(1-w) (densityvdb.cu:115-123), from the 8 corner
+// values in the order of corner_delta.
+__device__ __forceinline__ float trilinear1_values(const float val[8], float u, float v, float w) {
   const float iu = 1.f - u, iv = 1.f - v, iw = 1.f - w;
-  int s[8];
-  corner_slots(g, i, j, k, s);
-  float val[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) val[c] = s[c] < 0 ? g.background : __ldg(g.data + s[c]);
   float r = 0.f;
   r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[0], iu), iv), iw));
   r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[1], iu), iv), w));
@@ -250,6 +244,17 @@ __device__ __forceinline__ float trilinear1(const GridView& g, float x, float y,
   r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[6], u), iv), w));
   r = __fadd_rn(r, __fmul_rn(__fmul_rn(__fmul_rn(val[7], u), iv), iw));
   return r;
+}
+
+// Density trilinear at index-space position (x, y, z).
+__device__ __forceinline__ float trilinear1(const GridView& g, float x, float y, float z) {
+  const int i = ifloor(x), j = ifloor(y), k = ifloor(z);
+  int s[8];
+  corner_slots(g, i, j, k, s);
+  float val[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) val[c] = s[c] < 0 ? g.background : __ldg(g.data + s[c]);
+  return trilinear1_values(val, x - float(i), y - float(j), z - float(k));
 }
 
 // Trilinear corner weights for the multi-channel formula (colorvdb.cu:100-107):
@@ -325,10 +330,12 @@ int radix_sort_pairs(ReduceScratch& rs, int64_t n, int key_bits, bool iota_vals,
 int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev, int key_bits,
                          bool iota_vals, int* out_buf, cudaStream_t st, uint32_t** status = nullptr);
 // Test hooks of the bounded device waits (pvdb_debug_wait_limit): the spin
-// limit of the look-back waits (0 = the built-in limit) and whether the first
-// publisher of a look-back chain withholds its count.
+// limit of the look-back waits (0 = the built-in limit), whether the first
+// publisher of a look-back chain withholds its count, and whether the first
+// block of the staged density pass issues no leaf copies.
 uint32_t debug_spin_limit(uint32_t builtin);
 int debug_hold_first();
+int debug_hold_staging();
 // Reads a device status word back (the stream is synchronised) and maps a
 // nonzero value to PVDB_ERR_TIMEOUT with the given message.
 int read_wait_status(const uint32_t* status, cudaStream_t st, const char* what);

@@ -490,7 +490,8 @@ uint32_t debug_spin_limit(uint32_t builtin) {
   return v ? v : builtin;
 }
 
-int debug_hold_first() { return g_dbg_hold.load(); }
+int debug_hold_first() { return g_dbg_hold.load() == 1 ? 1 : 0; }
+int debug_hold_staging() { return g_dbg_hold.load() == 2 ? 1 : 0; }
 
 int read_wait_status(const uint32_t* status, cudaStream_t st, const char* what) {
   uint32_t h = 0;
@@ -514,7 +515,7 @@ using namespace pvdb;
 extern "C" int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first) {
   clear_error();
   g_dbg_spin.store(spins);
-  g_dbg_hold.store(hold_first ? 1 : 0);
+  g_dbg_hold.store(hold_first == 2 ? 2 : hold_first ? 1 : 0);
   return PVDB_OK;
 }
 

@@ -402,6 +402,7 @@ static std::vector<uint8_t> graph_key(const TrainArgs& t) {
   key_put(k, m->red.vals[0]);
   key_put(k, m->red.vals[1]);
   key_put(k, m->b_rec_s);
+  key_put(k, m->leaf_staging);
   key_put(k, m->red.hist);
   key_put(k, m->red.partial);
   key_put(k, m->scan_partial);

@@ -45,7 +45,8 @@ def march_params(xyz_min, xyz_max, near, stepdist, act_shift, interval, fast_col
 class MarchWorkspace:
     """Owns a pvdb_march workspace for up to max_rays rays."""
 
-    def __init__(self, max_rays: int, xyz_min, xyz_max, stepdist: float, samples_cap: int = 0):
+    def __init__(self, max_rays: int, xyz_min, xyz_max, stepdist: float, samples_cap: int = 0,
+                 leaf_staging: bool = False):
         lib = L.load()
         if samples_cap <= 0:
             samples_cap = lib.pvdb_march_samples_cap(L.f32arr(xyz_min), L.f32arr(xyz_max),
@@ -58,6 +59,13 @@ class MarchWorkspace:
         self.generation = 0
         self.k0_channels = 0
         self.n_rays = 0
+        if leaf_staging:
+            self.set_leaf_staging(True)
+
+    def set_leaf_staging(self, on: bool) -> None:
+        """Stage the density leaves of the forward's density pass in shared
+        memory (bulk copies); bitwise the same results."""
+        L.call("pvdb_march_set_leaf_staging", self.h, 1 if on else 0)
 
     def __del__(self):
         try:

@@ -45,6 +45,7 @@ class FineStageConfig:
     tv_dense_mode: bool = False
     precision: int = 0              # 0 FP32 SIMT rgbnet, 1 BF16 tensor cores
     use_graph: bool = True          # replay the fused step as a captured CUDA graph
+    leaf_staging: bool = False      # density leaves staged in shared memory by bulk copies
 
     @property
     def voxel_size(self) -> float:
@@ -63,7 +64,8 @@ class FineStageTrainer:
         b0, b1 = cfg.betas
         self.dopt = DensityOpt(density, cfg.lr_density, cfg.eps, b0, b1)
         self.kopt = ColorOpt(k0, cfg.lr_k0, cfg.eps, b0, b1)
-        self.ws = MarchWorkspace(max_rays, cfg.xyz_min, cfg.xyz_max, cfg.stepdist)
+        self.ws = MarchWorkspace(max_rays, cfg.xyz_min, cfg.xyz_max, cfg.stepdist,
+                                 leaf_staging=cfg.leaf_staging)
         w0, b0_, w1, b1_, w2, b2 = rgbnet_params
         self.c0 = k0.ndim
         self.pe = (w0.shape[1] - self.c0 - 3) // 6

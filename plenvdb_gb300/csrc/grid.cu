@@ -86,6 +86,22 @@ __device__ __forceinline__ void slot_coord(const GridView& g, int leaf, int vox,
   z = __ldg(g.origin + leaf * 3 + 2) + (vox & 7);
 }
 
+// Slots of the 6 face neighbours of voxel (x, y, z) = (leaf, vox), in the order
+// -z, +z, -y, +y, -x, +x: -2 outside [0, reso) (no TV term), -1 in no
+// allocated leaf (background). A neighbour inside the voxel's own leaf follows
+// from the offset layout (+64 x, +8 y, +1 z) without a table lookup.
+__device__ __forceinline__ void face_neighbours(const GridView& g, int leaf, int vox, int x, int y,
+                                                int z, int nb[6]) {
+  const int base = leaf << 9;
+  const int lx = vox >> 6, ly = (vox >> 3) & 7, lz = vox & 7;
+  nb[0] = z == 0 ? -2 : lz > 0 ? base | (vox - 1) : slot_of(g, x, y, z - 1);
+  nb[1] = z == g.reso[2] - 1 ? -2 : lz < 7 ? base | (vox + 1) : slot_of(g, x, y, z + 1);
+  nb[2] = y == 0 ? -2 : ly > 0 ? base | (vox - 8) : slot_of(g, x, y - 1, z);
+  nb[3] = y == g.reso[1] - 1 ? -2 : ly < 7 ? base | (vox + 8) : slot_of(g, x, y + 1, z);
+  nb[4] = x == 0 ? -2 : lx > 0 ? base | (vox - 64) : slot_of(g, x - 1, y, z);
+  nb[5] = x == g.reso[0] - 1 ? -2 : lx < 7 ? base | (vox + 64) : slot_of(g, x + 1, y, z);
+}
+
 // copyFromDense: active voxels only (densityvdb.cu:39-48, colorvdb.cu:52-62).
 __global__ void k_copy_from_dense(GridView g, float* dst, const float* __restrict__ arr, int rx,
                                   int ry, int rz) {
@@ -208,14 +224,8 @@ __global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
     int x, y, z;
     slot_coord(g, leaf, vox, x, y, z);
     if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) continue;
-    // neighbour slots; -2 = outside [0,reso) (no term), -1 = no leaf (background)
     int nb[6];
-    nb[0] = z == 0 ? -2 : slot_of(g, x, y, z - 1);
-    nb[1] = z == g.reso[2] - 1 ? -2 : slot_of(g, x, y, z + 1);
-    nb[2] = y == 0 ? -2 : slot_of(g, x, y - 1, z);
-    nb[3] = y == g.reso[1] - 1 ? -2 : slot_of(g, x, y + 1, z);
-    nb[4] = x == 0 ? -2 : slot_of(g, x - 1, y, z);
-    nb[5] = x == g.reso[0] - 1 ? -2 : slot_of(g, x + 1, y, z);
+    face_neighbours(g, leaf, vox, x, y, z, nb);
     const float wt[6] = {wz, wz, wy, wy, wx, wx};
     const int64_t t0 = (int64_t(leaf) * kLeafVox + vox) * g.C;
     for (int ch = 0; ch < g.C; ++ch) {
@@ -284,12 +294,7 @@ __global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mod
     slot_coord(g, leaf, vox, x, y, z);
     if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) continue;
     int nb[6];
-    nb[0] = z == 0 ? -2 : slot_of(g, x, y, z - 1);
-    nb[1] = z == g.reso[2] - 1 ? -2 : slot_of(g, x, y, z + 1);
-    nb[2] = y == 0 ? -2 : slot_of(g, x, y - 1, z);
-    nb[3] = y == g.reso[1] - 1 ? -2 : slot_of(g, x, y + 1, z);
-    nb[4] = x == 0 ? -2 : slot_of(g, x - 1, y, z);
-    nb[5] = x == g.reso[0] - 1 ? -2 : slot_of(g, x + 1, y, z);
+    face_neighbours(g, leaf, vox, x, y, z, nb);
     const float wt[6] = {wz, wz, wy, wy, wx, wx};
     float p[12], add[12];
     const float4* d4 = reinterpret_cast<const float4*>(g.data + t0);

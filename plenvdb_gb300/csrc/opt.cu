@@ -73,6 +73,71 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
   }
 }
 
+// The same update for scalar grids (density), one thread per voxel. A warp's
+// 32 voxels are 32 consecutive offsets of one leaf (one x, four y, all z), so
+// the brick bounds their growing values raise span at most 2 x 3 x 3 bricks:
+// the warp takes the max per brick and issues one atomicMax for it, instead of
+// up to 8 atomics per voxel on the same few words. The bounds end as by
+// bmax_raise. Per-voxel arithmetic is identical to k_vdb_adam.
+__global__ void __launch_bounds__(256)
+    k_vdb_adam1(GridView g, float* __restrict__ m, float* __restrict__ v,
+                const float* __restrict__ perlr, float stepsz, const float* __restrict__ stepsz_dev,
+                float eps, float b0, float b1, int mode, int zero_after,
+                const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+  const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
+  if (stepsz_dev) stepsz = *stepsz_dev;
+  const int lane = threadIdx.x & 31;
+  // whole leaves and whole warps: every lane of a warp takes the same trips
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list ? list[i >> 9] : int(i >> 9);
+    const int vox = int(i & 511);
+    const int64_t slot = int64_t(leaf) * kLeafVox + vox;
+    const bool active = (__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull;
+    const float gr = active ? g.grad[slot] : 0.f;
+    bool grew = false;
+    float nv = 0.f;
+    if (active && !(mode == 1 && gr == 0.f)) {
+      const float lrf = mode == 2 ? perlr[slot] : 1.f;
+      const float mn = b0 * m[slot] + (1 - b0) * gr;
+      const float vn = b1 * v[slot] + (1 - b1) * gr * gr;
+      m[slot] = mn;
+      v[slot] = vn;
+      const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
+      const float old = g.data[slot];
+      nv = old - num / (eps + sqrtf(vn));
+      g.data[slot] = nv;
+      if (zero_after) g.grad[slot] = 0.f;
+      grew = !(nv <= old);
+    }
+    // keep the march's brick bound an upper bound
+    if (!g.bmax || !__any_sync(0xffffffffu, grew)) continue;
+    const int x = g.origin[leaf * 3] + (vox >> 6);
+    const int y = g.origin[leaf * 3 + 1] + ((vox >> 3) & 7);
+    const int z = g.origin[leaf * 3 + 2] + (vox & 7);
+    const int x0 = max((x - 2) >> 2, 0), x1 = min((x + 1) >> 2, g.bdim[0] - 1);
+    const int y0 = max((y - 2) >> 2, 0), y1 = min((y + 1) >> 2, g.bdim[1] - 1);
+    const int z0 = max((z - 2) >> 2, 0), z1 = min((z + 1) >> 2, g.bdim[2] - 1);
+    const int big = 1 << 30;
+    const int ux0 = __reduce_min_sync(0xffffffffu, grew ? x0 : big);
+    const int ux1 = __reduce_max_sync(0xffffffffu, grew ? x1 : -1);
+    const int uy0 = __reduce_min_sync(0xffffffffu, grew ? y0 : big);
+    const int uy1 = __reduce_max_sync(0xffffffffu, grew ? y1 : -1);
+    const int uz0 = __reduce_min_sync(0xffffffffu, grew ? z0 : big);
+    const int uz1 = __reduce_max_sync(0xffffffffu, grew ? z1 : -1);
+    const uint32_t key = grew ? fkey(nv) : 0u;
+    for (int bx = ux0; bx <= ux1; ++bx)
+      for (int by = uy0; by <= uy1; ++by)
+        for (int bz = uz0; bz <= uz1; ++bz) {
+          const bool mine = grew && bx >= x0 && bx <= x1 && by >= y0 && by <= y1 && bz >= z0 &&
+                            bz <= z1;
+          const uint32_t kmax = __reduce_max_sync(0xffffffffu, mine ? key : 0u);
+          if (lane == 0 && kmax)
+            atomicMax(g.bmax + (int64_t(bx) * g.bdim[1] + by) * g.bdim[2] + bz, kmax);
+        }
+  }
+}
+
 // The same update for 12-channel grids (k0), one thread per voxel with the
 // channels in float4 loads; the four Vec3 groups keep their own skip rule.
 // Per-channel arithmetic is identical to k_vdb_adam.
@@ -219,6 +284,11 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
           o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half);
+    else if (g->C == 1)
+      k_vdb_adam1<<<stride_grid(), 256, 0, st>>>(
+          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
+          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
     else
       k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,

@@ -85,6 +85,9 @@ def parse():
                     help="skip the timings of the steps around the training step")
     ap.add_argument("--lifecycle-only", action="store_true",
                     help="only the lifecycle timings (for profiling their kernels)")
+    ap.add_argument("--large-only", action="store_true",
+                    help="only the 320^3 / 65536-ray training measurement (for profiling "
+                         "its kernels)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the fused step eagerly instead of replaying a CUDA graph")
@@ -1149,6 +1152,14 @@ def main():
         dg, kg = build_grids(scfg)
         grids = type("Grids", (), {"density": dg, "k0": kg})()
         print(json.dumps({"lifecycle": run_lifecycle(scfg, cfg, CameraConfig(), grids)}),
+              flush=True)
+        torch.cuda.synchronize()
+    elif args.large_only:
+        import torch
+
+        from plenvdb_gb300 import _lib as L
+        L.load()
+        print(json.dumps({"large": run_large(args, steps=args.steps, warmup=args.warmup)}),
               flush=True)
         torch.cuda.synchronize()
     else:

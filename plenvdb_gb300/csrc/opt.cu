@@ -75,10 +75,14 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
 
 // The same update for scalar grids (density), one thread per voxel. A warp's
 // 32 voxels are 32 consecutive offsets of one leaf (one x, four y, all z), so
-// the brick bounds their growing values raise span at most 2 x 3 x 3 bricks:
-// the warp takes the max per brick and issues one atomicMax for it, instead of
-// up to 8 atomics per voxel on the same few words. The bounds end as by
-// bmax_raise. Per-voxel arithmetic is identical to k_vdb_adam.
+// the brick bounds their growing values raise (bmax_raise) span at most
+// 2 x 3 x 4 bricks: the warp raises every brick of that box to the largest
+// grown value, one atomicMax per brick from its own lane, instead of up to 8
+// atomics per voxel on the same few words. A bound may end above bmax_raise's
+// (by a value from at most a few voxels away); it stays an upper bound, which
+// is all the march's skip test needs (a skipped sample's alpha is below the
+// threshold either way, so results do not depend on it). Per-voxel
+// arithmetic is identical to k_vdb_adam.
 __global__ void __launch_bounds__(256)
     k_vdb_adam1(GridView g, float* __restrict__ m, float* __restrict__ v,
                 const float* __restrict__ perlr, float stepsz, const float* __restrict__ stepsz_dev,
@@ -125,16 +129,12 @@ __global__ void __launch_bounds__(256)
     const int uy1 = __reduce_max_sync(0xffffffffu, grew ? y1 : -1);
     const int uz0 = __reduce_min_sync(0xffffffffu, grew ? z0 : big);
     const int uz1 = __reduce_max_sync(0xffffffffu, grew ? z1 : -1);
-    const uint32_t key = grew ? fkey(nv) : 0u;
-    for (int bx = ux0; bx <= ux1; ++bx)
-      for (int by = uy0; by <= uy1; ++by)
-        for (int bz = uz0; bz <= uz1; ++bz) {
-          const bool mine = grew && bx >= x0 && bx <= x1 && by >= y0 && by <= y1 && bz >= z0 &&
-                            bz <= z1;
-          const uint32_t kmax = __reduce_max_sync(0xffffffffu, mine ? key : 0u);
-          if (lane == 0 && kmax)
-            atomicMax(g.bmax + (int64_t(bx) * g.bdim[1] + by) * g.bdim[2] + bz, kmax);
-        }
+    const uint32_t kmax = __reduce_max_sync(0xffffffffu, grew ? fkey(nv) : 0u);
+    const int ny = uy1 - uy0 + 1, nz = uz1 - uz0 + 1;
+    if (kmax && lane < (ux1 - ux0 + 1) * ny * nz) {  // at most 24 bricks: one per lane
+      const int bx = ux0 + lane / (ny * nz), by = uy0 + (lane / nz) % ny, bz = uz0 + lane % nz;
+      atomicMax(g.bmax + (int64_t(bx) * g.bdim[1] + by) * g.bdim[2] + bz, kmax);
+    }
   }
 }
 

@@ -595,15 +595,23 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
           gv[c] = __ldg(grad_rgb + mrow * 3 + c);
         }
       }
-      // ---- E0: H0 = relu(Z0)
+      // ---- E0: H0 = relu(Z0) (the thread's 64 columns in one TMEM round trip)
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
+      {
+        uint32_t r[64];
 #pragma unroll
-      for (int cb = 0; cb < 64; cb += 32) {
-        float v[32];
-        tc::tmem_ld32(tA + uint32_t(cb), v);
-        store_relu32(h0, row, c0 + cb, 144, v, nullptr);
+        for (int q = 0; q < 4; ++q) tc::tmem_ld16_issue(tA + uint32_t(16 * q), r + 16 * q);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          float v[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) v[e] = __uint_as_float(r[8 * g + e]);
+          *reinterpret_cast<uint4*>(h0 + tc::kmaj(row, c0 + 8 * g, 144)) =
+              relu_pack8(v, nullptr, 0);
+        }
       }
       epi_done(ebar + s);
       // ---- E1: H1 = relu(Z1 + b1); dl = grad_rgb * y * (1 - y)
@@ -669,7 +677,12 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       for (int g = 0; g < 8; ++g)
         *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + 8 * g, 128)) = hp[g];
       epi_done(ebar + s);
-      // ---- E3: dZ0 = dH0 * [H0 > 0], over dZ1
+      // ---- E3: dZ0 = dH0 * [H0 > 0], over dZ1 (the thread's own H0 columns,
+      // written by its E0, are read before the wait)
+      uint4 hm[8];
+#pragma unroll
+      for (int g = 0; g < 8; ++g)
+        hm[g] = *reinterpret_cast<const uint4*>(h0 + tc::kmaj(row, c0 + 8 * g, 144));
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
@@ -678,12 +691,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         float v[32];
         tc::tmem_ld32(tA + uint32_t(cb), v);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const uint4 h =
-              *reinterpret_cast<const uint4*>(h0 + tc::kmaj(row, c0 + cb + 8 * c, 144));
+        for (int c = 0; c < 4; ++c)
           *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128)) =
-              mask_pack(v + 8 * c, h);
-        }
+              mask_pack(v + 8 * c, hm[cb / 8 + c]);
       }
       epi_done(ebar + s);
       // ---- E4: grad k0; the tile's X buffer is free again (S4 is done): it

@@ -174,11 +174,27 @@ static int train_reserve(pvdb_march_s* m, int C) {
   return PVDB_OK;
 }
 
-// Writes the step sizes a captured train step reads.
-__global__ void k_set_step_scalars(float* scal, float ss_d, float ss_k, float ss_n) {
-  scal[0] = ss_d;
-  scal[1] = ss_k;
-  scal[2] = ss_n;
+// Before a graph replay: the step's rays, view directions and targets into the
+// fixed input buffer the captured step reads (dst = [rays_o | rays_d |
+// viewdirs | target], n3 floats each), and the step sizes it reads; one
+// launch for what would be four copies and a scalar write.
+__global__ void __launch_bounds__(256)
+    k_step_inputs(float* __restrict__ dst, const float* __restrict__ ro,
+                  const float* __restrict__ rd, const float* __restrict__ vd,
+                  const float* __restrict__ tgt, int64_t n3, float* scal, float ss_d, float ss_k,
+                  float ss_n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[0] = ss_d;
+    scal[1] = ss_k;
+    scal[2] = ss_n;
+  }
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < 4 * n3;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int q = int(i / n3);
+    const int64_t e = i - int64_t(q) * n3;
+    const float* src = q == 0 ? ro : q == 1 ? rd : q == 2 ? vd : tgt;
+    dst[i] = __ldg(src + e);
+  }
 }
 
 struct TrainArgs {
@@ -509,12 +525,11 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   *net->step += 1;
   t.ss[2] = adam_step_size(*net->lr, cfg->rgbnet_beta1, cfg->rgbnet_beta2, *net->step);
   if (graph_ok) {
-    const size_t R3 = size_t(n_rays) * 3;
-    k_set_step_scalars<<<1, 1, 0, st>>>(m->g_scal, t.ss[0], t.ss[1], t.ss[2]);
-    PVDB_CHECK_LAUNCH("k_set_step_scalars");
-    const float* src[4] = {rays_o, rays_d, viewdirs, target};
-    for (int q = 0; q < 4; ++q)
-      PVDB_CHECK_CUDA(cudaMemcpyAsync(m->g_in + q * R3, src[q], R3 * 4, cudaMemcpyDeviceToDevice, st));
+    const int64_t R3 = int64_t(n_rays) * 3;
+    k_step_inputs<<<int(std::min<int64_t>(ceil_div(4 * R3, 256), int64_t(2 * num_sms()))), 256,
+                    0, st>>>(m->g_in, rays_o, rays_d, viewdirs, target, R3, m->g_scal, t.ss[0],
+                             t.ss[1], t.ss[2]);
+    PVDB_CHECK_LAUNCH("k_step_inputs");
     PVDB_CHECK_CUDA(cudaGraphLaunch(m->g_exec, st));
     count_launches(int(m->g_launches));
     PVDB_CHECK_CUDA(cudaMemcpyAsync(loss_out, m->g_scal + 4, 4, cudaMemcpyDeviceToDevice, st));

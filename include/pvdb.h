@@ -453,7 +453,10 @@ typedef struct pvdb_train_config {
   float lr_decay_factor;                 /* applied after the step (run.py:592-598) */
   float rgbnet_lr, rgbnet_beta1, rgbnet_beta2, rgbnet_eps;
   int32_t precision;                     /* 0 FP32, 1 BF16 rgbnet */
-  int32_t use_graph;                     /* 1: replay the step as a captured CUDA graph */
+  int32_t use_graph;                     /* 1: replay the step as a captured CUDA graph
+                                            (captured once the same buffers, configuration
+                                            and loss_out were seen twice in a row; a call
+                                            with other ones runs eagerly and recaptures) */
 } pvdb_train_config;
 
 typedef struct pvdb_rgbnet_state {

@@ -457,6 +457,11 @@ typedef struct pvdb_train_config {
                                             (captured once the same buffers, configuration
                                             and loss_out were seen twice in a row; a call
                                             with other ones runs eagerly and recaptures) */
+  int32_t tv_in_place;                   /* sparse TV (tv_dense_mode 0): 0 computes the TV
+                                            terms beside the gradient sums and the voxel
+                                            Adam adds them to the channels with a gradient;
+                                            1 adds them to the gradient in place first, as
+                                            the reference does. The same values either way */
 } pvdb_train_config;
 
 typedef struct pvdb_rgbnet_state {

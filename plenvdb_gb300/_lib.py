@@ -74,7 +74,7 @@ class TrainConfig(C.Structure):
                 ("weight_rgbper", f32), ("tv_weight_density", f32), ("tv_weight_k0", f32),
                 ("tv_dense_mode", i32), ("lr_decay_factor", f32), ("rgbnet_lr", f32),
                 ("rgbnet_beta1", f32), ("rgbnet_beta2", f32), ("rgbnet_eps", f32),
-                ("precision", i32), ("use_graph", i32)]
+                ("precision", i32), ("use_graph", i32), ("tv_in_place", i32)]
 
 
 class RgbnetState(C.Structure):

@@ -337,6 +337,100 @@ __global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mod
   }
 }
 
+// The TV sums of k_tv / k_tv_c12 (same neighbours, order and rounding)
+// without the gradient: tv[slot*C + ch] for every active voxel of the listed
+// leaves (0 outside [0, reso)). In sparse mode k_tv adds them to the channels
+// whose gradient is nonzero; the fused step's voxel Adam does that addition
+// instead, so this pass needs only the values and can run beside the
+// gradient sums.
+__global__ void k_tv_terms(GridView g, float wx, float wy, float wz,
+                           const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
+                           float* __restrict__ tv) {
+  const int64_t nl = *count;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list[i >> 9];
+    const int vox = int(i & 511);
+    if (!is_active(g, leaf, vox)) continue;
+    const int64_t t0 = (int64_t(leaf) * kLeafVox + vox) * g.C;
+    int x, y, z;
+    slot_coord(g, leaf, vox, x, y, z);
+    if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) {
+      for (int ch = 0; ch < g.C; ++ch) tv[t0 + ch] = 0.f;
+      continue;
+    }
+    int nb[6];
+    face_neighbours(g, leaf, vox, x, y, z, nb);
+    const float wt[6] = {wz, wz, wy, wy, wx, wx};
+    for (int ch = 0; ch < g.C; ++ch) {
+      const float p = g.data[t0 + ch];
+      float add = 0.f;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (nb[q] == -2) continue;
+        const float vn = nb[q] < 0 ? g.background : g.data[int64_t(nb[q]) * g.C + ch];
+        add = __fadd_rn(add, __fmul_rn(wt[q], tv_clamp(p - vn)));
+      }
+      tv[t0 + ch] = add;
+    }
+  }
+}
+
+__global__ void k_tv_terms_c12(GridView g, float wx, float wy, float wz,
+                               const int32_t* __restrict__ list,
+                               const uint32_t* __restrict__ count, float* __restrict__ tv) {
+  const int64_t nl = *count;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int leaf = list[i >> 9];
+    const int vox = int(i & 511);
+    if (!is_active(g, leaf, vox)) continue;
+    const int64_t t0 = (int64_t(leaf) * kLeafVox + vox) * 12;
+    float4* o4 = reinterpret_cast<float4*>(tv + t0);
+    int x, y, z;
+    slot_coord(g, leaf, vox, x, y, z);
+    if (x >= g.reso[0] || y >= g.reso[1] || z >= g.reso[2]) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) o4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    int nb[6];
+    face_neighbours(g, leaf, vox, x, y, z, nb);
+    const float wt[6] = {wz, wz, wy, wy, wx, wx};
+    float p[12], add[12];
+    const float4* d4 = reinterpret_cast<const float4*>(g.data + t0);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float4 v = d4[b];
+      p[4 * b] = v.x; p[4 * b + 1] = v.y; p[4 * b + 2] = v.z; p[4 * b + 3] = v.w;
+    }
+#pragma unroll
+    for (int ch = 0; ch < 12; ++ch) add[ch] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      if (nb[q] == -2) continue;
+      float vn[12];
+      if (nb[q] < 0) {
+#pragma unroll
+        for (int ch = 0; ch < 12; ++ch) vn[ch] = g.background;
+      } else {
+        const float4* n4 = reinterpret_cast<const float4*>(g.data + int64_t(nb[q]) * 12);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const float4 v = n4[b];
+          vn[4 * b] = v.x; vn[4 * b + 1] = v.y; vn[4 * b + 2] = v.z; vn[4 * b + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int ch = 0; ch < 12; ++ch)
+        add[ch] = __fadd_rn(add[ch], __fmul_rn(wt[q], tv_clamp(p[ch] - vn[ch])));
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      o4[b] = make_float4(add[4 * b], add[4 * b + 1], add[4 * b + 2], add[4 * b + 3]);
+  }
+}
+
 __global__ void k_touched_compact(const uint8_t* __restrict__ touched, int nleaf, int32_t* list,
                                   uint32_t* count) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
@@ -472,6 +566,27 @@ __global__ void k_half_build(const float* __restrict__ src, __nv_bfloat16* dst, 
   d4[0] = make_uint4(tc::pack_bf16(a.x, a.y), tc::pack_bf16(a.z, a.w), tc::pack_bf16(b.x, b.y),
                      tc::pack_bf16(b.z, b.w));
   d4[1] = make_uint4(tc::pack_bf16(c.x, c.y), tc::pack_bf16(c.z, c.w), 0u, 0u);
+}
+
+int tv_terms_launch(pvdb_grid_s* g, float wx, float wy, float wz, cudaStream_t st) {
+  if (g->nslots() == 0) return PVDB_OK;
+  if (!g->tlist_valid) return set_error(PVDB_ERR_STATE, "TV terms: the touched list is stale");
+  if (!g->d_tv) {
+    const int rc = dev_alloc((void**)&g->d_tv, size_t(g->nslots()) * g->C * 4);
+    if (rc) return rc;
+  }
+  // the reference divides the weights by 6 on the host (total_variation_kernel.cu:45-47)
+  wx /= 6.f;
+  wy /= 6.f;
+  wz /= 6.f;
+  if (g->C == 12)
+    k_tv_terms_c12<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, g->d_tlist, g->d_tcount,
+                                                  g->d_tv);
+  else
+    k_tv_terms<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, g->d_tlist, g->d_tcount,
+                                              g->d_tv);
+  PVDB_CHECK_LAUNCH("k_tv_terms");
+  return PVDB_OK;
 }
 
 int half_ensure(pvdb_grid_s* g, cudaStream_t st) {
@@ -619,6 +734,7 @@ int pvdb_grid_destroy(pvdb_grid g) {
   dev_free(g->d_tcount);
   dev_free(g->d_bmax);
   dev_free(g->d_half);
+  dev_free(g->d_tv);
   dev_free(g->d_stage);
   free_scratch(g->red);
   delete g;

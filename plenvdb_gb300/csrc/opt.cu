@@ -31,7 +31,7 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
                            const float* __restrict__ perlr, float stepsz,
                            const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
                            int mode, int zero_after, const int32_t* __restrict__ list,
-                           const uint32_t* __restrict__ count) {
+                           const uint32_t* __restrict__ count, const float* __restrict__ tv) {
   const int G = g.C == 1 ? 1 : 3;
   const int ngroups = g.C / G;
   const int64_t per = int64_t(kLeafVox) * ngroups;
@@ -51,6 +51,8 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
     bool allzero = true;
     for (int q = 0; q < G; ++q) {
       gr[q] = g.grad[base + q];
+      // deferred sparse TV: its term joins the channels with a gradient
+      if (tv && gr[q] != 0.f) gr[q] = gr[q] + tv[base + q];
       allzero = allzero && (gr[q] == 0.f);
     }
     if (mode == 1 && allzero) continue;
@@ -87,7 +89,8 @@ __global__ void __launch_bounds__(256)
     k_vdb_adam1(GridView g, float* __restrict__ m, float* __restrict__ v,
                 const float* __restrict__ perlr, float stepsz, const float* __restrict__ stepsz_dev,
                 float eps, float b0, float b1, int mode, int zero_after,
-                const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+                const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
+                const float* __restrict__ tv) {
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   const int lane = threadIdx.x & 31;
@@ -98,7 +101,8 @@ __global__ void __launch_bounds__(256)
     const int vox = int(i & 511);
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
     const bool active = (__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull;
-    const float gr = active ? g.grad[slot] : 0.f;
+    float gr = active ? g.grad[slot] : 0.f;
+    if (tv && gr != 0.f) gr = gr + tv[slot];  // deferred sparse TV
     bool grew = false;
     float nv = 0.f;
     if (active && !(mode == 1 && gr == 0.f)) {
@@ -146,7 +150,8 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
                                const float* __restrict__ perlr, float stepsz,
                                const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
                                int mode, int zero_after, const int32_t* __restrict__ list,
-                               const uint32_t* __restrict__ count, __nv_bfloat16* half) {
+                               const uint32_t* __restrict__ count, __nv_bfloat16* half,
+                               const float* __restrict__ tv) {
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
@@ -161,6 +166,17 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
     for (int b = 0; b < 3; ++b) {
       const float4 x = g4[b];
       gr[4 * b] = x.x; gr[4 * b + 1] = x.y; gr[4 * b + 2] = x.z; gr[4 * b + 3] = x.w;
+    }
+    if (tv) {  // deferred sparse TV: its terms join the channels with a gradient
+      const float4* t4 = reinterpret_cast<const float4*>(tv + slot * 12);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float4 x = t4[b];
+        const float t[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (gr[4 * b + e] != 0.f) gr[4 * b + e] = gr[4 * b + e] + t[e];
+      }
     }
     bool live[4];
     bool any = false;
@@ -254,7 +270,7 @@ int adam_dense_launch(float* param, const float* grad, float* m, float* v, const
 }
 
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st);
+               cudaStream_t st, const float* tv = nullptr);
 
 // Advances the step counter and returns this step's Adam step size.
 float opt_next_stepsz(pvdb_opt_s* o) {
@@ -269,11 +285,14 @@ int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st) {
 
 // The launches of one voxel-Adam step; the step size is stepsz, or
 // *stepsz_dev when that is given (a captured graph reads it each replay).
+// tv (optional): TV terms of the touched leaves' voxels (tv_terms_launch),
+// added to the channels with a nonzero gradient before the update.
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st) {
+               cudaStream_t st, const float* tv) {
   pvdb_grid_s* g = o->params;
   // mode 1 skips voxels whose gradient is zero: only the touched leaves matter
   const bool use_list = mode == 1 && !g->all_touched;
+  if (tv && !use_list) return set_error(PVDB_ERR_STATE, "deferred TV needs the touched leaves");
   if (g->nslots()) {
     if (use_list) {
       int rc = touched_list(g, st);
@@ -283,17 +302,18 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
       k_vdb_adam_c12<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half);
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half,
+          tv);
     else if (g->C == 1)
       k_vdb_adam1<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv);
     else
       k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount);
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv);
     PVDB_CHECK_LAUNCH("k_vdb_adam");
     if (g->C != 12) g->half_valid = false;  // only the 12-channel update writes the shadow
   }

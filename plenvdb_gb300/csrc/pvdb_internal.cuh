@@ -140,6 +140,10 @@ struct pvdb_grid_s {
   // does the brick bound.
   __nv_bfloat16* d_half = nullptr;
   bool half_valid = false;
+  // TV terms of the touched leaves' voxels, [nleaf*512][C] (the fused train
+  // step's deferred sparse TV: written beside the gradient sums, added by the
+  // voxel Adam); allocated at first use
+  float* d_tv = nullptr;
   std::vector<int32_t> h_table;
   std::vector<int32_t> h_origin;
   std::vector<uint64_t> h_mask;
@@ -370,6 +374,10 @@ uint64_t launch_counter();
 int bmax_ensure(pvdb_grid_s* g, cudaStream_t st);
 // Allocates (once) and rebuilds the BF16 shadow of a grid's values if invalid.
 int half_ensure(pvdb_grid_s* g, cudaStream_t st);
+// The TV terms k_tv / k_tv_c12 would add in sparse mode, into g->d_tv, for the
+// active voxels of the grid's touched leaves (the touched list must be
+// current); weights as pvdb_grid_tv_add_grad's.
+int tv_terms_launch(pvdb_grid_s* g, float wx, float wy, float wz, cudaStream_t st);
 // Marks the grid's derived data (brick bound, BF16 shadow) stale after a
 // write of its values that the library does not track.
 inline void data_written(pvdb_grid_s* g) {

@@ -39,7 +39,7 @@ int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st
 int march_backward_clear(pvdb_march_s* m, cudaStream_t st);
 float opt_next_stepsz(pvdb_opt_s* o);
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st);
+               cudaStream_t st, const float* tv);
 pvdb_grid_s* opt_params(pvdb_opt_s* o);
 pvdb_grid_s* opt_moment(pvdb_opt_s* o, int which);
 float opt_lr_scale(pvdb_opt_s* o, float factor);
@@ -322,35 +322,54 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
     rc = march_backward_keys(m, m->t_grad_w, m->t_grad_last, true, st);
     if (rc) return rc;
   }
-  // the cell counts are reset beside TV / Adam (stage profiling: in sequence)
+  // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays)).
+  // Sparse TV adds its terms only to voxels with a nonzero gradient, and the
+  // terms depend on the values alone: they are computed beside the gradient
+  // sums (for the touched leaves' voxels) and the voxel Adam adds them to the
+  // channels with a gradient. Dense TV (every voxel) keeps the in-place pass.
+  const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
+  const float w_k = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
+  const float w_d = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
+  const bool defer = !cfg->tv_dense_mode && !cfg->tv_in_place;
+  const bool defer_k = defer && cfg->tv_weight_k0 > 0.f && !kg->all_touched;
+  const bool defer_d = defer && cfg->tv_weight_density > 0.f && !dg->all_touched;
+  if (defer_k || defer_d) {
+    // the touched leaves (flagged by the grouping) for the terms and for Adam
+    if (defer_d && (rc = touched_list(dg, st))) return rc;
+    if (defer_k && (rc = touched_list(kg, st))) return rc;
+    if ((rc = fork_side(m, st, 1))) return rc;
+    if (defer_k && (rc = tv_terms_launch(kg, w_k, w_k, w_k, m->side[0]))) return rc;
+    if (defer_d && (rc = tv_terms_launch(dg, w_d, w_d, w_d, m->side[0]))) return rc;
+  }
+  // the cell counts are reset beside Adam (stage profiling: in sequence)
   rc = march_backward_reduce(m, m->t_grad_k0, st, t.prof);
   if (rc) return rc;
-  // TV (dvgo.py:245-251: w = weight * max(world_size) / 128; run.py:580 divides by len(rays))
-  // TV of the two grids side by side (each grid's own touched list), then the
-  // three Adam updates side by side; the rgbnet Adam needs only the rgbnet
-  // gradients, complete since the MLP backward
-  const int wsmax = std::max(dg->reso[0], std::max(dg->reso[1], dg->reso[2]));
+  if ((defer_k || defer_d) && (rc = join_side(m, st, 1))) return rc;
+  // TV in place where it is not deferred (the two grids side by side, each
+  // with its own touched list), then the three Adam updates side by side; the
+  // rgbnet Adam needs only the rgbnet gradients, complete since the MLP
+  // backward
   if ((rc = fork_side(m, st, 2))) return rc;
   if (!t.prof && (rc = march_backward_clear(m, m->side[1]))) return rc;
   rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
                          t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0,
                          m->side[1], t.ss_dev ? t.ss_dev + 2 : nullptr);
   if (rc) return rc;
-  if (cfg->tv_weight_k0 > 0.f) {
-    const float w = cfg->tv_weight_k0 / float(n_rays) * float(wsmax) / 128.f;
-    rc = pvdb_grid_tv_add_grad(kg, w, w, w, cfg->tv_dense_mode, 0,
+  if (cfg->tv_weight_k0 > 0.f && !defer_k) {
+    rc = pvdb_grid_tv_add_grad(kg, w_k, w_k, w_k, cfg->tv_dense_mode, 0,
                                reinterpret_cast<pvdb_stream>(m->side[0]));
     if (rc) return rc;
   }
-  rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, m->side[0]);
+  rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, m->side[0],
+                  defer_k ? kg->d_tv : nullptr);
   if (rc) return rc;
-  if (cfg->tv_weight_density > 0.f) {
-    const float w = cfg->tv_weight_density / float(n_rays) * float(wsmax) / 128.f;
-    rc = pvdb_grid_tv_add_grad(dg, w, w, w, cfg->tv_dense_mode, 0, s);
+  if (cfg->tv_weight_density > 0.f && !defer_d) {
+    rc = pvdb_grid_tv_add_grad(dg, w_d, w_d, w_d, cfg->tv_dense_mode, 0, s);
     if (rc) return rc;
   }
   if (t.prof) prof_mark(st, 9);
-  rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st);
+  rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st,
+                  defer_d ? dg->d_tv : nullptr);
   if (rc) return rc;
   if ((rc = join_side(m, st, 2))) return rc;
   if (t.prof) {
@@ -386,6 +405,8 @@ static void grid_key(std::vector<uint8_t>& k, const pvdb_grid_s* g) {
   key_put(k, g->bmax_valid);
   key_put(k, g->d_half);
   key_put(k, g->half_valid);
+  key_put(k, g->d_tv);
+  key_put(k, g->all_touched);
 }
 
 // Everything a captured step has baked in: sizes, configuration, and the

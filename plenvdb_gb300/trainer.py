@@ -46,6 +46,7 @@ class FineStageConfig:
     precision: int = 0              # 0 FP32 SIMT rgbnet, 1 BF16 tensor cores
     use_graph: bool = True          # replay the fused step as a captured CUDA graph
     leaf_staging: bool = False      # density leaves staged in shared memory by bulk copies
+    tv_in_place: bool = False       # sparse TV added to the gradient before Adam, not deferred
 
     @property
     def voxel_size(self) -> float:
@@ -100,6 +101,7 @@ class FineStageTrainer:
         # bytes per k0 feature the BF16 step gathers (its 12-channel BF16 shadow)
         self.k0_feature_bytes = 2 if (cfg.precision == 1 and self.c0 == 12) else 4
         self.tc.use_graph = int(cfg.use_graph)
+        self.tc.tv_in_place = int(cfg.tv_in_place)
         self.loss = torch.zeros(1, device="cuda")
         # gradients start clean
         density.zero_grad()

@@ -545,10 +545,15 @@ def run_density_only(scfg, cfg, dev, args, flush):
 #   cell_grouping   32 B per kept sample (key read twice, rank written and read,
 #                   cell offset read, grouped key and index written)
 #   voxel_gather    64 B record + 8 corner gradients (1 + C floats) per kept sample
-#   tv              12 B per visited voxel-channel (value read, gradient read
-#                   and written; the six neighbour reads are cache hits)
-#   voxel_adam      28 B per visited voxel-channel (p, g, m, v read; p, m, v
-#                   written); visited = every voxel of the touched leaves
+#   tv              8 B per visited voxel-channel: the sparse TV terms (value
+#                   read, term written; the six neighbour reads are cache hits);
+#                   visited = the active voxels of the touched leaves
+#   voxel_adam      4 B per visited voxel-channel (gradient read) + 32 B per
+#                   updated voxel-channel (TV term, p, m, v read; p, m, v
+#                   written; gradient zeroed) + 32 B per updated k0 voxel (its
+#                   BF16 feature record); updated = a nonzero gradient. The
+#                   visited and updated counts come from the Adam kernels of
+#                   the profiled step (pvdb_march_adam_counts)
 RGBNET_FWD_ROW, RGBNET_FWD_RAY, RGBNET_BWD_ROW = 36608.0, 6912.0, 73216.0
 # DRAM bytes (read + write) per launch of each stage's kernels at this workload,
 # from the ncu captures summarised in profiles/*_bf16_160cube_8192rays.md
@@ -572,12 +577,22 @@ def touched_leaves(grid):
     return int(n.value)
 
 
+def adam_counts(ws):
+    """Voxels visited and updated by the density and k0 Adam of the last
+    profiled step: (density visited, density updated, k0 visited, k0 updated)."""
+    import ctypes
+    from plenvdb_gb300 import _lib as L
+    out = (ctypes.c_int64 * 4)()
+    L.call("pvdb_march_adam_counts", ws.h, out, L.stream_of())
+    return [int(v) for v in out]
+
+
 def stage_work(tr, R):
     """(bound, algorithmic units per launch) of each stage for the last step."""
     kept, rows, evaluated = tr.ws.stats()
     C = 12
     feat = getattr(tr, "k0_feature_bytes", 4)  # bytes per gathered k0 feature
-    vox = touched_leaves(tr.density) * 512 + touched_leaves(tr.k0) * 512 * C
+    dvis, dupd, kvis, kupd = adam_counts(tr.ws)
     return {
         "march_fwd": ("hbm", evaluated * 36.0),
         "k0_gather": ("hbm", rows * (8 * C * feat + 16.0)),
@@ -586,8 +601,8 @@ def stage_work(tr, R):
         "march_bwd": ("hbm", kept * 120.0),
         "cell_grouping": ("hbm", kept * 32.0),
         "voxel_gather": ("hbm", kept * (64.0 + 8 * (1 + C) * 4.0)),
-        "tv": ("hbm", vox * 12.0),
-        "voxel_adam": ("hbm", vox * 28.0),
+        "tv": ("hbm", (dvis + kvis * C) * 8.0),
+        "voxel_adam": ("hbm", (dvis + kvis * C) * 4.0 + (dupd + kupd * C) * 32.0 + kupd * 32.0),
     }, (kept, rows, evaluated)
 
 
@@ -625,6 +640,8 @@ def roofline(stage_ms, tr, scfg, R=RAYS):
            "traffic_source": f"ncu capture, profiles/ (stage {name})" if R == RAYS else None,
            "peak_source": src, "avg_ms": stage_ms[name],
            "kept_samples": kept, "color_rows": rows, "evaluated_samples": evaluated,
+           "adam_voxels": dict(zip(["density_visited", "density_updated", "k0_visited",
+                                    "k0_updated"], adam_counts(tr.ws))),
            "stages": table}
     return out
 

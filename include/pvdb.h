@@ -76,8 +76,9 @@ int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first);
  * and writes, for each mark i < n_marks, the total milliseconds between the
  * previous recorded mark and mark i, summed over the calls. Train-step marks:
  * 1 march forward, 2 k0 gather, 3 rgbnet forward, 4 composite + loss,
- * 5 rgbnet backward, 6 march backward (keys), 7 radix sort, 8 segmented
- * reduce, 9 TV, 10 voxel Adam, 11 rgbnet Adam. Renderer marks: 1 count march,
+ * 5 rgbnet backward, 6 march backward (keys), 7 grouping by cell, 8 per-voxel
+ * sums, 9 TV, 10 voxel Adam, 11 rgbnet Adam (a profiled step runs these in
+ * sequence on its stream). Renderer marks: 1 count march,
  * 2 scan, 3 fill march, 4 rgbnet, 5 composite. */
 int pvdb_profile_begin(int32_t max_steps);
 /* Number of kernels the library has launched so far (all threads). */
@@ -385,6 +386,13 @@ int pvdb_march_totals(pvdb_march m, int64_t* total_kept, int64_t* total_rows, pv
  * materialises these as tensor sizes. */
 int pvdb_march_stats(pvdb_march m, int64_t* kept, int64_t* rows, int64_t* evaluated,
                      pvdb_stream s);
+/* Voxel counts of the last pvdb_train_step run under the stage profiler
+ * (synchronises s): out[4] = {density voxels visited, density voxels updated,
+ * k0 voxels visited, k0 voxels updated} by the voxel Adam (visited: the
+ * active voxels of the touched leaves; updated: those with a nonzero
+ * gradient). Zeros until a profiled step ran. No reference counterpart: it
+ * feeds the byte model of the TV and Adam stages. */
+int pvdb_march_adam_counts(pvdb_march m, int64_t* out, pvdb_stream s);
 
 /* Backward. grad_weight [M] (per colour row), grad_last [R], grad_k0 [M, C] (may
  * be NULL when k0 is NULL or gets no gradient). Adds into density->grad and

@@ -141,6 +141,7 @@ _SIGS = {
     "pvdb_march_views": (C.c_int, [vp, C.POINTER(MarchViews)]),
     "pvdb_march_totals": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), vp]),
     "pvdb_march_stats": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), vp]),
+    "pvdb_march_adam_counts": (C.c_int, [vp, C.POINTER(i64), vp]),
     "pvdb_march_backward": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "pvdb_composite_forward": (C.c_int, [vp, vp, f32, vp, i32, vp]),
     "pvdb_composite_backward": (C.c_int, [vp, vp, vp, f32, vp, vp, vp, i32, vp]),

@@ -663,7 +663,9 @@ __global__ void __launch_bounds__(kMarchThreads)
 //   k_cell_heads   per cell: sorts its segment by sample index (so the
 //                  placement equals a stable sort by key: each cell's samples
 //                  contiguous, in ascending sample order), and flags the leaves
-//                  holding the cell's corners as touched.
+//                  holding the cell's corners as touched;
+//   k_group_records per grouped sample (once the rows' k0 gradients exist):
+//                  its record and its row's k0 gradient, in grouped order.
 // Then one thread per voxel of the touched leaves computes
 //   grad += sum over c' = 0..7, in that order, of
 //           (sum over the samples of cell v - delta(c'), in sample order,
@@ -796,17 +798,17 @@ __device__ __forceinline__ void sort8(uint32_t v[8]) {
 }
 
 // Thread per placed index; cell heads sort their segment (by sample index),
-// lay the segment's gradient records out in that order (rec_s, row_s: the
-// per-voxel sums then read each cell's records contiguously, without the
-// sample-index indirection), and flag the leaves of the cell's corners as
+// lay the segment's gradient records out in that order when rec_s is given
+// (the density-only backward: the per-voxel sums then read each cell's
+// records contiguously; with k0 rows, k_group_records does this once the
+// rows' gradients exist), and flag the leaves of the cell's corners as
 // touched in the density grid and (touched_c != NULL) the k0 grid (k0_same:
 // the k0 grid has the density topology, so the density grid's corner slots
 // serve both).
 __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
                              const uint32_t* __restrict__ cnt, uint32_t* svals, GridView gd,
                              GridView gc, uint8_t* touched_d, uint8_t* touched_c, int k0_same,
-                             const float4* __restrict__ rec, const int32_t* __restrict__ brow,
-                             float4* rec_s, int32_t* row_s) {
+                             const float4* __restrict__ rec, float4* rec_s) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -822,16 +824,12 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
       for (uint32_t t = 0; t < 8; ++t)
         if (t < len) {
           svals[i + t] = v[t];
-          rec_s[i + t] = rec[v[t]];
-          row_s[i + t] = brow[v[t]];
+          if (rec_s) rec_s[i + t] = rec[v[t]];
         }
     } else {
       sort_segment(svals + i, len);
-      for (uint32_t t = 0; t < len; ++t) {
-        const uint32_t sv = svals[i + t];
-        rec_s[i + t] = rec[sv];
-        row_s[i + t] = brow[sv];
-      }
+      if (rec_s)
+        for (uint32_t t = 0; t < len; ++t) rec_s[i + t] = rec[svals[i + t]];
     }
     const int off = int(key & 511u);
     const int al = __ldg(gd.table + (key >> 9));  // the cell's own leaf, if allocated
@@ -885,9 +883,6 @@ __device__ __forceinline__ float corner_scale(float u, float v, float w, int c) 
   return __fmul_rn(__fmul_rn(a, b), cc);
 }
 
-// Thread per voxel of the listed (touched) leaves of grid g; adds the density
-// sum to grad_d and/or the k0 sums to grad_c (C channels). NQ = the number of
-// float4 chunks of the k0 gradient (0 = density only).
 // A kept sample's k0-gradient row (NQ float4), zero when it has none.
 template <int NQ>
 __device__ __forceinline__ void gather_row(const float* __restrict__ gk0, int32_t row, int C,
@@ -910,16 +905,45 @@ __device__ __forceinline__ void gather_row(const float* __restrict__ gk0, int32_
   }
 }
 
+// Thread per grouped index j: the grouped record of sample svals[j] — its
+// gradient record (index-space position, dL/dsigma) followed by its colour
+// row's k0 gradient (NQ float4; zeros when the sample has no colour row) —
+// as 1 + NQ consecutive float4. The per-voxel sums then read a cell's
+// samples as one contiguous run, without the dependent row lookup (the rows
+// are in ray order, the cells in key order). Runs once the rgbnet backward
+// has written the rows' gradients.
+template <int NQ>
+__global__ void __launch_bounds__(256)
+    k_group_records(const uint32_t* __restrict__ svals, const uint32_t* n_dev,
+                    const float4* __restrict__ rec, const int32_t* __restrict__ brow,
+                    const float* __restrict__ gk0, int C, int vec, float4* rec_g) {
+  constexpr int NB = NQ > 0 ? NQ : 1;
+  const int64_t n = *n_dev;
+  for (int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; j < n;
+       j += int64_t(gridDim.x) * blockDim.x) {
+    const uint32_t sv = __ldg(svals + j);
+    const float4 p = __ldg(rec + sv);
+    float4 q[NB];
+    if (NQ) gather_row<NQ>(gk0, __ldg(brow + sv), C, vec, q);
+    float4* dst = rec_g + j * (1 + NQ);
+    dst[0] = p;
+#pragma unroll
+    for (int b = 0; b < NQ; ++b) dst[1 + b] = q[b];
+  }
+}
+
 // Adds one sample's contribution to corner c of its cell: the density term
 // (when the grid takes one and the sample's dL/dsigma is nonzero) and the
-// k0 row scaled by the corner weight (when the sample has a colour row).
+// k0 row scaled by the corner weight (want_c; a sample without a colour row
+// carries a zero row, whose products leave the sums' bits unchanged: they
+// start at +0 and adding a signed zero to a value other than -0 returns it).
 template <int NQ>
-__device__ __forceinline__ void gather_add(const float4 p, const float4* q, bool has_row,
+__device__ __forceinline__ void gather_add(const float4 p, const float4* q, bool want_c,
                                            bool want_d, int c, float& pd, float4* pk) {
   const float u = p.x - float(ifloor(p.x)), v = p.y - float(ifloor(p.y)),
               w = p.z - float(ifloor(p.z));
   if (want_d && p.w != 0.f) pd = __fadd_rn(pd, density_corner_term(p.w, u, v, w, c));
-  if (has_row) {
+  if (want_c) {
     const float sce = corner_scale(u, v, w, c);
 #pragma unroll
     for (int b = 0; b < NQ; ++b) {
@@ -931,13 +955,14 @@ __device__ __forceinline__ void gather_add(const float4 p, const float4* q, bool
   }
 }
 
+// Thread per voxel of the listed (touched) leaves of grid g; adds the density
+// sum to grad_d and/or the k0 sums to grad_c (C channels). NQ = the number of
+// float4 chunks of the k0 gradient in a grouped record (0 = density only).
 template <int NQ>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                    const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
-                   const float4* __restrict__ rec_s, const int32_t* __restrict__ row_s,
-                   const float* __restrict__ gk0, int gk0_vec, float* grad_d, float* grad_c,
-                   int C) {
+                   const float4* __restrict__ rec_g, float* grad_d, float* grad_c, int C) {
   constexpr int NB = NQ > 0 ? NQ : 1;
   const int64_t nv = int64_t(*count) * kLeafVox;
   const bool want_d = grad_d != nullptr, want_c = NQ && grad_c;
@@ -977,11 +1002,14 @@ __global__ void __launch_bounds__(256)
       for (int b = 0; b < NB; ++b) pk[b] = make_float4(0.f, 0.f, 0.f, 0.f);
       const uint32_t h = __ldg(off + key[c]);
       for (uint32_t j = h; j < h + len[c]; ++j) {
-        const float4 p0 = rec_s[j];
-        const int32_t r0 = want_c ? row_s[j] : -1;
+        const float4* r = rec_g + int64_t(j) * (1 + NQ);
+        const float4 p0 = __ldg(r);
         float4 q0[NB];
-        gather_row<NQ>(gk0, r0, C, gk0_vec, q0);
-        gather_add<NQ>(p0, q0, r0 >= 0, want_d, c, pd, pk);
+        if (want_c) {
+#pragma unroll
+          for (int b = 0; b < NQ; ++b) q0[b] = __ldg(r + 1 + b);
+        }
+        gather_add<NQ>(p0, q0, want_c, want_d, c, pd, pk);
       }
       sum_d = __fadd_rn(sum_d, pd);
 #pragma unroll
@@ -1018,18 +1046,25 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
   const bool same = NQ && k0->h_table == density->h_table;
   const int C = NQ ? k0->C : 0;
   const int vec = NQ && C % 4 == 0 && (reinterpret_cast<uintptr_t>(grad_k0) & 15u) == 0;
-  // the kept samples' records in grouped order (k_cell_heads)
-  const float4* rec_s = m->b_rec_s;
-  const int32_t* row_s = reinterpret_cast<const int32_t*>(m->red.vals[1]);
+  if (m->bwd_with_k0) {
+    // the grouped records with their rows' k0 gradients (k_cell_heads wrote
+    // the density-only records already when the keys ran without k0)
+    PVDB_REQUIRE(m->b_rec_s_cap >= size_t(m->slots) * 16 * (1 + NQ),
+                 "march backward: grouped-record buffer too small");
+    const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(grid)));
+    k_group_records<NQ><<<sgrid, 256, 0, st>>>(m->red.vals[0], m->w.totals + 5, m->w.b_rec,
+                                               m->w.b_row, grad_k0, C, vec, m->b_rec_s);
+    PVDB_CHECK_LAUNCH("k_group_records");
+  }
+  const float4* rec_g = m->b_rec_s;
   k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_cnt,
-                                           m->cell_off, rec_s, row_s, grad_k0, vec,
-                                           density->d_grad, same ? k0->d_grad : nullptr, C);
+                                           m->cell_off, rec_g, density->d_grad,
+                                           same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
     k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
-                                             m->cell_off, rec_s, row_s, grad_k0, vec, nullptr,
-                                             k0->d_grad, C);
+                                             m->cell_off, rec_g, nullptr, k0->d_grad, C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -1238,7 +1273,8 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   }
   if ((rc = dev_reserve((void**)&m->w.b_rec, &m->b_rec_cap, size_t(nmax) * 16)) ||
       (rc = dev_reserve((void**)&m->w.b_row, &m->b_row_cap, size_t(nmax) * 4)) ||
-      (rc = dev_reserve((void**)&m->b_rec_s, &m->b_rec_s_cap, size_t(nmax) * 16)))
+      (rc = dev_reserve((void**)&m->b_rec_s, &m->b_rec_s_cap,
+                        size_t(nmax) * 16 * (1 + (k0 ? (k0->C + 3) / 4 : 0)))))
     return rc;
   const int nb = ceil_div(R, kMarchWarps);
   // the kept samples' keys, with their per-cell ranks and the per-cell and
@@ -1263,13 +1299,10 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   PVDB_CHECK_LAUNCH("k_cell_place");
   const GridView gv = density->view();
   const GridView kv = k0 ? k0->view() : gv;
-  // (the ranks are dead after the placement: their buffer takes the
-  // grouped-order colour rows)
   k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals, gv, kv,
                                               density->d_touched, k0 ? k0->d_touched : nullptr,
                                               k0 && k0->h_table == density->h_table ? 1 : 0,
-                                              m->w.b_rec, m->w.b_row, m->b_rec_s,
-                                              reinterpret_cast<int32_t*>(rank));
+                                              m->w.b_rec, k0 ? nullptr : m->b_rec_s);
   PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;
   if (k0) k0->tlist_valid = false;
@@ -1492,6 +1525,17 @@ int pvdb_march_stats(pvdb_march m, int64_t* kept, int64_t* rows, int64_t* evalua
   if (kept) *kept = t[0];
   if (rows) *rows = t[1];
   if (evaluated) *evaluated = t[4];
+  return PVDB_OK;
+}
+
+int pvdb_march_adam_counts(pvdb_march m, int64_t* out, pvdb_stream s) {
+  clear_error();
+  PVDB_REQUIRE(m && out, "null argument");
+  uint32_t t[4];
+  cudaStream_t st = as_stream(s);
+  PVDB_CHECK_CUDA(cudaMemcpyAsync(t, m->w.totals + 8, 16, cudaMemcpyDeviceToHost, st));
+  PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < 4; ++i) out[i] = t[i];
   return PVDB_OK;
 }
 

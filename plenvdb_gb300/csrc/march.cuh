@@ -54,7 +54,9 @@ struct MarchW {
   // leaf-staging test hook, [3] error flags (1 samples_cap exceeded,
   // 2 tensor-core wait, 4 ray-offset look-back wait, 8 leaf-staging copy
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
-  // [6] k_march_chain ray counter, [7] train-step loss block counter
+  // [6] k_march_chain ray counter, [7] train-step loss block counter,
+  // [8..11] voxels visited / updated by the density and k0 Adam of the last
+  // profiled train step
   uint32_t* totals;
 };
 
@@ -75,7 +77,9 @@ struct pvdb_march_s {
   uint32_t* leaf_off = nullptr;
   size_t cell_cap = 0;  // cells
   size_t b_rec_cap = 0;         // bytes of w.b_rec
-  float4* b_rec_s = nullptr;    // w.b_rec in grouped (cell, sample) order
+  // grouped (cell, sample) order records: w.b_rec, followed (backward with
+  // k0) by the sample's k0-row gradient, 1 + ceil(C/4) float4 per sample
+  float4* b_rec_s = nullptr;
   size_t b_rec_s_cap = 0;
   size_t b_row_cap = 0;         // bytes of w.b_row
   bool bwd_keys_ready = false;  // march_backward_keys ran since the last reduce

@@ -75,6 +75,17 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
   }
 }
 
+// Adds a thread's two counts to counts[0..1], one atomic per warp (every lane
+// of the warp calls it).
+__device__ __forceinline__ void count_add(uint32_t* counts, uint32_t a, uint32_t b) {
+  a = __reduce_add_sync(0xffffffffu, a);
+  b = __reduce_add_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(counts, a);
+    atomicAdd(counts + 1, b);
+  }
+}
+
 // The same update for scalar grids (density), one thread per voxel. A warp's
 // 32 voxels are 32 consecutive offsets of one leaf (one x, four y, all z), so
 // the brick bounds their growing values raise (bmax_raise) span at most
@@ -90,10 +101,11 @@ __global__ void __launch_bounds__(256)
                 const float* __restrict__ perlr, float stepsz, const float* __restrict__ stepsz_dev,
                 float eps, float b0, float b1, int mode, int zero_after,
                 const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
-                const float* __restrict__ tv) {
+                const float* __restrict__ tv, uint32_t* counts) {
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   const int lane = threadIdx.x & 31;
+  uint32_t n_act = 0, n_upd = 0;
   // whole leaves and whole warps: every lane of a warp takes the same trips
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -105,7 +117,9 @@ __global__ void __launch_bounds__(256)
     if (tv && gr != 0.f) gr = gr + tv[slot];  // deferred sparse TV
     bool grew = false;
     float nv = 0.f;
+    n_act += active;
     if (active && !(mode == 1 && gr == 0.f)) {
+      ++n_upd;
       const float lrf = mode == 2 ? perlr[slot] : 1.f;
       const float mn = b0 * m[slot] + (1 - b0) * gr;
       const float vn = b1 * v[slot] + (1 - b1) * gr * gr;
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(256)
       atomicMax(g.bmax + (int64_t(bx) * g.bdim[1] + by) * g.bdim[2] + bz, kmax);
     }
   }
+  if (counts) count_add(counts, n_act, n_upd);
 }
 
 // The same update for 12-channel grids (k0), one thread per voxel with the
@@ -151,14 +166,16 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
                                const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
                                int mode, int zero_after, const int32_t* __restrict__ list,
                                const uint32_t* __restrict__ count, __nv_bfloat16* half,
-                               const float* __restrict__ tv) {
+                               const float* __restrict__ tv, uint32_t* counts) {
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
+  uint32_t n_act = 0, n_upd = 0;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
     const int leaf = list ? list[i >> 9] : int(i >> 9);
     const int vox = int(i & 511);
     if (!((__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull)) continue;
+    ++n_act;
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
     float4* g4 = reinterpret_cast<float4*>(g.grad + slot * 12);
     float gr[12];
@@ -168,6 +185,12 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
       gr[4 * b] = x.x; gr[4 * b + 1] = x.y; gr[4 * b + 2] = x.z; gr[4 * b + 3] = x.w;
     }
     if (tv) {  // deferred sparse TV: its terms join the channels with a gradient
+      // (tv is given in mode 1 only: a voxel without a gradient is skipped
+      // below whatever its terms, so they are not read)
+      bool nz = false;
+#pragma unroll
+      for (int ch = 0; ch < 12; ++ch) nz = nz || gr[ch] != 0.f;
+      if (!nz) continue;
       const float4* t4 = reinterpret_cast<const float4*>(tv + slot * 12);
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
@@ -186,6 +209,7 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
       any = any || live[q];
     }
     if (!any) continue;
+    ++n_upd;
     float4* m4 = reinterpret_cast<float4*>(m + slot * 12);
     float4* v4 = reinterpret_cast<float4*>(v + slot * 12);
     float4* d4 = reinterpret_cast<float4*>(g.data + slot * 12);
@@ -222,6 +246,7 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
       h4[1] = make_uint4(tc::pack_bf16(dd[8], dd[9]), tc::pack_bf16(dd[10], dd[11]), 0u, 0u);
     }
   }
+  if (counts) count_add(counts, n_act, n_upd);
 }
 
 // zero_after for voxels the Adam pass skipped (mode 1, all-zero gradient):
@@ -270,7 +295,7 @@ int adam_dense_launch(float* param, const float* grad, float* m, float* v, const
 }
 
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st, const float* tv = nullptr);
+               cudaStream_t st, const float* tv = nullptr, uint32_t* counts = nullptr);
 
 // Advances the step counter and returns this step's Adam step size.
 float opt_next_stepsz(pvdb_opt_s* o) {
@@ -287,8 +312,11 @@ int opt_step_launch(pvdb_opt_s* o, int mode, int zero_after, cudaStream_t st) {
 // *stepsz_dev when that is given (a captured graph reads it each replay).
 // tv (optional): TV terms of the touched leaves' voxels (tv_terms_launch),
 // added to the channels with a nonzero gradient before the update.
+// counts (optional, 1- and 12-channel grids): two words that get the number
+// of active voxels visited and of voxels updated (the stage profiler's byte
+// model).
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st, const float* tv) {
+               cudaStream_t st, const float* tv, uint32_t* counts) {
   pvdb_grid_s* g = o->params;
   // mode 1 skips voxels whose gradient is zero: only the touched leaves matter
   const bool use_list = mode == 1 && !g->all_touched;
@@ -303,12 +331,13 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
           o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half,
-          tv);
+          tv, counts);
     else if (g->C == 1)
       k_vdb_adam1<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
           mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv);
+          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv,
+          counts);
     else
       k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
           g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,

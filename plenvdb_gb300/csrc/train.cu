@@ -39,7 +39,7 @@ int march_backward_reduce(pvdb_march_s* m, const float* grad_k0, cudaStream_t st
 int march_backward_clear(pvdb_march_s* m, cudaStream_t st);
 float opt_next_stepsz(pvdb_opt_s* o);
 int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const float* stepsz_dev,
-               cudaStream_t st, const float* tv);
+               cudaStream_t st, const float* tv, uint32_t* counts);
 pvdb_grid_s* opt_params(pvdb_opt_s* o);
 pvdb_grid_s* opt_moment(pvdb_opt_s* o, int which);
 float opt_lr_scale(pvdb_opt_s* o, float factor);
@@ -337,12 +337,40 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
     // the touched leaves (flagged by the grouping) for the terms and for Adam
     if (defer_d && (rc = touched_list(dg, st))) return rc;
     if (defer_k && (rc = touched_list(kg, st))) return rc;
-    if ((rc = fork_side(m, st, 1))) return rc;
-    if (defer_k && (rc = tv_terms_launch(kg, w_k, w_k, w_k, m->side[0]))) return rc;
-    if (defer_d && (rc = tv_terms_launch(dg, w_d, w_d, w_d, m->side[0]))) return rc;
   }
-  // the cell counts are reset beside Adam (stage profiling: in sequence)
-  rc = march_backward_reduce(m, m->t_grad_k0, st, t.prof);
+  if (t.prof) {
+    // stage profiler: every stage in sequence on the launching stream, with
+    // a mark between the per-voxel sums, the TV terms and the Adam updates
+    if ((rc = march_backward_reduce(m, m->t_grad_k0, st, true))) return rc;
+    if (defer_k && (rc = tv_terms_launch(kg, w_k, w_k, w_k, st))) return rc;
+    if (defer_d && (rc = tv_terms_launch(dg, w_d, w_d, w_d, st))) return rc;
+    if (cfg->tv_weight_k0 > 0.f && !defer_k &&
+        (rc = pvdb_grid_tv_add_grad(kg, w_k, w_k, w_k, cfg->tv_dense_mode, 0, s)))
+      return rc;
+    if (cfg->tv_weight_density > 0.f && !defer_d &&
+        (rc = pvdb_grid_tv_add_grad(dg, w_d, w_d, w_d, cfg->tv_dense_mode, 0, s)))
+      return rc;
+    prof_mark(st, 9);
+    // the Adam updates count the voxels they visit and update (totals[8..11])
+    PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals + 8, 0, 16, st));
+    if ((rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, st,
+                         defer_k ? kg->d_tv : nullptr, m->w.totals + 10)) ||
+        (rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st,
+                         defer_d ? dg->d_tv : nullptr, m->w.totals + 8)))
+      return rc;
+    prof_mark(st, 10);
+    rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
+                           t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0, st,
+                           t.ss_dev ? t.ss_dev + 2 : nullptr);
+    if (rc) return rc;
+    prof_mark(st, 11);
+    return PVDB_OK;
+  }
+  if ((defer_k || defer_d) && (rc = fork_side(m, st, 1))) return rc;
+  if (defer_k && (rc = tv_terms_launch(kg, w_k, w_k, w_k, m->side[0]))) return rc;
+  if (defer_d && (rc = tv_terms_launch(dg, w_d, w_d, w_d, m->side[0]))) return rc;
+  // the cell counts are reset beside Adam
+  rc = march_backward_reduce(m, m->t_grad_k0, st, false);
   if (rc) return rc;
   if ((defer_k || defer_d) && (rc = join_side(m, st, 1))) return rc;
   // TV in place where it is not deferred (the two grids side by side, each
@@ -350,7 +378,7 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   // rgbnet Adam needs only the rgbnet gradients, complete since the MLP
   // backward
   if ((rc = fork_side(m, st, 2))) return rc;
-  if (!t.prof && (rc = march_backward_clear(m, m->side[1]))) return rc;
+  if ((rc = march_backward_clear(m, m->side[1]))) return rc;
   rc = adam_dense_launch(net->params, net->grads, net->exp_avg, net->exp_avg_sq, nullptr, P,
                          t.ss[2], cfg->rgbnet_beta1, cfg->rgbnet_beta2, cfg->rgbnet_eps, 0,
                          m->side[1], t.ss_dev ? t.ss_dev + 2 : nullptr);
@@ -361,21 +389,16 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
     if (rc) return rc;
   }
   rc = opt_launch(t.kopt, 1, 1, t.ss[1], t.ss_dev ? t.ss_dev + 1 : nullptr, m->side[0],
-                  defer_k ? kg->d_tv : nullptr);
+                  defer_k ? kg->d_tv : nullptr, nullptr);
   if (rc) return rc;
   if (cfg->tv_weight_density > 0.f && !defer_d) {
     rc = pvdb_grid_tv_add_grad(dg, w_d, w_d, w_d, cfg->tv_dense_mode, 0, s);
     if (rc) return rc;
   }
-  if (t.prof) prof_mark(st, 9);
   rc = opt_launch(t.dopt, 1, 1, t.ss[0], t.ss_dev ? t.ss_dev + 0 : nullptr, st,
-                  defer_d ? dg->d_tv : nullptr);
+                  defer_d ? dg->d_tv : nullptr, nullptr);
   if (rc) return rc;
   if ((rc = join_side(m, st, 2))) return rc;
-  if (t.prof) {
-    prof_mark(st, 10);
-    prof_mark(st, 11);
-  }
   return PVDB_OK;
 }
 

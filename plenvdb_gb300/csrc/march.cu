@@ -658,12 +658,12 @@ __global__ void __launch_bounds__(kMarchThreads)
 //                  particular order) and the counts per cell and per leaf;
 //   leaf scan      exclusive scan of the per-leaf counts (one block);
 //   k_cell_offsets per leaf with samples: exclusive scan of its 512 cell
-//                  counts, offset by the leaf's start;
+//                  counts, offset by the leaf's start; flags the leaves
+//                  holding corners of its cells with samples as touched;
 //   k_cell_place   per sample: position = cell offset + rank;
 //   k_cell_heads   per cell: sorts its segment by sample index (so the
 //                  placement equals a stable sort by key: each cell's samples
-//                  contiguous, in ascending sample order), and flags the leaves
-//                  holding the cell's corners as touched;
+//                  contiguous, in ascending sample order);
 //   k_group_records per grouped sample (once the rows' k0 gradients exist):
 //                  its record and its row's k0 gradient, in grouped order.
 // Then one thread per voxel of the touched leaves computes
@@ -673,30 +673,18 @@ __global__ void __launch_bounds__(kMarchThreads)
 // Every sum has an order fixed by the data, so the result is bitwise
 // reproducible without atomics on floats. Corners in no allocated leaf are
 // dropped (densityvdb.cu:23).
-__device__ __forceinline__ void cell_decode(const int ld[3], uint32_t key, int& i, int& j, int& k) {
-  const int leaf = int(key >> 9), off = int(key & 511u);
-  const int lk = leaf % ld[2];
-  const int lj = (leaf / ld[2]) % ld[1];
-  const int li = leaf / (ld[2] * ld[1]);
-  i = (li << 3) | (off >> 6);
-  j = (lj << 3) | ((off >> 3) & 7);
-  k = (lk << 3) | (off & 7);
-}
-
-__device__ __forceinline__ void mark_corner_leaves(const GridView& g, int ci, int cj, int ck,
-                                                   uint8_t* touched) {
-  int s[8];
-  corner_slots(g, ci, cj, ck, s);
-#pragma unroll
-  for (int c = 0; c < 8; ++c)
-    if (s[c] >= 0) touched[s[c] >> 9] = 1;
-}
 
 // Warp per dense leaf with samples: lane t scans cells 16t .. 16t+15 (four
-// 16-byte loads), the warp scans the lane totals.
+// 16-byte loads), the warp scans the lane totals. The warp also flags as
+// touched the allocated leaves that hold a corner of one of the leaf's cells
+// with samples: the leaf itself and, for cells on its +x / +y / +z faces,
+// the neighbour leaves those corners fall in — in the density grid gd and
+// (touched_c != NULL) the k0 grid gc (k0_same: gc has gd's leaves).
 __global__ void __launch_bounds__(256)
     k_cell_offsets(const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ leaf_cnt,
-                   const uint32_t* __restrict__ leaf_off, int64_t nleaves, uint32_t* off) {
+                   const uint32_t* __restrict__ leaf_off, int64_t nleaves, uint32_t* off,
+                   GridView gd, GridView gc, uint8_t* touched_d, uint8_t* touched_c,
+                   int k0_same) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
@@ -729,6 +717,33 @@ __global__ void __launch_bounds__(256)
         run += v[4 * b + e];
       }
       dst[b] = make_uint4(o4[0], o4[1], o4[2], o4[3]);
+    }
+    // bit (di, dj, dk) = 4 di + 2 dj + dk: some cell with samples has a
+    // corner in the leaf at that offset (cells of lane t: x = t / 4,
+    // y = 2 (t % 4) + q / 8, z = q % 8)
+    uint32_t dm = 0;
+    const bool fx = (lane >> 2) == 7;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      if (!v[q]) continue;
+      const bool fy = ((lane & 3) == 3) && q >= 8, fz = (q & 7) == 7;
+      dm |= 1u | (fz ? 2u : 0u) | (fy ? 4u : 0u) | (fy && fz ? 8u : 0u);
+      if (fx) dm |= 16u | (fz ? 32u : 0u) | (fy ? 64u : 0u) | (fy && fz ? 128u : 0u);
+    }
+    dm = __reduce_or_sync(0xffffffffu, dm);
+    if (lane < 8 && ((dm >> lane) & 1u)) {
+      const int lk = int(l % gd.ldim[2]), lj = int((l / gd.ldim[2]) % gd.ldim[1]),
+                li = int(l / (int64_t(gd.ldim[2]) * gd.ldim[1]));
+      const int ni = li + (lane >> 2), nj = lj + ((lane >> 1) & 1), nk = lk + (lane & 1);
+      const int al = leaf_of(gd, ni << 3, nj << 3, nk << 3);
+      if (al >= 0) {
+        touched_d[al] = 1;
+        if (touched_c && k0_same) touched_c[al] = 1;
+      }
+      if (touched_c && !k0_same) {
+        const int alc = leaf_of(gc, ni << 3, nj << 3, nk << 3);
+        if (alc >= 0) touched_c[alc] = 1;
+      }
     }
   }
 }
@@ -797,17 +812,13 @@ __device__ __forceinline__ void sort8(uint32_t v[8]) {
   }
 }
 
-// Thread per placed index; cell heads sort their segment (by sample index),
-// lay the segment's gradient records out in that order when rec_s is given
-// (the density-only backward: the per-voxel sums then read each cell's
-// records contiguously; with k0 rows, k_group_records does this once the
-// rows' gradients exist), and flag the leaves of the cell's corners as
-// touched in the density grid and (touched_c != NULL) the k0 grid (k0_same:
-// the k0 grid has the density topology, so the density grid's corner slots
-// serve both).
+// Thread per placed index; cell heads sort their segment (by sample index)
+// and lay the segment's gradient records out in that order when rec_s is
+// given (the density-only backward: the per-voxel sums then read each
+// cell's records contiguously; with k0 rows, k_group_records does this once
+// the rows' gradients exist).
 __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
-                             const uint32_t* __restrict__ cnt, uint32_t* svals, GridView gd,
-                             GridView gc, uint8_t* touched_d, uint8_t* touched_c, int k0_same,
+                             const uint32_t* __restrict__ cnt, uint32_t* svals,
                              const float4* __restrict__ rec, float4* rec_s) {
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
@@ -815,7 +826,9 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
     const uint32_t key = skeys[i];
     if (i > 0 && skeys[i - 1] == key) continue;
     const uint32_t len = cnt[key];
-    if (len <= 8) {
+    if (len == 1) {
+      if (rec_s) rec_s[i] = rec[svals[i]];
+    } else if (len <= 8) {
       uint32_t v[8];
 #pragma unroll
       for (uint32_t t = 0; t < 8; ++t) v[t] = t < len ? svals[i + t] : 0xFFFFFFFFu;
@@ -831,34 +844,6 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
       if (rec_s)
         for (uint32_t t = 0; t < len; ++t) rec_s[i + t] = rec[svals[i + t]];
     }
-    const int off = int(key & 511u);
-    const int al = __ldg(gd.table + (key >> 9));  // the cell's own leaf, if allocated
-    const bool interior = al >= 0 && (off >> 6) != 7 && ((off >> 3) & 7) != 7 && (off & 7) != 7;
-    if (interior) {
-      // all 8 corners lie in the cell's own leaf
-      touched_d[al] = 1;
-      if (touched_c && k0_same) touched_c[al] = 1;
-    }
-    if (interior && (!touched_c || k0_same)) continue;
-    int ci, cj, ck;
-    if (al >= 0) {
-      ci = __ldg(gd.origin + al * 3) + (off >> 6);
-      cj = __ldg(gd.origin + al * 3 + 1) + ((off >> 3) & 7);
-      ck = __ldg(gd.origin + al * 3 + 2) + (off & 7);
-    } else {
-      cell_decode(gd.ldim, key, ci, cj, ck);
-    }
-    if (!interior) {
-      int sl[8];
-      corner_slots(gd, ci, cj, ck, sl);
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (sl[c] >= 0) {
-          touched_d[sl[c] >> 9] = 1;
-          if (touched_c && k0_same) touched_c[sl[c] >> 9] = 1;
-        }
-    }
-    if (touched_c && !k0_same) mark_corner_leaves(gc, ci, cj, ck, touched_c);
   }
 }
 
@@ -1292,16 +1277,16 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   rc = scan_exclusive_u32(m->leaf_cnt, m->leaf_off, nleaves, m->w.totals + 5, &m->scan_partial,
                           &m->scan_partial_cap, st);
   if (rc) return rc;
+  const GridView gv = density->view();
+  const GridView kv = k0 ? k0->view() : gv;
   k_cell_offsets<<<int(std::min<int64_t>(ceil_div(nleaves, 8), int64_t(stride_grid()))), 256, 0,
-                   st>>>(m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off);
+                   st>>>(m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off, gv, kv,
+                         density->d_touched, k0 ? k0->d_touched : nullptr,
+                         k0 && k0->h_table == density->h_table ? 1 : 0);
   PVDB_CHECK_LAUNCH("k_cell_offsets");
   k_cell_place<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
   PVDB_CHECK_LAUNCH("k_cell_place");
-  const GridView gv = density->view();
-  const GridView kv = k0 ? k0->view() : gv;
-  k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals, gv, kv,
-                                              density->d_touched, k0 ? k0->d_touched : nullptr,
-                                              k0 && k0->h_table == density->h_table ? 1 : 0,
+  k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals,
                                               m->w.b_rec, k0 ? nullptr : m->b_rec_s);
   PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;

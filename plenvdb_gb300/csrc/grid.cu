@@ -71,6 +71,7 @@ int dev_reserve(void** p, size_t* cap, size_t bytes) {
 
 // ------------------------------------------------------------------ kernels
 __global__ void k_fill(float* p, int64_t n, float v) {
+  grid_dep_sync();
   int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i < n) p[i] = v;
 }
@@ -105,6 +106,7 @@ __device__ __forceinline__ void face_neighbours(const GridView& g, int leaf, int
 // copyFromDense: active voxels only (densityvdb.cu:39-48, colorvdb.cu:52-62).
 __global__ void k_copy_from_dense(GridView g, float* dst, const float* __restrict__ arr, int rx,
                                   int ry, int rz) {
+  grid_dep_sync();
   int64_t n = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (n >= int64_t(g.nleaf) * kLeafVox) return;
   const int leaf = int(n >> 9), vox = int(n & 511);
@@ -119,6 +121,7 @@ __global__ void k_copy_from_dense(GridView g, float* dst, const float* __restric
 // copyToDense: every voxel of [0,reso) gets its stored or background value.
 __global__ void k_copy_to_dense(GridView g, const float* __restrict__ src, float* out, int rx,
                                 int ry, int rz, float bg) {
+  grid_dep_sync();
   int64_t n = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (n >= int64_t(rx) * ry * rz) return;
   const int z = int(n % rz), y = int((n / rz) % ry), x = int(n / (int64_t(ry) * rz));
@@ -128,6 +131,7 @@ __global__ void k_copy_to_dense(GridView g, const float* __restrict__ src, float
 
 __global__ void k_set_by_mask(GridView g, const uint8_t* __restrict__ mask, float val, int rx,
                               int ry, int rz) {
+  grid_dep_sync();
   int64_t n = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (n >= int64_t(g.nleaf) * kLeafVox) return;
   const int leaf = int(n >> 9), vox = int(n & 511);
@@ -141,6 +145,7 @@ __global__ void k_set_by_mask(GridView g, const uint8_t* __restrict__ mask, floa
 
 __global__ void k_sample1(GridView g, const float* __restrict__ xs, const float* __restrict__ ys,
                           const float* __restrict__ zs, int64_t n, float* out) {
+  grid_dep_sync();
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   out[p] = trilinear1(g, xs[p], ys[p], zs[p]);
@@ -150,6 +155,7 @@ __global__ void k_sample1(GridView g, const float* __restrict__ xs, const float*
 // first, then out[c] += value[c]*scale in corner order.
 __global__ void k_sampleC(GridView g, const float* __restrict__ xs, const float* __restrict__ ys,
                           const float* __restrict__ zs, int64_t n, float* out) {
+  grid_dep_sync();
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   const float x = xs[p], y = ys[p], z = zs[p];
@@ -176,6 +182,7 @@ __global__ void k_sampleC(GridView g, const float* __restrict__ xs, const float*
 
 __global__ void k_lookup(GridView g, const int32_t* __restrict__ is, const int32_t* __restrict__ js,
                          const int32_t* __restrict__ ks, int64_t n, float* out, uint8_t* act) {
+  grid_dep_sync();
   int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   const int i = is[p], j = js[p], k = ks[p];
@@ -187,6 +194,7 @@ __global__ void k_lookup(GridView g, const int32_t* __restrict__ is, const int32
 }
 
 __global__ void k_zero_grad(GridView g, const uint8_t* __restrict__ touched) {
+  grid_dep_sync();
   int64_t n = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (n >= int64_t(g.nleaf) * kLeafVox) return;
   const int leaf = int(n >> 9), vox = int(n & 511);
@@ -196,6 +204,7 @@ __global__ void k_zero_grad(GridView g, const uint8_t* __restrict__ touched) {
 }
 
 __global__ void k_clear_touched(uint8_t* t, int n) {
+  grid_dep_sync();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) t[i] = 0;
 }
@@ -215,6 +224,7 @@ __device__ __forceinline__ float value_c(const GridView& g, int i, int j, int k,
 // order z-, z+, y-, y+, x-, x+.
 __global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
                      const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+  grid_dep_sync();
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -252,6 +262,7 @@ __global__ void k_tv(GridView g, float wx, float wy, float wz, int dense_mode,
 // Brick bound from scratch: one thread per brick, the max over the 7^3
 // voxels [4b-1, 4b+5] (background outside allocated leaves).
 __global__ void k_bmax_init(GridView g, uint32_t* bmax) {
+  grid_dep_sync();
   const int64_t nb = int64_t(g.bdim[0]) * g.bdim[1] * g.bdim[2];
   for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < nb;
        t += int64_t(gridDim.x) * blockDim.x) {
@@ -272,6 +283,7 @@ __global__ void k_bmax_init(GridView g, uint32_t* bmax) {
 // float4 loads; per-channel arithmetic and order as k_tv.
 __global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mode,
                          const int32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+  grid_dep_sync();
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -346,6 +358,7 @@ __global__ void k_tv_c12(GridView g, float wx, float wy, float wz, int dense_mod
 __global__ void k_tv_terms(GridView g, float wx, float wy, float wz,
                            const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                            float* __restrict__ tv) {
+  grid_dep_sync();
   const int64_t nl = *count;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -379,6 +392,7 @@ __global__ void k_tv_terms(GridView g, float wx, float wy, float wz,
 __global__ void k_tv_terms_c12(GridView g, float wx, float wy, float wz,
                                const int32_t* __restrict__ list,
                                const uint32_t* __restrict__ count, float* __restrict__ tv) {
+  grid_dep_sync();
   const int64_t nl = *count;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < nl * kLeafVox;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -433,6 +447,7 @@ __global__ void k_tv_terms_c12(GridView g, float wx, float wy, float wz,
 
 __global__ void k_touched_compact(const uint8_t* __restrict__ touched, int nleaf, int32_t* list,
                                   uint32_t* count) {
+  grid_dep_sync();
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l < nleaf && touched[l]) list[atomicAdd(count, 1u)] = l;
 }
@@ -510,7 +525,7 @@ static int build_grid(const int reso[3], int C, float bg,
     return cuda_error(e, "grid upload");
   }
   if (nval) {
-    k_fill<<<ceil_div(nval, 256), 256>>>(g->d_data, nval, bg);
+    launch_k(k_fill, ceil_div(nval, 256), 256, 0, 0, g->d_data, nval, bg);
     if ((e = cudaGetLastError()) || (e = cudaDeviceSynchronize())) {
       pvdb_grid_destroy(g);
       return cuda_error(e, "grid fill");
@@ -530,8 +545,8 @@ int touched_list(pvdb_grid_s* g, cudaStream_t st) {
   if (g->tlist_valid) return PVDB_OK;
   PVDB_CHECK_CUDA(cudaMemsetAsync(g->d_tcount, 0, 4, st));
   if (g->nleaf) {
-    k_touched_compact<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf, g->d_tlist,
-                                                              g->d_tcount);
+    launch_k(k_touched_compact, ceil_div(g->nleaf, 256), 256, 0, st, g->d_touched, g->nleaf,
+             g->d_tlist, g->d_tcount);
     PVDB_CHECK_LAUNCH("k_touched_compact");
   }
   g->tlist_valid = true;
@@ -548,7 +563,7 @@ int bmax_ensure(pvdb_grid_s* g, cudaStream_t st) {
     if (rc) return rc;
   }
   GridView v = g->view();
-  k_bmax_init<<<stride_grid(), 256, 0, st>>>(v, g->d_bmax);
+  launch_k(k_bmax_init, stride_grid(), 256, 0, st, v, g->d_bmax);
   PVDB_CHECK_LAUNCH("k_bmax_init");
   g->bmax_valid = true;
   return PVDB_OK;
@@ -558,6 +573,7 @@ int bmax_ensure(pvdb_grid_s* g, cudaStream_t st) {
 // thread: 32 bytes per voxel, channels 0..11 then four zeros, so that a voxel
 // is one aligned 32-byte sector and two 16-byte loads.
 __global__ void k_half_build(const float* __restrict__ src, __nv_bfloat16* dst, int64_t nvox) {
+  grid_dep_sync();
   const int64_t v = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (v >= nvox) return;
   const float4* s4 = reinterpret_cast<const float4*>(src + v * 12);
@@ -580,11 +596,11 @@ int tv_terms_launch(pvdb_grid_s* g, float wx, float wy, float wz, cudaStream_t s
   wy /= 6.f;
   wz /= 6.f;
   if (g->C == 12)
-    k_tv_terms_c12<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, g->d_tlist, g->d_tcount,
-                                                  g->d_tv);
+    launch_k(k_tv_terms_c12, stride_grid(), 256, 0, st, g->view(), wx, wy, wz, g->d_tlist,
+             g->d_tcount, g->d_tv);
   else
-    k_tv_terms<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, g->d_tlist, g->d_tcount,
-                                              g->d_tv);
+    launch_k(k_tv_terms, stride_grid(), 256, 0, st, g->view(), wx, wy, wz, g->d_tlist, g->d_tcount,
+             g->d_tv);
   PVDB_CHECK_LAUNCH("k_tv_terms");
   return PVDB_OK;
 }
@@ -599,7 +615,7 @@ int half_ensure(pvdb_grid_s* g, cudaStream_t st) {
   }
   if (g->half_valid) return PVDB_OK;
   if (nvox) {
-    k_half_build<<<ceil_div(nvox, 256), 256, 0, st>>>(g->d_data, g->d_half, nvox);
+    launch_k(k_half_build, ceil_div(nvox, 256), 256, 0, st, g->d_data, g->d_half, nvox);
     PVDB_CHECK_LAUNCH("k_half_build");
   }
   g->half_valid = true;
@@ -781,9 +797,9 @@ int pvdb_grid_copy_from_dense(pvdb_grid g, int32_t which, const float* arr, int6
   }
   const int64_t ns = g->nslots();
   if (ns)
-    k_copy_from_dense<<<ceil_div(ns, 256), 256, 0, st>>>(
-        g->view(), which == PVDB_WHICH_DATA ? g->d_data : g->d_grad, src, g->reso[0],
-        g->reso[1], g->reso[2]);
+    launch_k(k_copy_from_dense, ceil_div(ns, 256), 256, 0, st, g->view(),
+             which == PVDB_WHICH_DATA ? g->d_data : g->d_grad, src, g->reso[0], g->reso[1],
+             g->reso[2]);
   PVDB_CHECK_LAUNCH("k_copy_from_dense");
   if (which == PVDB_WHICH_GRAD) g->all_touched = true;
   if (which == PVDB_WHICH_DATA) data_written(g);
@@ -808,9 +824,9 @@ int pvdb_grid_copy_to_dense(pvdb_grid g, int32_t which, float* out, int64_t n, i
   // the gradient of a voxel outside every leaf reads as 0, data as the background
   const float bg = which == PVDB_WHICH_DATA ? g->background : 0.f;
   if (nvox)
-    k_copy_to_dense<<<ceil_div(nvox, 256), 256, 0, st>>>(
-        g->view(), which == PVDB_WHICH_DATA ? g->d_data : g->d_grad, dst, g->reso[0], g->reso[1],
-        g->reso[2], bg);
+    launch_k(k_copy_to_dense, ceil_div(nvox, 256), 256, 0, st, g->view(),
+             which == PVDB_WHICH_DATA ? g->d_data : g->d_grad, dst, g->reso[0], g->reso[1],
+             g->reso[2], bg);
   PVDB_CHECK_LAUNCH("k_copy_to_dense");
   if (mem == PVDB_MEM_HOST) {
     PVDB_CHECK_CUDA(cudaMemcpyAsync(out, dst, n * 4, cudaMemcpyDeviceToHost, st));
@@ -835,8 +851,8 @@ int pvdb_grid_set_values_by_mask(pvdb_grid g, const uint8_t* mask, int64_t n, fl
   }
   const int64_t ns = g->nslots();
   if (ns)
-    k_set_by_mask<<<ceil_div(ns, 256), 256, 0, st>>>(g->view(), m, val, g->reso[0], g->reso[1],
-                                                     g->reso[2]);
+    launch_k(k_set_by_mask, ceil_div(ns, 256), 256, 0, st, g->view(), m, val, g->reso[0],
+             g->reso[1], g->reso[2]);
   PVDB_CHECK_LAUNCH("k_set_by_mask");
   data_written(g);
   if (mem == PVDB_MEM_HOST) PVDB_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -863,9 +879,9 @@ int pvdb_grid_sample(pvdb_grid g, const float* xs, const float* ys, const float*
     dx = b; dy = b + n; dz = b + 2 * n; dout = b + 3 * n;
   }
   if (g->C == 1)
-    k_sample1<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), dx, dy, dz, n, dout);
+    launch_k(k_sample1, ceil_div(n, 256), 256, 0, st, g->view(), dx, dy, dz, n, dout);
   else
-    k_sampleC<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), dx, dy, dz, n, dout);
+    launch_k(k_sampleC, ceil_div(n, 256), 256, 0, st, g->view(), dx, dy, dz, n, dout);
   PVDB_CHECK_LAUNCH("k_sample");
   if (mem == PVDB_MEM_HOST) {
     PVDB_CHECK_CUDA(cudaMemcpyAsync(out, dout, n * 4 * g->C, cudaMemcpyDeviceToHost, st));
@@ -896,7 +912,7 @@ int pvdb_grid_lookup(pvdb_grid g, const int32_t* is, const int32_t* js, const in
     dout = (float*)(b + 3 * n);
     dact = active_out ? (uint8_t*)(dout + n * g->C) : nullptr;
   }
-  k_lookup<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), di, dj, dk, n, dout, dact);
+  launch_k(k_lookup, ceil_div(n, 256), 256, 0, st, g->view(), di, dj, dk, n, dout, dact);
   PVDB_CHECK_LAUNCH("k_lookup");
   if (mem == PVDB_MEM_HOST) {
     PVDB_CHECK_CUDA(cudaMemcpyAsync(out, dout, n * 4 * g->C, cudaMemcpyDeviceToHost, st));
@@ -925,11 +941,11 @@ int pvdb_grid_tv_add_grad(pvdb_grid g, float wx, float wy, float wz, int32_t den
     if (rc) return rc;
   }
   if (g->C == 12)
-    k_tv_c12<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
-                                            use_list ? g->d_tlist : nullptr, g->d_tcount);
+    launch_k(k_tv_c12, stride_grid(), 256, 0, st, g->view(), wx, wy, wz, dense_mode ? 1 : 0,
+             use_list ? g->d_tlist : nullptr, g->d_tcount);
   else
-    k_tv<<<stride_grid(), 256, 0, st>>>(g->view(), wx, wy, wz, dense_mode ? 1 : 0,
-                                        use_list ? g->d_tlist : nullptr, g->d_tcount);
+    launch_k(k_tv, stride_grid(), 256, 0, st, g->view(), wx, wy, wz, dense_mode ? 1 : 0,
+             use_list ? g->d_tlist : nullptr, g->d_tcount);
   PVDB_CHECK_LAUNCH("k_tv");
   if (dense_mode) g->all_touched = true;
   return PVDB_OK;
@@ -956,10 +972,10 @@ int pvdb_grid_zero_grad(pvdb_grid g, pvdb_stream s) {
   cudaStream_t st = as_stream(s);
   const int64_t ns = g->nslots();
   if (ns) {
-    k_zero_grad<<<ceil_div(ns, 256), 256, 0, st>>>(g->view(),
-                                                   g->all_touched ? nullptr : g->d_touched);
+    launch_k(k_zero_grad, ceil_div(ns, 256), 256, 0, st, g->view(),
+             g->all_touched ? nullptr : g->d_touched);
     PVDB_CHECK_LAUNCH("k_zero_grad");
-    k_clear_touched<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf);
+    launch_k(k_clear_touched, ceil_div(g->nleaf, 256), 256, 0, st, g->d_touched, g->nleaf);
     PVDB_CHECK_LAUNCH("k_clear_touched");
   }
   g->all_touched = false;

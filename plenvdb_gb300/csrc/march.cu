@@ -58,6 +58,7 @@ __device__ __forceinline__ void load_ray(const float* __restrict__ ro, const flo
 __global__ void __launch_bounds__(256)
     k_march_setup(const float* __restrict__ ro, const float* __restrict__ rd, int R, MarchP P,
                   MarchW W) {
+  grid_dep_sync();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
   float o[3], d[3];
@@ -119,6 +120,7 @@ __device__ __forceinline__ void load_ray_setup(const MarchW& W, int r, RaySetup&
 // One block per ray, threads over the ray's samples.
 __global__ void __launch_bounds__(256)
     k_march_alpha(GridView gd, MarchP P, MarchW W) {
+  grid_dep_sync();
   const int r = blockIdx.x;
   const int ns = W.ray_ns[r];
   RaySetup rs;
@@ -177,6 +179,7 @@ __device__ __forceinline__ void stage_insert(int32_t* hkey, int16_t* hslot, uint
 
 __global__ void __launch_bounds__(256)
     k_march_alpha_staged(GridView gd, MarchP P, MarchW W, uint32_t spin_max, int hold) {
+  grid_dep_sync();
   extern __shared__ __align__(128) float st_vox[];  // [kStageSlots][512]
   __shared__ int32_t hkey[kStageHash];
   __shared__ int16_t hslot[kStageHash];
@@ -280,6 +283,7 @@ constexpr uint32_t kChainSpinMax = 1u << 24;
 
 __global__ void __launch_bounds__(kMarchThreads)
     k_march_chain(int R, MarchP P, MarchW W, uint32_t spin_max, int hold_first) {
+  grid_dep_sync();
   const int lane = threadIdx.x & 31;
   uint32_t ticket = 0;
   if (lane == 0) ticket = atomicAdd(W.totals + 6, 1u);
@@ -500,6 +504,7 @@ __device__ __forceinline__ void k0_trilinear_half(const GridView& g,
 // (colorvdb.cu:81-111).
 __global__ void __launch_bounds__(256)
     k_march_k0(GridView gk, MarchP P, MarchW W) {
+  grid_dep_sync();
   const int64_t M = W.totals[1];
   for (int64_t m = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; m < M;
        m += int64_t(gridDim.x) * blockDim.x) {
@@ -521,6 +526,7 @@ template <int CT>
 __global__ void __launch_bounds__(256)
     k_march_k0_x(GridView gk, MarchP P, MarchW W, const float* __restrict__ pe, int pe_stride,
                  int dpe, uint8_t* xt, const __nv_bfloat16* __restrict__ half) {
+  grid_dep_sync();
   // CT = 12: the channel count is a compile-time constant, so the row's
   // features stay in registers; CT = 0: any count up to 16
   const int64_t M = W.totals[1];
@@ -578,6 +584,7 @@ __global__ void __launch_bounds__(kMarchThreads)
     k_march_bwd(GridView gd, int R, MarchP P, MarchW W, const float* __restrict__ grad_w,
                 const float* __restrict__ grad_last, uint32_t* keys, uint32_t* cnt,
                 uint32_t* leaf_cnt, uint32_t* rank) {
+  grid_dep_sync();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -685,6 +692,7 @@ __global__ void __launch_bounds__(256)
                    const uint32_t* __restrict__ leaf_off, int64_t nleaves, uint32_t* off,
                    GridView gd, GridView gc, uint8_t* touched_d, uint8_t* touched_c,
                    int k0_same) {
+  grid_dep_sync();
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
@@ -751,6 +759,7 @@ __global__ void __launch_bounds__(256)
 __global__ void k_cell_place(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
                              const uint32_t* __restrict__ off, const uint32_t* __restrict__ rank,
                              uint32_t* skeys, uint32_t* svals) {
+  grid_dep_sync();
   const int64_t n = *n_dev;
   for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
        s += int64_t(gridDim.x) * blockDim.x) {
@@ -820,6 +829,7 @@ __device__ __forceinline__ void sort8(uint32_t v[8]) {
 __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t* n_dev,
                              const uint32_t* __restrict__ cnt, uint32_t* svals,
                              const float4* __restrict__ rec, float4* rec_s) {
+  grid_dep_sync();
   const int64_t n = *n_dev;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x) {
@@ -850,6 +860,7 @@ __global__ void k_cell_heads(const uint32_t* __restrict__ skeys, const uint32_t*
 // Resets the counts of the cells and leaves that got samples.
 __global__ void k_cell_clear(const uint32_t* __restrict__ keys, const uint32_t* n_dev,
                              uint32_t* cnt, uint32_t* leaf_cnt) {
+  grid_dep_sync();
   const int64_t n = *n_dev;
   for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n;
        s += int64_t(gridDim.x) * blockDim.x) {
@@ -902,6 +913,7 @@ __global__ void __launch_bounds__(256)
     k_group_records(const uint32_t* __restrict__ svals, const uint32_t* n_dev,
                     const float4* __restrict__ rec, const int32_t* __restrict__ brow,
                     const float* __restrict__ gk0, int C, int vec, float4* rec_g) {
+  grid_dep_sync();
   constexpr int NB = NQ > 0 ? NQ : 1;
   const int64_t n = *n_dev;
   for (int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; j < n;
@@ -948,6 +960,7 @@ __global__ void __launch_bounds__(256, 4)
     k_voxel_gather(GridView g, const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                    const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off,
                    const float4* __restrict__ rec_g, float* grad_d, float* grad_c, int C) {
+  grid_dep_sync();
   constexpr int NB = NQ > 0 ? NQ : 1;
   const int64_t nv = int64_t(*count) * kLeafVox;
   const bool want_d = grad_d != nullptr, want_c = NQ && grad_c;
@@ -1037,19 +1050,18 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
     PVDB_REQUIRE(m->b_rec_s_cap >= size_t(m->slots) * 16 * (1 + NQ),
                  "march backward: grouped-record buffer too small");
     const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(grid)));
-    k_group_records<NQ><<<sgrid, 256, 0, st>>>(m->red.vals[0], m->w.totals + 5, m->w.b_rec,
-                                               m->w.b_row, grad_k0, C, vec, m->b_rec_s);
+    launch_k(k_group_records<NQ>, sgrid, 256, 0, st, m->red.vals[0], m->w.totals + 5, m->w.b_rec,
+             m->w.b_row, grad_k0, C, vec, m->b_rec_s);
     PVDB_CHECK_LAUNCH("k_group_records");
   }
   const float4* rec_g = m->b_rec_s;
-  k_voxel_gather<NQ><<<grid, 256, 0, st>>>(gv, density->d_tlist, density->d_tcount, m->cell_cnt,
-                                           m->cell_off, rec_g, density->d_grad,
-                                           same ? k0->d_grad : nullptr, C);
+  launch_k(k_voxel_gather<NQ>, grid, 256, 0, st, gv, density->d_tlist, density->d_tcount,
+           m->cell_cnt, m->cell_off, rec_g, density->d_grad, same ? k0->d_grad : nullptr, C);
   PVDB_CHECK_LAUNCH("k_voxel_gather");
   if (NQ && !same) {
     if ((rc = touched_list(k0, st))) return rc;
-    k_voxel_gather<NQ><<<grid, 256, 0, st>>>(kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
-                                             m->cell_off, rec_g, nullptr, k0->d_grad, C);
+    launch_k(k_voxel_gather<NQ>, grid, 256, 0, st, kv, k0->d_tlist, k0->d_tcount, m->cell_cnt,
+             m->cell_off, rec_g, nullptr, k0->d_grad, C);
     PVDB_CHECK_LAUNCH("k_voxel_gather(k0)");
   }
   return PVDB_OK;
@@ -1058,6 +1070,7 @@ static int cell_reduce_launch(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s
 // --------------------------------------------------------------- composite
 __global__ void __launch_bounds__(kMarchThreads)
     k_composite_fwd(MarchW W, const float* __restrict__ rgb, float bg, float* out, int R) {
+  grid_dep_sync();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -1088,6 +1101,7 @@ __global__ void __launch_bounds__(kMarchThreads)
 __global__ void __launch_bounds__(kMarchThreads)
     k_composite_bwd(MarchW W, const float* __restrict__ rgb, const float* __restrict__ g, float bg,
                     float* grad_rgb, float* grad_w, float* grad_last, int R) {
+  grid_dep_sync();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kMarchWarps + warp;
   if (r >= R) return;
@@ -1175,27 +1189,26 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   PVDB_CHECK_CUDA(cudaMemsetAsync(m->w.totals, 0, 32, st));
   if (R > 0) {
     const int nb = ceil_div(R, kMarchWarps);
-    k_march_setup<<<ceil_div(R, 256), 256, 0, st>>>(ro, rd, R, m->p, m->w);
+    launch_k(k_march_setup, ceil_div(R, 256), 256, 0, st, ro, rd, R, m->p, m->w);
     PVDB_CHECK_LAUNCH("k_march_setup");
     if (m->leaf_staging) {
       PVDB_SMEM_ATTR(k_march_alpha_staged, int(kStageSmem));
-      k_march_alpha_staged<<<R, 256, kStageSmem, st>>>(density->view(), m->p, m->w,
-                                                       debug_spin_limit(kStageSpinMax),
-                                                       debug_hold_staging());
+      launch_k(k_march_alpha_staged, R, 256, kStageSmem, st, density->view(), m->p, m->w,
+               debug_spin_limit(kStageSpinMax), debug_hold_staging());
       PVDB_CHECK_LAUNCH("k_march_alpha_staged");
     } else {
-      k_march_alpha<<<R, 256, 0, st>>>(density->view(), m->p, m->w);
+      launch_k(k_march_alpha, R, 256, 0, st, density->view(), m->p, m->w);
       PVDB_CHECK_LAUNCH("k_march_alpha");
     }
-    k_march_chain<<<nb, kMarchThreads, 0, st>>>(R, m->p, m->w, debug_spin_limit(kChainSpinMax),
-                                                debug_hold_first());
+    launch_k(k_march_chain, nb, kMarchThreads, 0, st, R, m->p, m->w,
+             debug_spin_limit(kChainSpinMax), debug_hold_first());
     PVDB_CHECK_LAUNCH("k_march_chain");
     if (m->prof) prof_mark(st, 1);
     GridView gk{};
     if (k0) gk = k0->view();
     if (k0 && !skip_k0) {
-      k_march_k0<<<int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16)), 256, 0,
-                   st>>>(gk, m->p, m->w);
+      launch_k(k_march_k0, int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16)),
+               256, 0, st, gk, m->p, m->w);
       PVDB_CHECK_LAUNCH("k_march_k0");
     }
     if (m->prof) prof_mark(st, 2);
@@ -1220,11 +1233,11 @@ int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t
                "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   const int grid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16));
   if (m->k0->C == 12)
-    k_march_k0_x<12><<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
-                                           half);
+    launch_k(k_march_k0_x<12>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
+             half);
   else
-    k_march_k0_x<0><<<grid, 256, 0, st>>>(m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
-                                          nullptr);
+    launch_k(k_march_k0_x<0>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
+             nullptr);
   PVDB_CHECK_LAUNCH("k_march_k0_x");
   if (m->prof) prof_mark(st, 2);
   return PVDB_OK;
@@ -1268,8 +1281,8 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   uint32_t* rank = m->red.vals[1];
   uint32_t* skeys = m->red.keys[1];
   uint32_t* svals = m->red.vals[0];
-  k_march_bwd<<<nb, kMarchThreads, 0, st>>>(density->view(), R, m->p, m->w, grad_w, grad_last,
-                                            m->red.keys[0], m->cell_cnt, m->leaf_cnt, rank);
+  launch_k(k_march_bwd, nb, kMarchThreads, 0, st, density->view(), R, m->p, m->w, grad_w, grad_last,
+           m->red.keys[0], m->cell_cnt, m->leaf_cnt, rank);
   PVDB_CHECK_LAUNCH("k_march_bwd");
   if (m->prof) prof_mark(st, 6);
   // group the kept samples by cell (stable order, see above)
@@ -1279,15 +1292,15 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
   if (rc) return rc;
   const GridView gv = density->view();
   const GridView kv = k0 ? k0->view() : gv;
-  k_cell_offsets<<<int(std::min<int64_t>(ceil_div(nleaves, 8), int64_t(stride_grid()))), 256, 0,
-                   st>>>(m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off, gv, kv,
-                         density->d_touched, k0 ? k0->d_touched : nullptr,
-                         k0 && k0->h_table == density->h_table ? 1 : 0);
+  launch_k(k_cell_offsets, int(std::min<int64_t>(ceil_div(nleaves, 8), int64_t(stride_grid()))),
+           256, 0, st, m->cell_cnt, m->leaf_cnt, m->leaf_off, nleaves, m->cell_off, gv, kv,
+           density->d_touched, k0 ? k0->d_touched : nullptr,
+           k0 && k0->h_table == density->h_table ? 1 : 0);
   PVDB_CHECK_LAUNCH("k_cell_offsets");
-  k_cell_place<<<sgrid, 256, 0, st>>>(keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
+  launch_k(k_cell_place, sgrid, 256, 0, st, keys, m->w.totals + 0, m->cell_off, rank, skeys, svals);
   PVDB_CHECK_LAUNCH("k_cell_place");
-  k_cell_heads<<<stride_grid(), 256, 0, st>>>(skeys, m->w.totals + 5, m->cell_cnt, svals,
-                                              m->w.b_rec, k0 ? nullptr : m->b_rec_s);
+  launch_k(k_cell_heads, stride_grid(), 256, 0, st, skeys, m->w.totals + 5, m->cell_cnt, svals,
+           m->w.b_rec, k0 ? nullptr : m->b_rec_s);
   PVDB_CHECK_LAUNCH("k_cell_heads");
   density->tlist_valid = false;
   if (k0) k0->tlist_valid = false;
@@ -1306,7 +1319,8 @@ int march_backward_keys(pvdb_march_s* m, const float* grad_w, const float* grad_
 int march_backward_clear(pvdb_march_s* m, cudaStream_t st) {
   if (m->n_rays == 0) return PVDB_OK;
   const int sgrid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(stride_grid())));
-  k_cell_clear<<<sgrid, 256, 0, st>>>(m->red.keys[0], m->w.totals + 0, m->cell_cnt, m->leaf_cnt);
+  launch_k(k_cell_clear, sgrid, 256, 0, st, m->red.keys[0], m->w.totals + 0, m->cell_cnt,
+           m->leaf_cnt);
   PVDB_CHECK_LAUNCH("k_cell_clear");
   return PVDB_OK;
 }
@@ -1347,7 +1361,7 @@ int march_backward_impl(pvdb_march_s* m, const float* grad_w, const float* grad_
 int composite_forward_impl(pvdb_march_s* m, const float* rgb, float bg, float* out, int R,
                            cudaStream_t st) {
   if (R <= 0) return PVDB_OK;
-  k_composite_fwd<<<ceil_div(R, kMarchWarps), kMarchThreads, 0, st>>>(m->w, rgb, bg, out, R);
+  launch_k(k_composite_fwd, ceil_div(R, kMarchWarps), kMarchThreads, 0, st, m->w, rgb, bg, out, R);
   PVDB_CHECK_LAUNCH("k_composite_fwd");
   return PVDB_OK;
 }
@@ -1356,8 +1370,8 @@ int composite_backward_impl(pvdb_march_s* m, const float* rgb, const float* g, f
                             float* grad_rgb, float* grad_w, float* grad_last, int R,
                             cudaStream_t st) {
   if (R <= 0) return PVDB_OK;
-  k_composite_bwd<<<ceil_div(R, kMarchWarps), kMarchThreads, 0, st>>>(m->w, rgb, g, bg, grad_rgb,
-                                                                      grad_w, grad_last, R);
+  launch_k(k_composite_bwd, ceil_div(R, kMarchWarps), kMarchThreads, 0, st, m->w, rgb, g, bg,
+           grad_rgb, grad_w, grad_last, R);
   PVDB_CHECK_LAUNCH("k_composite_bwd");
   return PVDB_OK;
 }

@@ -45,7 +45,8 @@ __host__ __device__ inline int64_t mlp_param_count(int din) { return int64_t(kW)
 constexpr int kPeRays = 32;
 __global__ void __launch_bounds__(128)
     k_pe_hpe(const float* __restrict__ viewdirs, int R, int npe, MlpArgs a, float* pe_out,
-             float* hpe) {  // hpe == NULL: the PE only
+             float* hpe) {
+  grid_dep_sync();  // hpe == NULL: the PE only
   __shared__ float wt[kMaxPe][kW];       // wt[q][n] = w0[n][c0+q]
   __shared__ float pe_s[kPeRays][kMaxPe];
   const int n = threadIdx.x;
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
     k_mlp_fwd_f32(MlpArgs a, const float* __restrict__ k0, const int32_t* __restrict__ ray,
                   const float* __restrict__ hpe, const uint32_t* __restrict__ totals,
                   float* rgb, int out_logits) {
+  grid_dep_sync();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem_raw);
   const int64_t M = totals[1];
@@ -211,6 +213,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
                   const float* __restrict__ hpe, const float* __restrict__ pe_buf,
                   const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
                   const float* __restrict__ grad_rgb, float* grad_k0, float* wpart) {
+  grid_dep_sync();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpBwdSmem& B = *reinterpret_cast<MlpBwdSmem*>(smem_raw);
   MlpSmem& S = B.f;
@@ -384,6 +387,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
 // increasing c, then the 8 warp sums combine as ((s0+s1)+(s2+s3))+((s4+s5)+(s6+s7)).
 __global__ void __launch_bounds__(256)
     k_wgrad_reduce(const float* __restrict__ wpart, int nparts, int64_t P, float* out) {
+  grid_dep_sync();
   __shared__ float part[8][33];
   const int u = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t i = blockIdx.x * 32ll + lane;
@@ -399,6 +403,7 @@ __global__ void __launch_bounds__(256)
 
 __global__ void k_scatter_grads(const float* __restrict__ flat, int din, float* w0, float* b0,
                                 float* w1, float* b1, float* w2, float* b2) {
+  grid_dep_sync();
   const int64_t P = mlp_param_count(din);
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= P) return;
@@ -448,8 +453,8 @@ int mlp_prepare(pvdb_march_s* m, const MlpArgs& a, const float* viewdirs, int R,
   int rc = mlp_reserve(m, a.din);
   if (rc) return rc;
   float* pe = m->hpe + size_t(m->max_rays) * kW;
-  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe,
-                                                 precision == 1 ? nullptr : m->hpe);
+  launch_k(k_pe_hpe, ceil_div(R, kPeRays), kW, 0, st, viewdirs, R, (a.dpe - 3) / 6, a, pe,
+           precision == 1 ? nullptr : m->hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_pack(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, &m->mlp_packed,
@@ -480,7 +485,7 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
   float* hpe = m->hpe;
   float* pe = m->hpe + size_t(m->max_rays) * kW;
   if (!prepared) {
-    k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+    launch_k(k_pe_hpe, ceil_div(R, kPeRays), kW, 0, st, viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
     PVDB_CHECK_LAUNCH("k_pe_hpe");
   }
   if (precision == 1)
@@ -489,8 +494,8 @@ int mlp_forward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows,
                                &m->mlp_packed, &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap,
                                m->w.totals + 3, st, prepared ? 1 : 0, x_ready ? 1 : 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
-  k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(
-      a, k0rows, m->w.r_ray, hpe, m->w.totals, rgb, 0);
+  launch_k(k_mlp_fwd_f32, mlp_grid(), kMlpThreads, sizeof(MlpSmem), st, a, k0rows, m->w.r_ray, hpe,
+           m->w.totals, rgb, 0);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_f32");
   return PVDB_OK;
 }
@@ -503,8 +508,8 @@ int mlp_pe_rows(const MlpArgs& a, const float* viewdirs, int R, float* hpe_buf, 
                 cudaStream_t st) {
   *pe_stride = kMaxPe;
   if (R <= 0) return PVDB_OK;
-  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a,
-                                                 hpe_buf + size_t(R) * kW, nullptr);
+  launch_k(k_pe_hpe, ceil_div(R, kPeRays), kW, 0, st, viewdirs, R, (a.dpe - 3) / 6, a,
+           hpe_buf + size_t(R) * kW, nullptr);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   return PVDB_OK;
 }
@@ -523,15 +528,15 @@ int mlp_forward_rows(const MlpArgs& a, const float* k0rows, const int32_t* ray,
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
                                kMaxPe, totals, max_rows, out, out_logits, blob, blob_cap, xt,
                                xt_cap, err, st, 0, 1);
-  k_pe_hpe<<<ceil_div(R, kPeRays), kW, 0, st>>>(viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
+  launch_k(k_pe_hpe, ceil_div(R, kPeRays), kW, 0, st, viewdirs, R, (a.dpe - 3) / 6, a, pe, hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   if (precision == 1)
     return mlp_tc_forward_rows(a.w0, a.b0, a.w1, a.b1, a.w2, a.b2, a.c0, a.dpe, k0rows, ray, pe,
                                kMaxPe, totals, max_rows, out, out_logits, blob, blob_cap, xt,
                                xt_cap, err, st, 0, 0);
   PVDB_SMEM_ATTR(k_mlp_fwd_f32, int(sizeof(MlpSmem)));
-  k_mlp_fwd_f32<<<mlp_grid(), kMlpThreads, sizeof(MlpSmem), st>>>(a, k0rows, ray, hpe, totals,
-                                                                  out, out_logits);
+  launch_k(k_mlp_fwd_f32, mlp_grid(), kMlpThreads, sizeof(MlpSmem), st, a, k0rows, ray, hpe, totals,
+           out, out_logits);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_f32(rows)");
   return PVDB_OK;
 }
@@ -565,16 +570,15 @@ int mlp_backward_impl(pvdb_march_s* m, const MlpArgs& a, const float* k0rows, co
                               &m->mlp_packed_cap, &m->mlp_xt, &m->mlp_xt_cap, m->w.totals + 3, st,
                               prepared ? 1 : 0, prepared ? 1 : 0);
     if (rc) return rc;
-    k_wgrad_reduce<<<ceil_div(P, 32), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+    launch_k(k_wgrad_reduce, ceil_div(P, 32), 256, 0, st, m->wpart, G, P, grad_flat);
     PVDB_CHECK_LAUNCH("k_wgrad_reduce");
     return PVDB_OK;
   }
   PVDB_SMEM_ATTR(k_mlp_bwd_f32, int(sizeof(MlpBwdSmem)));
-  k_mlp_bwd_f32<<<G, kMlpThreads, sizeof(MlpBwdSmem), st>>>(
-      a, k0rows, m->w.r_ray, m->hpe, m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb,
-      grad_rgb, grad_k0, m->wpart);
+  launch_k(k_mlp_bwd_f32, G, kMlpThreads, sizeof(MlpBwdSmem), st, a, k0rows, m->w.r_ray, m->hpe,
+           m->hpe + size_t(m->max_rays) * kW, m->w.totals, rgb, grad_rgb, grad_k0, m->wpart);
   PVDB_CHECK_LAUNCH("k_mlp_bwd_f32");
-  k_wgrad_reduce<<<ceil_div(P, 32), 256, 0, st>>>(m->wpart, G, P, grad_flat);
+  launch_k(k_wgrad_reduce, ceil_div(P, 32), 256, 0, st, m->wpart, G, P, grad_flat);
   PVDB_CHECK_LAUNCH("k_wgrad_reduce");
   return PVDB_OK;
 }
@@ -627,16 +631,16 @@ int pvdb_mlp_backward(pvdb_march m, const pvdb_mlp_weights* w, const float* k0,
   // backward does not rely on a preceding forward call of the same weights.
   rc = mlp_reserve(m, a.din);
   if (rc) return rc;
-  k_pe_hpe<<<ceil_div(m->n_rays, kPeRays), kW, 0, st>>>(
-      viewdirs, m->n_rays, (a.dpe - 3) / 6, a, m->hpe + size_t(m->max_rays) * kW, m->hpe);
+  launch_k(k_pe_hpe, ceil_div(m->n_rays, kPeRays), kW, 0, st, viewdirs, m->n_rays, (a.dpe - 3) / 6,
+           a, m->hpe + size_t(m->max_rays) * kW, m->hpe);
   PVDB_CHECK_LAUNCH("k_pe_hpe");
   const int64_t P = mlp_param_count(a.din);
   float* flat = m->wpart + int64_t(mlp_grid()) * P;  // spare slot after the partials
   rc = mlp_backward_impl(m, a, k0 ? k0 : m->w.r_k0, rgb, grad_rgb, grad_k0, flat, precision, st,
                          false);
   if (rc) return rc;
-  k_scatter_grads<<<ceil_div(P, 256), 256, 0, st>>>(flat, a.din, g->w0, g->b0, g->w1, g->b1, g->w2,
-                                                     g->b2);
+  launch_k(k_scatter_grads, ceil_div(P, 256), 256, 0, st, flat, a.din, g->w0, g->b0, g->w1, g->b1,
+           g->w2, g->b2);
   PVDB_CHECK_LAUNCH("k_scatter_grads");
   return PVDB_OK;
 }

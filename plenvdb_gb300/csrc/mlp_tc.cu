@@ -59,6 +59,7 @@ struct MlpArgsTc {
 // element). The backward reads the same tiles, transposed through MN-major
 // descriptors.
 __global__ void k_pack(MlpArgsTc a, uint8_t* blob) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   __nv_bfloat16* w0 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW0);
   __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(blob + kOffW1);
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(256)
     k_build_x(MlpArgsTc a, const float* __restrict__ k0, const int32_t* __restrict__ ray,
               const float* __restrict__ pe, int pe_stride, const uint32_t* __restrict__ totals,
               uint8_t* xt) {
+  grid_dep_sync();
   const int64_t M = totals[1];
   const int64_t nchunks = (M + 127) / 128 * (128 * 6);
   for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < nchunks;
@@ -163,6 +165,7 @@ __device__ __forceinline__ void store_relu32(uint8_t* tile, int row, int col0, i
 __global__ void __launch_bounds__(kTcThreads, 2)
     k_mlp_fwd_tc(MlpArgsTc a, const uint8_t* __restrict__ blob, const uint8_t* __restrict__ xt,
                  const uint32_t* __restrict__ totals, float* out, int out_logits, uint32_t* err) {
+  grid_dep_sync();
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
   const int64_t ntiles = (M + 127) / 128;
@@ -414,6 +417,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
                  const uint32_t* __restrict__ totals, const float* __restrict__ rgb,
                  const float* __restrict__ grad_rgb, float* grad_k0, float* wpart, uint32_t* err,
                  uint32_t spin_max, int hold) {
+  grid_dep_sync();
   extern __shared__ __align__(1024) uint8_t sm[];
   const int64_t M = totals[1];
   const int64_t ntiles = (M + 127) / 128;
@@ -825,7 +829,7 @@ int mlp_tc_pack(const float* w0, const float* b0, const float* w1, const float* 
   int rc = dev_reserve(blob, blob_cap, kPackFwdBytes);
   if (rc) return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
-  k_pack<<<ceil_div(128 * 128, 256), 256, 0, st>>>(a, static_cast<uint8_t*>(*blob));
+  launch_k(k_pack, ceil_div(128 * 128, 256), 256, 0, st, a, static_cast<uint8_t*>(*blob));
   PVDB_CHECK_LAUNCH("k_pack");
   return PVDB_OK;
 }
@@ -842,8 +846,8 @@ int mlp_tc_build_x(int c0, int dpe, const float* k0rows, const int32_t* ray, con
   if (rc) return rc;
   MlpArgsTc a{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, c0, dpe, c0 + dpe};
   const int grid = int(std::min<int64_t>(ceil_div(ntiles * 128 * 6, 256), int64_t(num_sms()) * 16));
-  k_build_x<<<std::max(grid, 1), 256, 0, st>>>(a, k0rows, ray, pe, pe_stride, totals,
-                                               static_cast<uint8_t*>(*xt));
+  launch_k(k_build_x, std::max(grid, 1), 256, 0, st, a, k0rows, ray, pe, pe_stride, totals,
+           static_cast<uint8_t*>(*xt));
   PVDB_CHECK_LAUNCH("k_build_x");
   return PVDB_OK;
 }
@@ -864,9 +868,9 @@ int mlp_tc_forward_rows(const float* w0, const float* b0, const float* w1, const
     return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_fwd_tc, int(kSmFwdBytes));
-  k_mlp_fwd_tc<<<2 * num_sms(), kTcThreads, kSmFwdBytes, st>>>(
-      a, static_cast<const uint8_t*>(*blob), static_cast<const uint8_t*>(*xt), totals, out,
-      out_logits, err);
+  launch_k(k_mlp_fwd_tc, 2 * num_sms(), kTcThreads, kSmFwdBytes, st, a,
+           static_cast<const uint8_t*>(*blob), static_cast<const uint8_t*>(*xt), totals, out,
+           out_logits, err);
   PVDB_CHECK_LAUNCH("k_mlp_fwd_tc");
   return PVDB_OK;
 }
@@ -888,9 +892,9 @@ int mlp_tc_backward_rows(const float* w0, const float* b0, const float* w1, cons
     return rc;
   MlpArgsTc a{w0, b0, w1, b1, w2, b2, c0, dpe, c0 + dpe};
   PVDB_SMEM_ATTR(k_mlp_bwd_tc, int(kSmBwdBytes));
-  k_mlp_bwd_tc<<<grid, kBwdThreads, kSmBwdBytes, st>>>(
-      a, static_cast<const uint8_t*>(*blob), static_cast<const uint8_t*>(*xt), totals, rgb,
-      grad_rgb, grad_k0, wpart, err, debug_spin_limit(kWaitIters), debug_hold_first());
+  launch_k(k_mlp_bwd_tc, grid, kBwdThreads, kSmBwdBytes, st, a, static_cast<const uint8_t*>(*blob),
+           static_cast<const uint8_t*>(*xt), totals, rgb, grad_rgb, grad_k0, wpart, err,
+           debug_spin_limit(kWaitIters), debug_hold_first());
   PVDB_CHECK_LAUNCH("k_mlp_bwd_tc");
   return PVDB_OK;
 }

@@ -32,6 +32,7 @@ __global__ void k_vdb_adam(GridView g, float* __restrict__ m, float* __restrict_
                            const float* __restrict__ stepsz_dev, float eps, float b0, float b1,
                            int mode, int zero_after, const int32_t* __restrict__ list,
                            const uint32_t* __restrict__ count, const float* __restrict__ tv) {
+  grid_dep_sync();
   const int G = g.C == 1 ? 1 : 3;
   const int ngroups = g.C / G;
   const int64_t per = int64_t(kLeafVox) * ngroups;
@@ -102,6 +103,7 @@ __global__ void __launch_bounds__(256)
                 float eps, float b0, float b1, int mode, int zero_after,
                 const int32_t* __restrict__ list, const uint32_t* __restrict__ count,
                 const float* __restrict__ tv, uint32_t* counts) {
+  grid_dep_sync();
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   const int lane = threadIdx.x & 31;
@@ -167,6 +169,7 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
                                int mode, int zero_after, const int32_t* __restrict__ list,
                                const uint32_t* __restrict__ count, __nv_bfloat16* half,
                                const float* __restrict__ tv, uint32_t* counts) {
+  grid_dep_sync();
   const int64_t nl = list ? int64_t(*count) : int64_t(g.nleaf);
   if (stepsz_dev) stepsz = *stepsz_dev;
   uint32_t n_act = 0, n_upd = 0;
@@ -253,6 +256,7 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
 // nothing to do, their gradient is already zero.
 
 __global__ void k_clear_u8(uint8_t* t, int n) {
+  grid_dep_sync();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) t[i] = 0;
 }
@@ -262,6 +266,7 @@ __global__ void k_adam_dense(float* __restrict__ p, const float* __restrict__ g,
                              float* __restrict__ m, float* __restrict__ v,
                              const float* __restrict__ perlr, int64_t n, float stepsz,
                              const float* __restrict__ stepsz_dev, float b1, float b2, float eps) {
+  grid_dep_sync();
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
@@ -285,11 +290,11 @@ int adam_dense_launch(float* param, const float* grad, float* m, float* v, const
   const int nb = ceil_div(n, 256);
   const float* sd = stepsz_dev;
   if (mode == 1)
-    k_adam_dense<1><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
+    launch_k(k_adam_dense<1>, nb, 256, 0, st, param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   else if (mode == 2)
-    k_adam_dense<2><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
+    launch_k(k_adam_dense<2>, nb, 256, 0, st, param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   else
-    k_adam_dense<0><<<nb, 256, 0, st>>>(param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
+    launch_k(k_adam_dense<0>, nb, 256, 0, st, param, grad, m, v, perlr, n, stepsz, sd, b1, b2, eps);
   PVDB_CHECK_LAUNCH("k_adam_dense");
   return PVDB_OK;
 }
@@ -327,27 +332,25 @@ int opt_launch(pvdb_opt_s* o, int mode, int zero_after, float stepsz, const floa
       if (rc) return rc;
     }
     if (g->C == 12)
-      k_vdb_adam_c12<<<stride_grid(), 256, 0, st>>>(
-          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
-          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, g->d_half,
-          tv, counts);
+      launch_k(k_vdb_adam_c12, stride_grid(), 256, 0, st, g->view(), o->exp_avg->d_data,
+               o->exp_avg_sq->d_data, mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev,
+               o->eps, o->beta0, o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr,
+               g->d_tcount, g->d_half, tv, counts);
     else if (g->C == 1)
-      k_vdb_adam1<<<stride_grid(), 256, 0, st>>>(
-          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
-          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv,
-          counts);
+      launch_k(k_vdb_adam1, stride_grid(), 256, 0, st, g->view(), o->exp_avg->d_data,
+               o->exp_avg_sq->d_data, mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev,
+               o->eps, o->beta0, o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr,
+               g->d_tcount, tv, counts);
     else
-      k_vdb_adam<<<stride_grid(), 256, 0, st>>>(
-          g->view(), o->exp_avg->d_data, o->exp_avg_sq->d_data,
-          mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev, o->eps, o->beta0,
-          o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr, g->d_tcount, tv);
+      launch_k(k_vdb_adam, stride_grid(), 256, 0, st, g->view(), o->exp_avg->d_data,
+               o->exp_avg_sq->d_data, mode == 2 ? o->per_lr->d_data : nullptr, stepsz, stepsz_dev,
+               o->eps, o->beta0, o->beta1, mode, zero_after, use_list ? g->d_tlist : nullptr,
+               g->d_tcount, tv);
     PVDB_CHECK_LAUNCH("k_vdb_adam");
     if (g->C != 12) g->half_valid = false;  // only the 12-channel update writes the shadow
   }
   if (zero_after && g->nleaf) {
-    k_clear_u8<<<ceil_div(g->nleaf, 256), 256, 0, st>>>(g->d_touched, g->nleaf);
+    launch_k(k_clear_u8, ceil_div(g->nleaf, 256), 256, 0, st, g->d_touched, g->nleaf);
     PVDB_CHECK_LAUNCH("k_clear_u8");
     g->all_touched = false;
     g->tlist_valid = false;

@@ -11,6 +11,7 @@
 // leaf*512 + offset. Leaves are numbered in Morton order of their leaf
 // coordinates so that leaves adjacent along a ray sit close together.
 #pragma once
+#include <utility>
 
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -391,6 +392,42 @@ int touched_list(pvdb_grid_s* g, cudaStream_t st);
 
 // Fixed grid for grid-stride kernels whose work size lives on the device.
 inline int stride_grid() { return num_sms() * 8; }
+
+// Programmatic dependent launch. Kernels launched by launch_k on a stream
+// that is not being captured may be scheduled while the kernel before them
+// in the stream is still running, so that a dependent kernel's launch
+// overlaps its predecessor's tail instead of following its completion (the
+// eager steps are chains of dependent kernels). Every kernel of the library
+// starts with grid_dep_sync(): it waits until the preceding kernel has
+// completed and its writes are visible (a no-op for a kernel launched
+// without the attribute), then allows the kernel after it to be scheduled.
+// So nothing a kernel reads or writes overlaps its predecessor; only the
+// launch does. Captured graphs keep plain edges: their kernel nodes launch
+// back to back already, and early-scheduled blocks waiting on one branch
+// measured slower beside the step's parallel branches.
+__device__ __forceinline__ void grid_dep_sync() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                     cudaStream_t st, Args&&... args) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  (void)cudaStreamIsCapturing(st, &cap);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = cap == cudaStreamCaptureStatusNone ? 1 : 0;
+  // an error is left for the PVDB_CHECK_LAUNCH that follows every launch
+  (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Number of key bits needed so that all slots and the invalid key sort apart.
 int slot_key_bits(int64_t nslots);

@@ -64,6 +64,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 __global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n_max,
                               const uint32_t* n_dev, uint32_t* partial) {
+  grid_dep_sync();
   const int64_t n = eff_size(n_max, n_dev);
   const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -80,6 +81,7 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n_max,
 
 __global__ void k_scan_partials(uint32_t* partial, int64_t n_max, const uint32_t* n_dev,
                                 uint32_t* total) {
+  grid_dep_sync();
   __shared__ uint32_t carry_s;
   const int64_t n = eff_size(n_max, n_dev);
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
@@ -101,6 +103,7 @@ __global__ void k_scan_partials(uint32_t* partial, int64_t n_max, const uint32_t
 
 __global__ void k_scan_apply(const uint32_t* __restrict__ in, uint32_t* out, int64_t n_max,
                              const uint32_t* n_dev, const uint32_t* __restrict__ partial) {
+  grid_dep_sync();
   const int64_t n = eff_size(n_max, n_dev);
   const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -135,6 +138,7 @@ __device__ __forceinline__ int scan1_pad(int i) { return i + (i >> 5); }
 __global__ void __launch_bounds__(kScan1Threads)
     k_scan_single(const uint32_t* __restrict__ in, uint32_t* out, int64_t n_max,
                   const uint32_t* n_dev, uint32_t* total) {
+  grid_dep_sync();
   constexpr int kChunk = kScan1Threads * kScan1Items;
   __shared__ uint32_t buf[kChunk + kChunk / 32];
   __shared__ uint32_t carry_s;
@@ -189,7 +193,7 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
     return PVDB_OK;
   }
   if (n_max <= kScan1Max) {
-    k_scan_single<<<1, kScan1Threads, 0, st>>>(in, out, n_max, n_dev, total);
+    launch_k(k_scan_single, 1, kScan1Threads, 0, st, in, out, n_max, n_dev, total);
     PVDB_CHECK_LAUNCH("k_scan_single");
     return PVDB_OK;
   }
@@ -197,9 +201,9 @@ int scan_exclusive_u32_dev(const uint32_t* in, uint32_t* out, int64_t n_max,
   int rc = dev_reserve((void**)partial, partial_cap, size_t(nb) * 4);
   if (rc) return rc;
   const int grid = int(std::min<int64_t>(nb, int64_t(num_sms()) * 8));
-  k_scan_reduce<<<grid, kScanThreads, 0, st>>>(in, n_max, n_dev, *partial);
-  k_scan_partials<<<1, 1024, 0, st>>>(*partial, n_max, n_dev, total);
-  k_scan_apply<<<grid, kScanThreads, 0, st>>>(in, out, n_max, n_dev, *partial);
+  launch_k(k_scan_reduce, grid, kScanThreads, 0, st, in, n_max, n_dev, *partial);
+  launch_k(k_scan_partials, 1, 1024, 0, st, *partial, n_max, n_dev, total);
+  launch_k(k_scan_apply, grid, kScanThreads, 0, st, in, out, n_max, n_dev, *partial);
   PVDB_CHECK_LAUNCHES("scan", 3);
   return PVDB_OK;
 }
@@ -246,6 +250,7 @@ static OsLayout os_layout(int64_t n_max, int npass) {
 
 __global__ void k_os_init(int64_t n_max, const uint32_t* n_dev, int npass, int64_t ntiles_max,
                           uint32_t* scratch, OsLayout L) {
+  grid_dep_sync();
   const int64_t n = eff_size(n_max, n_dev);
   const int64_t ntiles = (n + kRsTile - 1) / kRsTile;
   const int64_t per = ntiles * kRsBins;
@@ -265,6 +270,7 @@ __global__ void k_os_init(int64_t n_max, const uint32_t* n_dev, int npass, int64
 
 __global__ void __launch_bounds__(kRsThreads)
     k_os_hist(const uint32_t* __restrict__ keys, int npass, uint32_t* scratch, OsLayout L) {
+  grid_dep_sync();
   __shared__ uint32_t h[4][kRsBins];
   const int64_t n = scratch[L.n];
   for (int q = threadIdx.x; q < 4 * kRsBins; q += blockDim.x) (&h[0][0])[q] = 0u;
@@ -285,6 +291,7 @@ __global__ void __launch_bounds__(kRsThreads)
     k_os_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, int pass,
                  uint32_t* scratch, OsLayout L, uint32_t* kout, uint32_t* vout, uint32_t* err,
                  uint32_t spin_max, int hold_first) {
+  grid_dep_sync();
   // an earlier pass gave up: its order is wrong, so this one does nothing
   if (*(volatile uint32_t*)err) return;
   __shared__ uint32_t wh[kRsWarps][kRsBins];
@@ -405,18 +412,17 @@ int radix_sort_pairs_dev(ReduceScratch& rs, int64_t n_max, const uint32_t* n_dev
   const int g_init = int(std::min<int64_t>(
       std::max<int64_t>(ceil_div(int64_t(npass) * L.ntiles_max * kRsBins, 256), 1),
       int64_t(num_sms()) * 8));
-  k_os_init<<<g_init, 256, 0, st>>>(n_max, n_dev, npass, L.ntiles_max, sc, L);
+  launch_k(k_os_init, g_init, 256, 0, st, n_max, n_dev, npass, L.ntiles_max, sc, L);
   PVDB_CHECK_LAUNCH("k_os_init");
   const int g_hist = int(std::min<int64_t>(ceil_div(n_max, kRsThreads), int64_t(num_sms()) * 4));
-  k_os_hist<<<g_hist, kRsThreads, 0, st>>>(rs.keys[0], npass, sc, L);
+  launch_k(k_os_hist, g_hist, kRsThreads, 0, st, rs.keys[0], npass, sc, L);
   PVDB_CHECK_LAUNCH("k_os_hist");
   const int grid = int(std::min<int64_t>(L.ntiles_max, int64_t(num_sms()) * 4));
   int cur = 0;
   for (int p = 0; p < npass; ++p) {
-    k_os_scatter<<<grid, kRsThreads, 0, st>>>(rs.keys[cur],
-                                              (p == 0 && iota_vals) ? nullptr : rs.vals[cur], p,
-                                              sc, L, rs.keys[cur ^ 1], rs.vals[cur ^ 1], errp,
-                                              spin, hold);
+    launch_k(k_os_scatter, grid, kRsThreads, 0, st, rs.keys[cur],
+             (p == 0 && iota_vals) ? nullptr : rs.vals[cur], p, sc, L, rs.keys[cur ^ 1],
+             rs.vals[cur ^ 1], errp, spin, hold);
     PVDB_CHECK_LAUNCH("k_os_scatter");
     cur ^= 1;
   }
@@ -503,6 +509,7 @@ int read_wait_status(const uint32_t* status, cudaStream_t st, const char* what) 
 
 __global__ void k_point_keys(GridView gv, const float* __restrict__ xs, const float* __restrict__ ys,
                              const float* __restrict__ zs, int64_t n, uint32_t* keys) {
+  grid_dep_sync();
   const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (p >= n) return;
   emit_corner_keys(gv, xs[p], ys[p], zs[p], keys, p);
@@ -543,7 +550,7 @@ extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const flo
   const int64_t nc = n * 8;
   int rc = reduce_reserve(g, nc);
   if (rc) return rc;
-  k_point_keys<<<ceil_div(n, 256), 256, 0, st>>>(g->view(), dx, dy, dz, n, g->red.keys[0]);
+  launch_k(k_point_keys, ceil_div(n, 256), 256, 0, st, g->view(), dx, dy, dz, n, g->red.keys[0]);
   PVDB_CHECK_LAUNCH("k_point_keys");
   int buf = 0;
   uint32_t* status = nullptr;
@@ -551,9 +558,9 @@ extern "C" int pvdb_grid_sample_backward(pvdb_grid g, const float* xs, const flo
   if (rc) return rc;
   PointSrc src{dx, dy, dz, dg, g->C};
   const int grid = int(std::min<int64_t>(ceil_div(nc, 256), int64_t(num_sms()) * 16));
-  k_segment_reduce<PointSrc><<<grid, 256, 0, st>>>(
-      g->red.keys[buf], g->red.vals[buf], nc, nullptr, src, g->C == 1 ? g->d_grad : nullptr,
-      g->C == 1 ? nullptr : g->d_grad, g->C, g->d_touched, g->d_touched, status);
+  launch_k(k_segment_reduce<PointSrc>, grid, 256, 0, st, g->red.keys[buf], g->red.vals[buf], nc,
+           nullptr, src, g->C == 1 ? g->d_grad : nullptr, g->C == 1 ? nullptr : g->d_grad, g->C,
+           g->d_touched, g->d_touched, status);
   PVDB_CHECK_LAUNCH("k_segment_reduce");
   g->tlist_valid = false;
   // the call waits for its stream (as the reference's backward does) so that a

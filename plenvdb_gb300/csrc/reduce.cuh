@@ -120,6 +120,7 @@ __global__ void k_segment_reduce(const uint32_t* __restrict__ skeys,
                                  const uint32_t* n_dev, Src src, float* grad_d, float* grad_c,
                                  int Cc, uint8_t* touched_d, uint8_t* touched_c,
                                  const uint32_t* status = nullptr) {
+  grid_dep_sync();
   if (status && *status) return;  // the sort gave up a wait: its order is wrong
   const int64_t n = n_dev ? min(n_max, (int64_t)*n_dev) : n_max;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;

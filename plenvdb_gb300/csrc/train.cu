@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256)
     k_loss(MarchW W, const float* __restrict__ rgb, float* rgbm_out,
            const float* __restrict__ target, int R, LossW L, float* grad_rgb, float* grad_w,
            float* grad_last, float* loss_part, float* loss) {
+  grid_dep_sync();
   __shared__ float red[256];
   __shared__ bool last_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(256)
                   const float* __restrict__ rd, const float* __restrict__ vd,
                   const float* __restrict__ tgt, int64_t n3, float* scal, float ss_d, float ss_k,
                   float ss_n) {
+  grid_dep_sync();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     scal[0] = ss_d;
     scal[1] = ss_k;
@@ -297,9 +299,8 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   if (rc) return rc;
   if (t.prof) prof_mark(st, 3);
   LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
-  k_loss<<<ceil_div(n_rays, 8), 256, 0, st>>>(m->w, m->t_rgb, m->t_rgb_marched, t.tgt, n_rays, L,
-                                              m->t_grad_rgb, m->t_grad_w, m->t_grad_last,
-                                              m->t_loss_part, t.loss);
+  launch_k(k_loss, ceil_div(n_rays, 8), 256, 0, st, m->w, m->t_rgb, m->t_rgb_marched, t.tgt, n_rays,
+           L, m->t_grad_rgb, m->t_grad_w, m->t_grad_last, m->t_loss_part, t.loss);
   PVDB_CHECK_LAUNCH("k_loss");
   if (t.prof) prof_mark(st, 4);
   // The march backward's density path and the grouping of the kept samples by
@@ -570,9 +571,9 @@ extern "C" int pvdb_train_step(pvdb_march m, pvdb_opt density_opt, pvdb_opt k0_o
   t.ss[2] = adam_step_size(*net->lr, cfg->rgbnet_beta1, cfg->rgbnet_beta2, *net->step);
   if (graph_ok) {
     const int64_t R3 = int64_t(n_rays) * 3;
-    k_step_inputs<<<int(std::min<int64_t>(ceil_div(4 * R3, 256), int64_t(2 * num_sms()))), 256,
-                    0, st>>>(m->g_in, rays_o, rays_d, viewdirs, target, R3, m->g_scal, t.ss[0],
-                             t.ss[1], t.ss[2]);
+    launch_k(k_step_inputs, int(std::min<int64_t>(ceil_div(4 * R3, 256), int64_t(2 * num_sms()))),
+             256, 0, st, m->g_in, rays_o, rays_d, viewdirs, target, R3, m->g_scal, t.ss[0], t.ss[1],
+             t.ss[2]);
     PVDB_CHECK_LAUNCH("k_step_inputs");
     PVDB_CHECK_CUDA(cudaGraphLaunch(m->g_exec, st));
     count_launches(int(m->g_launches));

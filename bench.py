@@ -819,6 +819,7 @@ def run_large(args, steps=10, warmup=3):
             roof = roofline(sm, tr, scfg, R=R)
             res[tag]["stage_ms"] = sm
             res[tag]["stages"] = roof["stages"]
+            res[tag]["adam_voxels"] = roof["adam_voxels"]
             res[tag]["leaf_staging"] = leaf_staging_compare(tr, batches, nb, None, None, sm, n=5)
         del tr, dg, kg
     res["speedup_bf16"] = res["bf16"]["it_s"] / res["fp32"]["it_s"]

@@ -222,6 +222,66 @@ class ClockSampler:
                 "samples_inside": len(inside), "interval_ms": self.INTERVAL_MS}
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (ctypes on the
+    driver's libnvidia-ml, read-only queries) every millisecond from a thread
+    while the timed region runs: a region of a few tens of milliseconds gets
+    tens of samples, where nvidia-smi's interval gets none."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes
+        self.ok = False
+        self.samples = []
+        try:
+            self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.nv.nvmlInit_v2() != 0:
+                return
+            self.h = ctypes.c_void_p()
+            if self.nv.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h)) != 0:
+                return
+            self.reason_fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = ctypes.c_uint()
+            self.max_mhz = (float(mx.value) if self.nv.nvmlDeviceGetMaxClockInfo(
+                self.h, 1, ctypes.byref(mx)) == 0 else None)
+            self.ok = True
+        except Exception:
+            self.ok = False
+
+    def _run(self):
+        import ctypes
+        mhz, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.halt:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(mhz)) == 0 and \
+                    self.reason_fn(self.h, ctypes.byref(rs)) == 0:
+                self.samples.append((float(mhz.value), int(rs.value)))
+            time.sleep(0.001)
+
+    def begin(self):
+        if not self.ok:
+            return
+        self.halt = False
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def end(self):
+        if not self.ok:
+            return {"samples": 0, "note": "NVML unavailable"}
+        self.halt = True
+        self.thread.join(timeout=1.0)
+        mask = 0
+        for _, r in self.samples:
+            mask |= r
+        return {"samples": len(self.samples),
+                "sm_mhz": float(np.median([m for m, _ in self.samples])) if self.samples else None,
+                "sm_mhz_min": min((m for m, _ in self.samples), default=None),
+                "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(n for b, n in self.REASONS.items() if mask & b)}
+
+
 # ------------------------------------------------------------------ setup
 def make_problem(device_seed=0):
     import torch
@@ -294,8 +354,10 @@ def run_ours(args):
     launches0 = lib.pvdb_launch_count()
     if ws_ > 1:
         dist.barrier()
+    nvml = NvmlSampler(local)
     torch.cuda.synchronize()
     clocks.begin()
+    nvml.begin()
     t_wall = time.perf_counter()
     for i in range(args.steps):
         flush_l2(flush)
@@ -304,9 +366,16 @@ def run_ours(args):
         evs[i][1].record(st)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
+    nv_clk = nvml.end()
     clocks.end()
     launches = lib.pvdb_launch_count() - launches0
     clk = clocks.stop()
+    clk["nvml_inside"] = nv_clk
+    if nv_clk.get("samples"):
+        # the in-region samples are the record; nvidia-smi's stay beside them
+        clk["sm_mhz"] = nv_clk["sm_mhz"]
+        clk["sm_max_mhz"] = nv_clk["sm_max_mhz"] or clk["sm_max_mhz"]
+        clk["reasons"] = sorted(set(clk["reasons"]) | set(nv_clk["reasons"]))
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
     value, ms_per_step = replica_throughput(step_ms, args.steps, ws_)
     stage_ms = stage_profile(tr, dev, nb, flush, args)
@@ -560,12 +629,14 @@ RGBNET_FWD_ROW, RGBNET_FWD_RAY, RGBNET_BWD_ROW = 36608.0, 6912.0, 73216.0
 # (cold L2; the grids are L2-resident in the live step, so these are the
 # bytes a launch pulls from HBM, not the algorithmic bytes above)
 NCU_TRAFFIC = {
-    "march_fwd": 2.137e6 + 11.177e6,   # k_march_alpha + k_march_chain
-    "k0_gather": 13.279e6,             # k_march_k0_x
-    "rgbnet_fwd": 15.113e6,            # k_mlp_fwd_tc
-    "rgbnet_bwd": 19.026e6,            # k_mlp_bwd_tc
-    "march_bwd": 7.266e6,              # k_march_bwd
-    "voxel_gather": 27.686e6,          # k_voxel_gather
+    "march_fwd": 2.133e6 + 11.115e6,   # k_march_alpha + k_march_chain
+    "k0_gather": 9.627e6,              # k_march_k0_x
+    "rgbnet_fwd": 14.691e6,            # k_mlp_fwd_tc
+    "rgbnet_bwd": 18.388e6,            # k_mlp_bwd_tc
+    "march_bwd": 7.145e6,              # k_march_bwd
+    "voxel_gather": 11.030e6 + 26.148e6,  # k_group_records + k_voxel_gather
+    "tv": 12.608e6,                    # k_tv_terms_c12 (the density grid's k_tv_terms not captured)
+    "voxel_adam": 52.651e6 + 3.142e6 + 6.055e6,  # k_vdb_adam_c12 + k_vdb_adam1
 }
 
 

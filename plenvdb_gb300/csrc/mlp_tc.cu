@@ -747,6 +747,15 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       if (xissued[b] > xwaits[b]) tc::mbar_wait(xbar + b, xwaits[b] & 1u, spin_max);
   }
   __syncthreads();
+  // The dW1 and dW0|db0 rows are staged in shared memory (the slots' space,
+  // free now) with odd row strides, so that thread n's row writes hit
+  // distinct banks, and then written out row-major by consecutive threads:
+  // coalesced stores, not one 32-byte sector per thread and store.
+  constexpr int kS1 = kW + 1;   // dW1 row stride (floats)
+  constexpr int kS0 = kXK + 1;  // dW0|db0 row stride
+  float* s1 = reinterpret_cast<float*>(sm);
+  float* s0 = s1 + kW * kS1;
+  static_assert((kW * kS1 + kW * kS0) * 4 <= kBX, "staging fits in the slots");
   if (failed) {
     for (int64_t i = tid; i < P; i += kBwdThreads) pw0[i] = 0.f;
   } else if (warp < 8) {
@@ -756,8 +765,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     const int n = 32 * q4 + lane;
     const uint32_t tl = tmem + (uint32_t(32 * q4) << 16);
     float v[16];
-    // (a CTA's partials start at blockIdx.x * P floats and P is odd: scalar stores)
-    float* w1row = pw1 + n * kW;
+    float* s1row = s1 + n * kS1;
+    float* s0row = s0 + n * kS0;
     if (half == 0) {
       tc::tmem_ld16(tl + kTW2, v);
 #pragma unroll
@@ -766,36 +775,38 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
       for (int j = 0; j < 2; ++j) {  // dW0|db0 columns 0..31
         tc::tmem_ld16(tl + kTW0 + 16 * j, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int qq = 16 * j + i;
-          if (qq < a.din) pw0[n * a.din + qq] = v[i];
-          else if (qq == a.din) pb0[n] = v[i];
-        }
+        for (int i = 0; i < 16; ++i) s0row[16 * j + i] = v[i];
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {  // dW1 columns 0..63
         tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w1row[16 * j + i] = v[i];
+        for (int i = 0; i < 16; ++i) s1row[16 * j + i] = v[i];
       }
       tc::tmem_ld16(tl + kTW1 + 128, v);  // db1
       pb1[n] = v[0];
     } else {
       tc::tmem_ld16(tl + kTW0 + 32, v);  // dW0|db0 columns 32..47
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int qq = 32 + i;
-        if (qq < a.din) pw0[n * a.din + qq] = v[i];
-        else if (qq == a.din) pb0[n] = v[i];
-      }
+      for (int i = 0; i < 16; ++i) s0row[32 + i] = v[i];
 #pragma unroll
       for (int j = 4; j < 8; ++j) {  // dW1 columns 64..127
         tc::tmem_ld16(tl + kTW1 + 16 * j, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w1row[16 * j + i] = v[i];
+        for (int i = 0; i < 16; ++i) s1row[16 * j + i] = v[i];
       }
     }
   }
+  __syncthreads();
+  if (!failed) {
+    for (int i = tid; i < kW * kW; i += kBwdThreads) pw1[i] = s1[(i >> 7) * kS1 + (i & 127)];
+    for (int i = tid; i < kW * a.din; i += kBwdThreads) {
+      const int n = i / a.din;
+      pw0[i] = s0[n * kS0 + (i - n * a.din)];
+    }
+    if (tid < kW) pb0[tid] = s0[tid * kS0 + a.din];
+  }
+
   if (!failed) {
     // db2: fixed-order sum of the per-row partials of both slots (the first X
     // buffer as scratch: no copy or MMA touches it any more)

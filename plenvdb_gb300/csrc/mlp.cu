@@ -392,21 +392,8 @@ __global__ void __launch_bounds__(256)
   const int u = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t i = blockIdx.x * 32ll + lane;
   float acc = 0.f;
-  if (i < P) {
-    // the same in-order sum, with four partials' loads in flight at a time
-    int c = u;
-    for (; c + 24 < nparts; c += 32) {
-      const float x0 = __ldg(wpart + int64_t(c) * P + i);
-      const float x1 = __ldg(wpart + int64_t(c + 8) * P + i);
-      const float x2 = __ldg(wpart + int64_t(c + 16) * P + i);
-      const float x3 = __ldg(wpart + int64_t(c + 24) * P + i);
-      acc += x0;
-      acc += x1;
-      acc += x2;
-      acc += x3;
-    }
-    for (; c < nparts; c += 8) acc += __ldg(wpart + int64_t(c) * P + i);
-  }
+  if (i < P)
+    for (int c = u; c < nparts; c += 8) acc += __ldg(wpart + int64_t(c) * P + i);
   part[u][lane] = acc;
   __syncthreads();
   if (u == 0 && i < P)

@@ -54,7 +54,7 @@ struct MarchW {
   // leaf-staging test hook, [3] error flags (1 samples_cap exceeded,
   // 2 tensor-core wait, 4 ray-offset look-back wait, 8 leaf-staging copy
   // wait), [4] samples evaluated, [5] samples grouped by cell (backward),
-  // [6] k_march_chain ray counter, [7] train-step loss block counter,
+  // [6] k_march_chain ray counter, [7] unused,
   // [8..11] voxels visited / updated by the density and k0 Adam of the last
   // profiled train step
   uint32_t* totals;

@@ -40,8 +40,8 @@ constexpr uint32_t kSmX = kPackFwdBytes;              // two X tiles [128 x 48] 
 constexpr uint32_t kSmH = kSmX + 2 * kXTile;          // H tile [128 x 128] bf16
 constexpr uint32_t kSmB1 = kSmH + 128 * 128 * 2;      // b1 f32[128]
 constexpr uint32_t kSmB2 = kSmB1 + 128 * 4;           // b2 f32[16]
-constexpr uint32_t kSmBar = kSmB2 + 16 * 4;           // mbarriers: MMA, X0, X1 (24 B)
-constexpr uint32_t kSmTmem = kSmBar + 24;             // TMEM base address (4 B)
+constexpr uint32_t kSmBar = kSmB2 + 16 * 4;           // mbarriers: MMA, X0, X1, weights (32 B)
+constexpr uint32_t kSmTmem = kSmBar + 32;             // TMEM base address (4 B)
 constexpr uint32_t kSmFlag = kSmTmem + 4;             // timeout flag (4 B)
 constexpr uint32_t kSmFwdBytes = kSmFlag + 16;
 static_assert(2 * kSmFwdBytes <= 228 * 1024, "two forward CTAs must fit on an SM");
@@ -176,19 +176,19 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kSmFlag);
   float* b1s = reinterpret_cast<float*>(sm + kSmB1);
   float* b2s = reinterpret_cast<float*>(sm + kSmB2);
-  {
-    const int4* src = reinterpret_cast<const int4*>(blob);
-    int4* dst = reinterpret_cast<int4*>(sm);
-    for (int i = tid; i < int(kPackFwdBytes / 16); i += kTcThreads) dst[i] = __ldg(src + i);
-  }
   if (tid < 128) b1s[tid] = a.b1[tid];
   if (tid < 16) b2s[tid] = tid < 3 ? a.b2[tid] : 0.f;
   uint64_t* xbar = bar + 1;  // X tile barriers, one per buffer
+  uint64_t* wbar = bar + 3;  // the weight tiles
   if (tid == 0) {
     *flag = 0;
     tc::mbar_init(bar, 1);
     tc::mbar_init(xbar, 1);
     tc::mbar_init(xbar + 1, 1);
+    tc::mbar_init(wbar, 1);
+    // the packed weights (48 KB) in one bulk copy, beside the first X tile's
+    tc::mbar_expect_tx(wbar, kPackFwdBytes);
+    tc::bulk_g2s(sm, blob, kPackFwdBytes, wbar);
     x_fetch(sm + kSmX, xt, blockIdx.x, xbar);
   }
   if (warp == 0) {
@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     ok = wait_or_flag(xbar + b, xph[b], flag, err);
     if (!ok) break;
     xph[b] ^= 1u;
+    if (it == 0 && !(ok = wait_or_flag(wbar, 0, flag, err))) break;
     if (tid == 0) {
       tc::fence_after();
 #pragma unroll
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     tc::mbar_wait(bar, phase ^ 1u, kWaitIters);
     tc::mbar_wait(xbar, xph[0], kWaitIters);
     tc::mbar_wait(xbar + 1, xph[1], kWaitIters);
+    tc::mbar_wait(wbar, 0, kWaitIters);
   }
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);

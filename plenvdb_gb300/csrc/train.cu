@@ -51,15 +51,12 @@ struct LossW {
 // Per ray (warp per ray): the composite rgb_marched = sum_rows w*rgb + T*bg
 // (the same arithmetic as k_composite_fwd), the losses and their gradients
 // w.r.t. rgb_marched (folded into the per-row colour gradient), alphainv_last
-// and the colour weights. The last block to finish sums the per-ray loss
-// partials in a fixed order (a counter in totals[7] picks it and is reset).
+// and the colour weights; each ray's loss partial (k_loss_sum adds them).
 __global__ void __launch_bounds__(256)
     k_loss(MarchW W, const float* __restrict__ rgb, float* rgbm_out,
            const float* __restrict__ target, int R, LossW L, float* grad_rgb, float* grad_w,
-           float* grad_last, float* loss_part, float* loss) {
+           float* grad_last, float* loss_part) {
   grid_dep_sync();
-  __shared__ float red[256];
-  __shared__ bool last_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * 8 + warp;
   if (r < R) {
@@ -118,15 +115,15 @@ __global__ void __launch_bounds__(256)
                      L.ent * ent / float(R) + L.rgbper * per / float(R);
     }
   }
-  // the last block sums the partials
-  __threadfence();  // this block's partials are visible device-wide before its ticket
-  __syncthreads();
-  if (threadIdx.x == 0) last_s = atomicAdd(W.totals + 7, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last_s) return;
-  __threadfence();
-  // thread t sums partials t, t + 256, ... in that order; eight L2 loads are
-  // in flight at a time (the other blocks' partials bypass L1)
+}
+
+// One block sums the rays' loss partials: thread t sums partials t, t + 256,
+// ... in that order (eight loads in flight at a time), then a fixed tree.
+// It runs beside the backward (only the step's reported loss needs it).
+__global__ void __launch_bounds__(256)
+    k_loss_sum(const float* __restrict__ loss_part, int R, float* loss) {
+  grid_dep_sync();
+  __shared__ float red[256];
   float acc = 0.f;
   for (int i0 = threadIdx.x; i0 < R; i0 += 8 * blockDim.x) {
     float v[8];
@@ -145,10 +142,7 @@ __global__ void __launch_bounds__(256)
     if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    loss[0] = red[0];
-    W.totals[7] = 0u;
-  }
+  if (threadIdx.x == 0) loss[0] = red[0];
 }
 
 static int train_reserve(pvdb_march_s* m, int C) {
@@ -300,8 +294,17 @@ static int train_launches(const TrainArgs& t, cudaStream_t st) {
   if (t.prof) prof_mark(st, 3);
   LossW L{cfg->weight_main, cfg->weight_entropy_last, cfg->weight_rgbper, cfg->march.bg};
   launch_k(k_loss, ceil_div(n_rays, 8), 256, 0, st, m->w, m->t_rgb, m->t_rgb_marched, t.tgt, n_rays,
-           L, m->t_grad_rgb, m->t_grad_w, m->t_grad_last, m->t_loss_part, t.loss);
+           L, m->t_grad_rgb, m->t_grad_w, m->t_grad_last, m->t_loss_part);
   PVDB_CHECK_LAUNCH("k_loss");
+  // the loss sum beside the backward (side[1] is free until the Adam updates)
+  cudaStream_t lst = st;
+  if (!t.prof) {
+    PVDB_CHECK_CUDA(cudaEventRecord(m->side_ev[0], st));
+    PVDB_CHECK_CUDA(cudaStreamWaitEvent(m->side[1], m->side_ev[0], 0));
+    lst = m->side[1];
+  }
+  launch_k(k_loss_sum, 1, 256, 0, lst, m->t_loss_part, n_rays, t.loss);
+  PVDB_CHECK_LAUNCH("k_loss_sum");
   if (t.prof) prof_mark(st, 4);
   // The march backward's density path and the grouping of the kept samples by
   // cell need only the weight / alphainv_last gradients: they run beside the

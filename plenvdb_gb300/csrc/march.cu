@@ -381,16 +381,30 @@ __global__ void __launch_bounds__(kMarchThreads)
     }
   }
   // colour rows: global row m = color_off + rank, the row record, k_row = m
-  for (int i = lane; i < nk; i += 32) {
-    const int64_t t = sbase + i;
-    const int32_t rank = W.k_row[t];
-    if (rank < 0) continue;
-    const int64_t m = int64_t(ex_c) + rank;
-    W.r_w[m] = W.k_w[t];
-    W.r_alpha[m] = W.k_alpha[t];
-    W.r_ray[m] = r;
-    W.r_step[m] = W.k_step[t] & 0x7fffffff;
-    W.k_row[t] = int32_t(m);
+  // (the kept records of four 32-sample chunks are loaded together)
+  for (int i0 = lane; i0 < nk; i0 += 4 * 32) {
+    int32_t rank[4], step[4];
+    float wv[4], av[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + 32 * u;
+      const int64_t t = sbase + i;
+      rank[u] = i < nk ? W.k_row[t] : -1;
+      wv[u] = i < nk ? W.k_w[t] : 0.f;
+      av[u] = i < nk ? W.k_alpha[t] : 0.f;
+      step[u] = i < nk ? W.k_step[t] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (rank[u] < 0) continue;
+      const int64_t t = sbase + i0 + 32 * u;
+      const int64_t m = int64_t(ex_c) + rank[u];
+      W.r_w[m] = wv[u];
+      W.r_alpha[m] = av[u];
+      W.r_ray[m] = r;
+      W.r_step[m] = step[u] & 0x7fffffff;
+      W.k_row[t] = int32_t(m);
+    }
   }
 }
 

@@ -321,14 +321,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 //   stage  MMAs (issuer)                                   epilogue (the slot's warps)
 //   S0     Z0 = X.W0f^T                -> A                E0  H0 = relu(Z0)
 //   S1     Z1 = H0.W1^T                -> A                E1  H1 = relu(Z1 + b1), dl
-//   S2     dW2 += H1^T.dl                                  E2  dZ1 over H1
+//   S2     dZ1' = dl.W2 -> A;  dW2 += H1^T.dl             E2  dZ1 = dZ1'*[H1 > 0], over H1
 //   S3     dH0 = dZ1.W1 -> A;  dW1|db1 += dZ1^T.[H0|1]     E3  dZ0 = dH0*[H0 > 0], over dZ1
 //   S4     gk0 = dZ0.W0k -> G; dW0|db0 += dZ0^T.X          E4  gk0 -> global
-// dl has three nonzero columns, so dZ1 = (dl.W2)*[H1 > 0] is formed on the
-// CUDA cores (three FMAs per element, from the BF16-rounded operands the MMA
-// would read), in registers after E1 has released H1 and dl to S2: the
-// arithmetic overlaps the dW2 MMA, and E2 only stores dZ1 once S2 is done. A ones
-// column in H0 and in X turns the bias sums into one more MMA column. W1 and
+// dl has three nonzero columns of the MMA's 16; dZ1' is one K = 16 MMA whose
+// B operand is W2's first 8 rows (rows 3..7 zero) followed, as the second
+// 8 of K, by finite weights that meet dl's zero columns. E2 masks it with the
+// relu of H1, which E1 keeps in registers. A ones column in H0 and in X turns
+// the bias sums into one more MMA column. W1 and
 // W0k are the forward's K-major weight tiles read through MN-major
 // descriptors (no transposed copies). An epilogue signals the issuer through
 // its slot's mbarrier (256 arrivals) after a proxy fence (its shared-memory
@@ -343,24 +343,25 @@ constexpr int kBwdEpiWarps = 8;             // per slot: 4 lane quarters x 2 col
 constexpr int kBwdThreads = (2 * kBwdEpiWarps + 1) * 32;  // + the issuer warp: 544
 constexpr int kBwdIssuer = 2 * kBwdEpiWarps;  // warp index of the issuer
 constexpr int kBwdXBufs = 3;                // X tiles in flight: tile j uses buffer j % 3
-// dZ1 column groups (8 columns each) formed while the dW2 MMA runs; the other
-// two after it (holding all eight across the wait spills registers)
-constexpr int kDz1Early = 6;
 constexpr uint32_t kSlH0 = 0;               // H0 [128 r][144 k], col 128 = 1
 constexpr uint32_t kSlH1 = kSlH0 + 128 * 144 * 2;  // H1, then dZ1, then dZ0 [128 r][128 n]
 constexpr uint32_t kSlDl = kSlH1 + 128 * 128 * 2;  // dl [128 r][16 c]
 constexpr uint32_t kSlot = kSlDl + 128 * 16 * 2;   // 73728 B per slot
 constexpr uint32_t kBX = 2 * kSlot;                // X x 3 [128 r][48 q]: k0 | PE | 1 | 0
-constexpr uint32_t kBW0f = kBX + kBwdXBufs * kXTile;  // W0f [128 n][48 q]
+// W2p rows 0..7 [8 c][128 k] (K-major, as in the blob): the B operand of
+// dZ1 = dl . W2, read MN-major; its K = 16 reaches 2 KB past the rows, into
+// W0f (finite values that meet dl's zero columns 8..15)
+constexpr uint32_t kBW2 = kBX + kBwdXBufs * kXTile;
+constexpr uint32_t kBW0f = kBW2 + 8 * 128 * 2;     // W0f [128 n][48 q]
 constexpr uint32_t kBW1 = kBW0f + 128 * kXK * 2;   // W1  [128 n][128 k]
-constexpr uint32_t kBW2f = kBW1 + 128 * 128 * 2;   // W2 as f32 [3 c][128 n] (BF16 values)
-constexpr uint32_t kBB1 = kBW2f + 3 * 128 * 4;     // b1 f32[128]
+constexpr uint32_t kBB1 = kBW1 + 128 * 128 * 2;    // b1 f32[128]
 constexpr uint32_t kBBar = kBB1 + 128 * 4;         // mma[2], epi[2], x[3], drain, weights
 constexpr uint32_t kBTmem = kBBar + 80;
 constexpr uint32_t kBFlag = kBTmem + 4;
 constexpr uint32_t kBXIssued = kBFlag + 4;         // X copies started, per buffer
 constexpr uint32_t kSmBwdBytes = kBXIssued + 12;
 constexpr uint32_t kBwdWBytes = kOffW2;            // W0f and W1 of the blob (45056 B)
+constexpr uint32_t kBwdW2Bytes = 8 * 128 * 2;      // W2p rows 0..7 of the blob
 static_assert(kSlot % 1024 == 0, "slot tiles keep their alignment");
 static_assert(kBW1 - kBW0f == kOffW1 - kOffW0 && kBwdWBytes % 16 == 0, "W0f, W1 as in the blob");
 static_assert(kSmBwdBytes <= 232448, "backward CTA exceeds 227 KB of shared memory");
@@ -446,10 +447,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
   uint32_t* flag = reinterpret_cast<uint32_t*>(sm + kBFlag);
   uint32_t* xissued = reinterpret_cast<uint32_t*>(sm + kBXIssued);
   float* b1s = reinterpret_cast<float*>(sm + kBB1);
-  float* w2f = reinterpret_cast<float*>(sm + kBW2f);
   if (tid < 128) b1s[tid] = a.b1[tid];
-  // W2 at the BF16 precision of the forward's operand, for dZ1 = dl . W2
-  if (tid < 3 * 128) w2f[tid] = __bfloat162float(__float2bfloat16_rn(a.w2[tid]));
   if (tid < 256) {
     // H0 columns 128..143 of both slots: [1, 0 x 15] for every row
     const int s = tid >> 7, r = tid & 127;
@@ -468,8 +466,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     tc::mbar_init(dbar, 1);
     tc::mbar_init(wbar, 1);
     // W0f and W1 of the forward's blob in one bulk copy
-    tc::mbar_expect_tx(wbar, kBwdWBytes);
+    tc::mbar_expect_tx(wbar, kBwdWBytes + kBwdW2Bytes);
     tc::bulk_g2s(sm + kBW0f, blob, kBwdWBytes, wbar);
+    tc::bulk_g2s(sm + kBW2, blob + kOffW2, kBwdW2Bytes, wbar);
     // the X tiles of the first three tiles
     for (int b = 0; b < kBwdXBufs; ++b) {
       xissued[b] = b < nj ? 1u : 0u;
@@ -534,7 +533,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
 #pragma unroll 1
               for (int q = 0; q < 8; ++q, da += 256 >> 4, db += 256 >> 4)
                 tc::mma_bf16(tA, da, db, id_kk, q > 0);
-            } else if (k == 2) {  // dW2 += H1^T . dl
+            } else if (k == 2) {  // dZ1' = dl . W2 -> A;  dW2 += H1^T . dl
+              tc::mma_bf16(tA, tc::make_desc(sl + kSlDl, 128, 256),
+                           tc::make_desc(sb + kBW2, 2048, 128), id_kn, 0u);
               uint64_t da = tc::make_desc(sl + kSlH1, 2048, 128);
               uint64_t db = tc::make_desc(sl + kSlDl, 256, 128);
 #pragma unroll 1
@@ -635,15 +636,11 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
           *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128)) = hp[cb / 8 + c];
         }
       }
-      // dl at the BF16 precision of the dW2 operand; E2 reuses the same values
-      float dlb[3];
+      // dl, in BF16 the A operand of dZ1' = dl . W2 and the B operand of dW2
       {
         float d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          d[c] = gv[c] * (1.f - yv[c]) * yv[c];
-          dlb[c] = __bfloat162float(__float2bfloat16_rn(d[c]));
-        }
+        for (int c = 0; c < 3; ++c) d[c] = gv[c] * (1.f - yv[c]) * yv[c];
         if (half == 0) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) db2[c] += d[c];
@@ -653,35 +650,19 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         }
       }
       epi_done(ebar + s);
-      // dZ1 = (dl . W2) * [H1 > 0] on the CUDA cores (dl has three nonzero
-      // columns), in registers while the dW2 MMA reads H1
-#pragma unroll
-      for (int g = 0; g < kDz1Early; ++g) {
-        const int n0 = c0 + 8 * g;
-        float v[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-          v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
-                           __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
-        hp[g] = mask_pack(v, hp[g]);
-      }
-      // ---- E2: dZ1 over H1 once the dW2 MMA has read it
+      // ---- E2: dZ1 = dZ1' * [H1 > 0] over H1 once the dW2 MMA has read it
       if (!(ok = bwait(mbar + s, mph, flag, err, spin_max))) break;
       mph ^= 1u;
       tc::fence_after();
 #pragma unroll
-      for (int g = kDz1Early; g < 8; ++g) {
-        const int n0 = c0 + 8 * g;
-        float v[8];
+      for (int cb = 0; cb < 64; cb += 32) {
+        float v[32];
+        tc::tmem_ld32(tA + uint32_t(cb), v);
 #pragma unroll
-        for (int e = 0; e < 8; ++e)
-          v[e] = __fmaf_rn(dlb[2], w2f[256 + n0 + e],
-                           __fmaf_rn(dlb[1], w2f[128 + n0 + e], __fmul_rn(dlb[0], w2f[n0 + e])));
-        hp[g] = mask_pack(v, hp[g]);
+        for (int c = 0; c < 4; ++c)
+          *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + cb + 8 * c, 128)) =
+              mask_pack(v + 8 * c, hp[cb / 8 + c]);
       }
-#pragma unroll
-      for (int g = 0; g < 8; ++g)
-        *reinterpret_cast<uint4*>(h1 + tc::kmaj(row, c0 + 8 * g, 128)) = hp[g];
       epi_done(ebar + s);
       // ---- E3: dZ0 = dH0 * [H0 > 0], over dZ1 (the thread's own H0 columns,
       // written by its E0, are read before the wait)

@@ -115,20 +115,27 @@ __global__ void __launch_bounds__(256)
     const int vox = int(i & 511);
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
     const bool active = (__ldg(g.mask + leaf * 8 + (vox >> 6)) >> (vox & 63)) & 1ull;
-    float gr = active ? g.grad[slot] : 0.f;
-    if (tv && gr != 0.f) gr = gr + tv[slot];  // deferred sparse TV
+    // the voxel's gradient, TV term, moments and value are loaded together
+    float gr = 0.f, tt = 0.f, ms = 0.f, vs = 0.f, old = 0.f;
+    if (active) {
+      gr = g.grad[slot];
+      if (tv) tt = tv[slot];
+      ms = m[slot];
+      vs = v[slot];
+      old = g.data[slot];
+    }
+    if (tv && gr != 0.f) gr = gr + tt;  // deferred sparse TV
     bool grew = false;
     float nv = 0.f;
     n_act += active;
     if (active && !(mode == 1 && gr == 0.f)) {
       ++n_upd;
       const float lrf = mode == 2 ? perlr[slot] : 1.f;
-      const float mn = b0 * m[slot] + (1 - b0) * gr;
-      const float vn = b1 * v[slot] + (1 - b1) * gr * gr;
+      const float mn = b0 * ms + (1 - b0) * gr;
+      const float vn = b1 * vs + (1 - b1) * gr * gr;
       m[slot] = mn;
       v[slot] = vn;
       const float num = mode == 2 ? lrf * stepsz * mn : stepsz * mn;
-      const float old = g.data[slot];
       nv = old - num / (eps + sqrtf(vn));
       g.data[slot] = nv;
       if (zero_after) g.grad[slot] = 0.f;
@@ -181,28 +188,27 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
     ++n_act;
     const int64_t slot = int64_t(leaf) * kLeafVox + vox;
     float4* g4 = reinterpret_cast<float4*>(g.grad + slot * 12);
-    float gr[12];
+    float4* m4 = reinterpret_cast<float4*>(m + slot * 12);
+    float4* v4 = reinterpret_cast<float4*>(v + slot * 12);
+    float4* d4 = reinterpret_cast<float4*>(g.data + slot * 12);
+    // the voxel's gradient, TV terms, moments and values are loaded together
+    // (one round trip; most voxels of a touched leaf are updated)
+    float gr[12], tt[12], mm[12], vv[12], dd[12];
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      const float4 x = g4[b];
+      const float4 x = g4[b], t = tv ? reinterpret_cast<const float4*>(tv + slot * 12)[b]
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 a = m4[b], c = v4[b], d = d4[b];
       gr[4 * b] = x.x; gr[4 * b + 1] = x.y; gr[4 * b + 2] = x.z; gr[4 * b + 3] = x.w;
+      tt[4 * b] = t.x; tt[4 * b + 1] = t.y; tt[4 * b + 2] = t.z; tt[4 * b + 3] = t.w;
+      mm[4 * b] = a.x; mm[4 * b + 1] = a.y; mm[4 * b + 2] = a.z; mm[4 * b + 3] = a.w;
+      vv[4 * b] = c.x; vv[4 * b + 1] = c.y; vv[4 * b + 2] = c.z; vv[4 * b + 3] = c.w;
+      dd[4 * b] = d.x; dd[4 * b + 1] = d.y; dd[4 * b + 2] = d.z; dd[4 * b + 3] = d.w;
     }
     if (tv) {  // deferred sparse TV: its terms join the channels with a gradient
-      // (tv is given in mode 1 only: a voxel without a gradient is skipped
-      // below whatever its terms, so they are not read)
-      bool nz = false;
 #pragma unroll
-      for (int ch = 0; ch < 12; ++ch) nz = nz || gr[ch] != 0.f;
-      if (!nz) continue;
-      const float4* t4 = reinterpret_cast<const float4*>(tv + slot * 12);
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const float4 x = t4[b];
-        const float t[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (gr[4 * b + e] != 0.f) gr[4 * b + e] = gr[4 * b + e] + t[e];
-      }
+      for (int ch = 0; ch < 12; ++ch)
+        if (gr[ch] != 0.f) gr[ch] = gr[ch] + tt[ch];
     }
     bool live[4];
     bool any = false;
@@ -213,17 +219,6 @@ __global__ void k_vdb_adam_c12(GridView g, float* __restrict__ m, float* __restr
     }
     if (!any) continue;
     ++n_upd;
-    float4* m4 = reinterpret_cast<float4*>(m + slot * 12);
-    float4* v4 = reinterpret_cast<float4*>(v + slot * 12);
-    float4* d4 = reinterpret_cast<float4*>(g.data + slot * 12);
-    float mm[12], vv[12], dd[12];
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      const float4 a = m4[b], c = v4[b], d = d4[b];
-      mm[4 * b] = a.x; mm[4 * b + 1] = a.y; mm[4 * b + 2] = a.z; mm[4 * b + 3] = a.w;
-      vv[4 * b] = c.x; vv[4 * b + 1] = c.y; vv[4 * b + 2] = c.z; vv[4 * b + 3] = c.w;
-      dd[4 * b] = d.x; dd[4 * b + 1] = d.y; dd[4 * b + 2] = d.z; dd[4 * b + 3] = d.w;
-    }
     const float lrf = mode == 2 ? perlr[slot] : 1.f;
 #pragma unroll
     for (int ch = 0; ch < 12; ++ch) {

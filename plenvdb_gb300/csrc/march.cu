@@ -536,8 +536,11 @@ __global__ void __launch_bounds__(256)
 // goes straight into the row of its X tile ([k0 | PE | 1 | 0], BF16), so the
 // FP32 k0 rows are never written. pe: per-ray PE (pe_stride floats per ray).
 // The padding rows of the last tile are zero.
-template <int CT>
-__global__ void __launch_bounds__(256)
+// MINB: resident blocks per SM the register budget is cut for (2: 128
+// registers, no spills; 3: 80 registers with a few spilled values — faster
+// once the rows fill several waves).
+template <int CT, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     k_march_k0_x(GridView gk, MarchP P, MarchW W, const float* __restrict__ pe, int pe_stride,
                  int dpe, uint8_t* xt, const __nv_bfloat16* __restrict__ half) {
   grid_dep_sync();
@@ -1246,12 +1249,20 @@ int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t
   PVDB_REQUIRE(m->k0->C <= 16 && m->k0->C + dpe + 1 <= kRgbXK,
                "the tensor-core rgbnet takes at most 16 k0 and 47 input channels");
   const int grid = int(std::min<int64_t>(ceil_div(m->slots, 256), int64_t(num_sms()) * 16));
-  if (m->k0->C == 12)
-    launch_k(k_march_k0_x<12>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
-             half);
+  // The row count is on the device; the batch's ray count stands in for it:
+  // 2 blocks per SM for batches up to 32768 rays (a few waves of rows), 3
+  // beyond (65536 rays at 320^3: 384 against 402 us; 8192 rays at 160^3: 21.8
+  // against 20.0 us).
+  const bool many = m->n_rays > 32768;
+  if (m->k0->C == 12 && many)
+    launch_k(k_march_k0_x<12, 3>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe,
+             xt, half);
+  else if (m->k0->C == 12)
+    launch_k(k_march_k0_x<12, 2>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe,
+             xt, half);
   else
-    launch_k(k_march_k0_x<0>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe, xt,
-             nullptr);
+    launch_k(k_march_k0_x<0, 2>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe,
+             xt, nullptr);
   PVDB_CHECK_LAUNCH("k_march_k0_x");
   if (m->prof) prof_mark(st, 2);
   return PVDB_OK;

@@ -69,6 +69,13 @@ int pvdb_debug_fail_next_allocs(int count);
  * reports PVDB_ERR_TIMEOUT). Applies to launches made after the call (a
  * captured train-step graph keeps the values it was captured with). */
 int pvdb_debug_wait_limit(uint32_t spins, int32_t hold_first);
+/* Test hook (no counterpart in the reference): blocks = 2 or 3 forces the
+ * resident-blocks-per-SM variant of the BF16 train step's k0 gather (one
+ * source compiled for 128 or 80 registers a thread; the library takes 2 for
+ * batches up to 32768 rays and 3 above), 0 restores that choice. Both give
+ * bitwise identical results. Applies to launches made after the call (a
+ * captured train-step graph keeps the variant it was captured with). */
+int pvdb_debug_k0_blocks(int blocks);
 
 /* Stage profiler. Between begin and end, pvdb_train_step and
  * pvdb_renderer_render record CUDA events on their stream at stage boundaries

@@ -88,6 +88,7 @@ _SIGS = {
     "pvdb_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "pvdb_debug_fail_next_allocs": (C.c_int, [C.c_int]),
     "pvdb_debug_wait_limit": (C.c_int, [C.c_uint32, i32]),
+    "pvdb_debug_k0_blocks": (C.c_int, [C.c_int]),
     "pvdb_grid_touched_leaves": (C.c_int, [vp, C.POINTER(i64), vp]),
     "pvdb_profile_begin": (C.c_int, [i32]),
     "pvdb_profile_end": (C.c_int, [P_f32, i32, P_i32]),

@@ -22,6 +22,7 @@
 // per-voxel gather over the touched leaves then adds the density and k0
 // gradients deterministically (see the reduction below).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -1234,6 +1235,9 @@ int march_forward_impl(pvdb_march_s* m, pvdb_grid_s* density, pvdb_grid_s* k0, c
   return PVDB_OK;
 }
 
+// Test hook: forces the k0 gather's blocks-per-SM variant (0: automatic).
+static std::atomic<int> g_dbg_k0_blocks{0};
+
 // Backward, first part: the density-path gradients of every kept sample
 // (k_march_bwd) and the grouping of the kept samples by cell, which need only
 // the gradients w.r.t. the weights and alphainv_last — so it can run while
@@ -1253,7 +1257,8 @@ int march_k0_x(pvdb_march_s* m, const float* pe, int pe_stride, int dpe, uint8_t
   // 2 blocks per SM for batches up to 32768 rays (a few waves of rows), 3
   // beyond (65536 rays at 320^3: 384 against 402 us; 8192 rays at 160^3: 21.8
   // against 20.0 us).
-  const bool many = m->n_rays > 32768;
+  const int forced = g_dbg_k0_blocks.load();
+  const bool many = forced ? forced == 3 : m->n_rays > 32768;
   if (m->k0->C == 12 && many)
     launch_k(k_march_k0_x<12, 3>, grid, 256, 0, st, m->k0->view(), m->p, m->w, pe, pe_stride, dpe,
              xt, half);
@@ -1406,6 +1411,13 @@ int composite_backward_impl(pvdb_march_s* m, const float* rgb, const float* g, f
 using namespace pvdb;
 
 extern "C" {
+
+int pvdb_debug_k0_blocks(int blocks) {
+  clear_error();
+  PVDB_REQUIRE(blocks == 0 || blocks == 2 || blocks == 3, "blocks must be 0, 2 or 3");
+  g_dbg_k0_blocks.store(blocks);
+  return PVDB_OK;
+}
 
 int32_t pvdb_march_samples_cap(const float xyz_min[3], const float xyz_max[3], float stepdist) {
   if (!xyz_min || !xyz_max || !(stepdist > 0.f)) return 0;

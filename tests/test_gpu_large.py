@@ -1,8 +1,9 @@
 """The training step at full size — a 320^3 sparse grid (32 ellipsoids plus a
 thin shell) with 65536 rays per step, BF16 — checked through size-independent
 properties: the CUDA-graph replay equals eager launches bitwise, two runs are
-bitwise identical, the loss decreases, and the kept-sample and colour-row
-counts stay within the workspace."""
+bitwise identical, the loss decreases, the kept-sample and colour-row
+counts stay within the workspace, and the k0 gather's two register variants
+(3 resident blocks per SM, taken at this batch size, and 2) agree bitwise."""
 import numpy as np
 import pytest
 
@@ -25,14 +26,19 @@ def large(lib):
     return scfg, batches
 
 
-def _run(scfg, batches, use_graph, steps=6):
+def _run(scfg, batches, use_graph, steps=6, k0_blocks=0):
     import torch
+    from plenvdb_gb300 import _lib as L
     from plenvdb_gb300.scene import build_grids, rgbnet_init
     from plenvdb_gb300.trainer import FineStageConfig, FineStageTrainer
     cfg = FineStageConfig(reso=RESO, precision=1, use_graph=use_graph)
     dg, kg = build_grids(scfg)
     tr = FineStageTrainer(dg, kg, rgbnet_init(seed=2), cfg, max_rays=RAYS)
-    losses = [float(tr.step(*batches[i % 2])) for i in range(steps)]
+    L.call("pvdb_debug_k0_blocks", k0_blocks)
+    try:
+        losses = [float(tr.step(*batches[i % 2])) for i in range(steps)]
+    finally:
+        L.call("pvdb_debug_k0_blocks", 0)
     kept, rows, evaluated = tr.ws.stats()
     torch.cuda.synchronize()
     out = dict(losses=losses, density=dg.get_dense_grid(device=True).cpu().numpy(),
@@ -49,9 +55,10 @@ def test_large_step_graph_equals_eager_and_deterministic(large):
     a = _run(scfg, batches, use_graph=True)
     b = _run(scfg, batches, use_graph=True)
     c = _run(scfg, batches, use_graph=False)
+    d = _run(scfg, batches, use_graph=True, k0_blocks=2)
     assert a["kept"] > 1_000_000 and 0 < a["rows"] <= a["kept"] <= a["evaluated"]
     assert a["kept"] <= a["slots"]
-    for x in (b, c):
+    for x in (b, c, d):
         assert x["losses"] == a["losses"]
         for key in ("density", "k0", "params"):
             assert np.array_equal(x[key], a[key]), key
